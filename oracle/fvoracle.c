@@ -1,0 +1,824 @@
+/* CPU oracle: plain-C restatement of the reference's CPU implementation of the
+ * explicit finite-volume step (alsfvm) and of the mean/variance statistics and
+ * the uniform sample generator (alsuq).
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE: only tests/, the smoke check and the
+ * CPU-baseline leg of bench.py load this library, as the checker.
+ *
+ * Build with -ffp-contract=off and without fast-math: every expression below
+ * keeps the reference's operand order so that results are bit-identical to the
+ * reference compiled the same way, on x86-64 and on aarch64.
+ * Parity is pinned against the reference itself (oracle/refbuild builds the
+ * unmodified reference sources) and against the fixtures in tests/golden/. */
+#include "fvoracle.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static __thread char g_err[512];
+
+static int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+const char* fv_last_error(void) { return g_err; }
+
+void fv_set_threads(int n) {
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
+
+int fv_get_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ names */
+
+enum { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3 };
+enum { FL_HLL, FL_HLL3, FL_GODUNOV };
+enum { RC_NONE, RC_WENO2, RC_ENO2, RC_ENO3, RC_ENO4 };
+enum { IN_FE, IN_RK2, IN_RK3 };
+enum { BC_NEUMANN, BC_PERIODIC };
+
+static int parse_eq(const char* s) {
+    if (!strcmp(s, "burgers")) return EQ_BURGERS;
+    if (!strcmp(s, "euler1")) return EQ_EULER1;
+    if (!strcmp(s, "euler2")) return EQ_EULER2;
+    if (!strcmp(s, "euler3")) return EQ_EULER3;
+    return -1;
+}
+static int parse_flux(const char* s) {
+    if (!strcmp(s, "hll")) return FL_HLL;
+    if (!strcmp(s, "hll3")) return FL_HLL3;
+    if (!strcmp(s, "godunov")) return FL_GODUNOV;
+    return -1;
+}
+static int parse_recon(const char* s) {
+    if (!strcmp(s, "none")) return RC_NONE;
+    if (!strcmp(s, "weno2")) return RC_WENO2;
+    if (!strcmp(s, "eno2")) return RC_ENO2;
+    if (!strcmp(s, "eno3")) return RC_ENO3;
+    if (!strcmp(s, "eno4")) return RC_ENO4;
+    return -1;
+}
+static int parse_integrator(const char* s) {
+    if (!strcmp(s, "forwardeuler")) return IN_FE;
+    if (!strcmp(s, "rungekutta2")) return IN_RK2;
+    if (!strcmp(s, "rungekutta3")) return IN_RK3;
+    return -1;
+}
+static int parse_bc(const char* s) {
+    if (!strcmp(s, "neumann")) return BC_NEUMANN;
+    if (!strcmp(s, "periodic")) return BC_PERIODIC;
+    return -1;
+}
+
+/* Reconstruction ghost width: none 1, weno2 2, enoK K
+ * (alsfvm/src/reconstruction/NoReconstruction.cpp:71-73, WENO2.hpp:93-95,
+ * ENOCPU.cpp:180-183); the two-point flux stencil needs 1. */
+static int recon_ghosts(int rc) {
+    switch (rc) {
+        case RC_NONE: return 1;
+        case RC_WENO2: return 2;
+        case RC_ENO2: return 2;
+        case RC_ENO3: return 3;
+        case RC_ENO4: return 4;
+    }
+    return -1;
+}
+
+int fv_ghost_cells(const char* recon) {
+    int rc = parse_recon(recon);
+    if (rc < 0) return fail(-1, "unknown reconstruction %s", recon);
+    return recon_ghosts(rc);
+}
+
+/* ------------------------------------------------------------------ grid */
+
+typedef struct {
+    int eq, nsd, nvar, dim;
+    int n[3], g[3], t[3];
+    long total;
+    double gamma;
+} grid_t;
+
+static int nvar_of(int eq) { return eq == EQ_BURGERS ? 1 : eq + 2; }
+
+/* Ghost cells exist only in active dimensions (alsfvm/src/volume/Volume.cpp:52-53). */
+static void make_grid(grid_t* G, int eq, const int n[3], int ghosts, double gamma) {
+    G->eq = eq;
+    G->nsd = eq == EQ_BURGERS ? 1 : eq;
+    G->nvar = nvar_of(eq);
+    G->dim = n[2] > 1 ? 3 : (n[1] > 1 ? 2 : 1);
+    for (int d = 0; d < 3; ++d) {
+        G->n[d] = n[d];
+        G->g[d] = d < G->dim ? ghosts : 0;
+        G->t[d] = n[d] + 2 * G->g[d];
+    }
+    G->total = (long)G->t[0] * G->t[1] * G->t[2];
+    G->gamma = gamma;
+}
+
+static inline long IDX(const grid_t* G, long x, long y, long z) {
+    return (z * G->t[1] + y) * G->t[0] + x;
+}
+
+/* ------------------------------------------------------------- equations */
+
+typedef struct {
+    double rho, m[3], E, p, u[3];
+} euler_all;
+
+/* Euler<nsd>::computeExtra: ie = E - 0.5 m.m / rho; u = m / rho;
+ * p = (gamma - 1) ie (alsfvm/include/alsfvm/equation/euler/Euler.hpp:204-211). */
+static inline void euler_fetch(euler_all* a, const double* U, long total, long i, int nsd,
+                               double gamma) {
+    a->rho = U[i];
+    for (int k = 0; k < nsd; ++k) a->m[k] = U[(1 + k) * total + i];
+    a->E = U[(1 + nsd) * total + i];
+    double dot = a->m[0] * a->m[0]; /* nsd >= 1 */
+    for (int k = 1; k < nsd; ++k) dot = dot + a->m[k] * a->m[k];
+    const double ie = a->E - 0.5 * dot / a->rho;
+    for (int k = 0; k < nsd; ++k) a->u[k] = a->m[k] / a->rho;
+    a->p = (gamma - 1) * ie;
+}
+
+/* Euler<nsd>::computePointFlux (Euler.hpp:172-181). F has nsd+2 entries. */
+static inline void euler_point_flux(const euler_all* a, int d, int nsd, double* F) {
+    F[0] = a->m[d];
+    for (int k = 0; k < nsd; ++k) F[1 + k] = a->u[d] * a->m[k];
+    F[1 + d] += a->p;
+    F[1 + nsd] = (a->E + a->p) * a->u[d];
+}
+
+static inline void euler_conserved(const euler_all* a, int nsd, double* c) {
+    c[0] = a->rho;
+    for (int k = 0; k < nsd; ++k) c[1 + k] = a->m[k];
+    c[1 + nsd] = a->E;
+}
+
+/* HLL3<nsd>::computeFlux + computeHLLSpeeds
+ * (alsfvm/include/alsfvm/numflux/euler/HLL3.hpp:52-148). */
+static double flux_hll3(const euler_all* L, const euler_all* R, int d, int nsd, double gamma,
+                        double* F) {
+    const double waveLeft = sqrt(L->rho);
+    const double waveRight = sqrt(R->rho);
+    const double rho = (L->rho + R->rho) / 2;
+    const double ud = (waveLeft * L->u[d] + waveRight * R->u[d]) / (waveLeft + waveRight);
+    const double p = (waveLeft * L->p + waveRight * R->p) / (waveLeft + waveRight);
+    const double cfLeft = sqrt(gamma * L->p / L->rho);
+    const double cfRight = sqrt(gamma * R->p / R->rho);
+    const double correct = 0.5 * fmax(0.0, L->u[d] - R->u[d]);
+    const double cs = sqrt(gamma * p / rho);
+    const double speedLeft = fmin(L->u[d] + correct - cfLeft, ud - cs);
+    const double speedRight = fmax(R->u[d] - correct + cfRight, ud + cs);
+
+    double fluxLeft[5], fluxRight[5];
+    euler_point_flux(L, d, nsd, fluxLeft);
+    euler_point_flux(R, d, nsd, fluxRight);
+    const double pressureLeft = L->p, pressureRight = R->p;
+    const double udl = L->u[d] - speedLeft;
+    const double udr = R->u[d] - speedRight;
+    const double aa = udr * R->rho - udl * L->rho;
+    const double sm = (R->m[d] * udr - L->m[d] * udl + pressureRight - pressureLeft) / aa;
+    double us[3];
+    for (int k = 0; k < nsd; ++k)
+        us[k] = (fluxRight[1 + k] - fluxLeft[1 + k] - speedRight * R->m[k] + speedLeft * L->m[k]) / aa;
+    us[d] = sm;
+    const int nv = nsd + 2;
+    if (speedLeft == 0) {
+        for (int k = 0; k < nv; ++k) F[k] = 0;
+    } else if (speedLeft > 0) {
+        for (int k = 0; k < nv; ++k) F[k] = fluxLeft[k];
+    } else if (speedRight < 0) {
+        for (int k = 0; k < nv; ++k) F[k] = fluxRight[k];
+    } else if (sm >= 0) {
+        double mid[5], c[5];
+        mid[0] = L->rho * udl / (sm - speedLeft);
+        for (int k = 0; k < nsd; ++k) mid[1 + k] = mid[0] * us[k];
+        const double pp = pressureLeft + L->rho * (L->u[d] - sm) * udl;
+        mid[1 + nsd] = (udl * L->E + pressureLeft * L->u[d] - pp * sm) / (sm - speedLeft);
+        euler_conserved(L, nsd, c);
+        for (int k = 0; k < nv; ++k) F[k] = fluxLeft[k] + speedLeft * (mid[k] - c[k]);
+    } else {
+        double mid[5], c[5];
+        mid[0] = R->rho * udr / (sm - speedRight);
+        for (int k = 0; k < nsd; ++k) mid[1 + k] = mid[0] * us[k];
+        const double pp = pressureRight + R->rho * (R->u[d] - sm) * udr;
+        mid[1 + nsd] = (udr * R->E + pressureRight * R->u[d] - pp * sm) / (sm - speedRight);
+        euler_conserved(R, nsd, c);
+        for (int k = 0; k < nv; ++k) F[k] = fluxRight[k] + speedRight * (mid[k] - c[k]);
+    }
+    return fmax(fabs(speedLeft), fabs(speedRight));
+}
+
+/* HLL<nsd>::computeFlux + computeHLLSpeeds
+ * (alsfvm/include/alsfvm/numflux/euler/HLL.hpp:51-115). */
+static double flux_hll(const euler_all* L, const euler_all* R, int d, int nsd, double gamma,
+                       double* F) {
+    const double waveLeft = sqrt(L->rho);
+    const double waveRight = sqrt(R->rho);
+    const double rho = (L->rho + R->rho) / 2;
+    const double ud = (waveLeft * L->u[d] + waveRight * R->u[d]) / (waveLeft + waveRight);
+    const double p = (L->p * waveLeft + R->p * waveRight) / (waveLeft + waveRight);
+    const double cs = sqrt(gamma * p / rho);
+    const double speedLeft = fmin(L->u[d] - sqrt(gamma * L->p / L->rho), ud - cs);
+    const double speedRight = fmax(R->u[d] + sqrt(gamma * R->p / R->rho), ud + cs);
+    const int nv = nsd + 2;
+    if (speedLeft == 0) {
+        for (int k = 0; k < nv; ++k) F[k] = 0;
+    } else if (speedLeft > 0) {
+        euler_point_flux(L, d, nsd, F);
+    } else if (speedRight < 0) {
+        euler_point_flux(R, d, nsd, F);
+    } else {
+        double fl[5], fr[5], cl[5], cr[5];
+        euler_point_flux(L, d, nsd, fl);
+        euler_point_flux(R, d, nsd, fr);
+        euler_conserved(L, nsd, cl);
+        euler_conserved(R, nsd, cr);
+        for (int k = 0; k < nv; ++k)
+            F[k] = (speedRight * fl[k] - speedLeft * fr[k] + speedRight * speedLeft * (cr[k] - cl[k])) /
+                   (speedRight - speedLeft);
+    }
+    return fmax(fabs(speedLeft), fabs(speedRight));
+}
+
+/* burgers::Godunov: F = max(f(max(uL,0)), f(min(uR,0))), f(u) = u*u/2; wave
+ * speed max(|uL|,|uR|) (alsfvm/include/alsfvm/numflux/burgers/Godunov.hpp:40-60,
+ * alsfvm/include/alsfvm/equation/burgers/Burgers.hpp:135-139). */
+static double flux_godunov(double uL, double uR, double* F) {
+    const double a = fmax(uL, 0.0);
+    const double b = fmin(uR, 0.0);
+    const double fl = a * a / 2;
+    const double fr = b * b / 2;
+    F[0] = fmax(fl, fr);
+    return fmax(fabs(uL), fabs(uR));
+}
+
+/* -------------------------------------------------------- reconstruction */
+
+/* ENO reconstruction coefficients, row r gives the value at the cell's
+ * left face for stencil shift r (row r+1 the right face); the standard
+ * uniform-grid ENO table (alsfvm/src/reconstruction/ENOCoefficients.cpp:21-49). */
+static const double ENO2C[3][2] = {{3.0 / 2.0, -1.0 / 2.0}, {1.0 / 2.0, 1.0 / 2.0}, {-1.0 / 2.0, 3.0 / 2.0}};
+static const double ENO3C[4][3] = {{11.0 / 6.0, -7.0 / 6.0, 1.0 / 3.0},
+                                   {1.0 / 3.0, 5.0 / 6.0, -1.0 / 6.0},
+                                   {-1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0},
+                                   {1.0 / 3.0, -7.0 / 6.0, 11.0 / 6.0}};
+static const double ENO4C[5][4] = {{25.0 / 12.0, -23.0 / 12.0, 13.0 / 12.0, -1.0 / 4.0},
+                                   {1.0 / 4.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0},
+                                   {-1.0 / 12.0, 7.0 / 12.0, 7.0 / 12.0, -1.0 / 12.0},
+                                   {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 1.0 / 4.0},
+                                   {-1.0 / 4.0, 13.0 / 12.0, -23.0 / 12.0, 25.0 / 12.0}};
+
+#define WENO_EPSILON 1e-8 /* alsfvm/include/alsfvm/reconstruction/WENOCoefficients.hpp:21 */
+
+/* Reconstructs cells [g-1, n-g+1) in the active direction and the interior in
+ * the other directions (ReconstructionCPU.cpp:37-97, ENOCPU.cpp:41-171). The
+ * weight / stencil-indicator variable is variable 0 (rho for Euler, u for
+ * Burgers: Euler.hpp:286-288, Burgers.hpp:225-227). */
+static void reconstruct(const grid_t* G, int rc, int dir, const double* U, double* left,
+                        double* right) {
+    const long total = G->total;
+    const int nvar = G->nvar;
+    const int dx = dir == 0, dy = dir == 1, dz = dir == 2;
+    const long stride = dir == 0 ? 1 : (dir == 1 ? G->t[0] : (long)G->t[0] * G->t[1]);
+    const int ng = recon_ghosts(rc);
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const int act = d == dir;
+        lo[d] = G->g[d] - act;
+        hi[d] = G->t[d] - G->g[d] + act;
+    }
+    (void)ng;
+    if (rc == RC_NONE) {
+        /* NoReconstruction copies every cell (NoReconstruction.cpp:52-64). */
+        for (int v = 0; v < nvar; ++v) {
+            memcpy(left + v * total, U + v * total, total * sizeof(double));
+            memcpy(right + v * total, U + v * total, total * sizeof(double));
+        }
+        return;
+    }
+    (void)dx; (void)dy; (void)dz;
+    for (int z = lo[2]; z < hi[2]; ++z) {
+#pragma omp parallel for schedule(static)
+        for (int y = lo[1]; y < hi[1]; ++y) {
+            for (int x = lo[0]; x < hi[0]; ++x) {
+                const long i = IDX(G, x, y, z);
+                if (rc == RC_WENO2) {
+                    /* WENO2::reconstruct (alsfvm/include/alsfvm/reconstruction/WENO2.hpp:31-91) */
+                    const long il = i - stride, ir = i + stride;
+                    const double i0 = U[i];
+                    const double d0 = U[ir] - i0;
+                    const double d1 = i0 - U[il];
+                    const double b0 = d0 * d0;
+                    const double b1 = d1 * d1;
+                    const double a0Left = 1 / (3 * (WENO_EPSILON + b0) * (WENO_EPSILON + b0));
+                    const double a1Left = 2 / (3 * (WENO_EPSILON + b1) * (WENO_EPSILON + b1));
+                    const double w0Left = a0Left / (a0Left + a1Left);
+                    const double w1Left = a1Left / (a0Left + a1Left);
+                    const double a0Right = 2 / (3 * (WENO_EPSILON + b0) * (WENO_EPSILON + b0));
+                    const double a1Right = 1 / (3 * (WENO_EPSILON + b1) * (WENO_EPSILON + b1));
+                    const double w0Right = a0Right / (a0Right + a1Right);
+                    const double w1Right = a1Right / (a0Right + a1Right);
+                    for (int v = 0; v < nvar; ++v) {
+                        const double* u = U + v * total;
+                        left[v * total + i] =
+                            0.5 * (w1Left * u[il] + (3 * w0Left + w1Left) * u[i] - w0Left * u[ir]);
+                        right[v * total + i] =
+                            0.5 * (w0Right * u[ir] + (3 * w1Right + w0Right) * u[i] - w1Right * u[il]);
+                    }
+                } else {
+                    /* ENOCPU<order>::performReconstruction: undivided differences of
+                     * variable 0 up to order-1 levels; at each level the shift grows
+                     * when |left difference| < |right difference|. */
+                    const int order = rc == RC_ENO2 ? 2 : (rc == RC_ENO3 ? 3 : 4);
+                    double w[9];
+                    for (int k = -(order - 1); k <= order - 1; ++k) w[k + order - 1] = U[i + k * stride];
+                    /* dd[level][j] for j = offset - (order-1) .. covering cells i-1, i */
+                    double dd[3][9];
+                    const int c = order - 1; /* position of cell i in w[] */
+                    for (int j = 0; j + 1 < 2 * order - 1; ++j) dd[0][j] = w[j + 1] - w[j];
+                    for (int l = 1; l < order - 1; ++l)
+                        for (int j = 0; j + 1 + l < 2 * order - 1; ++j) dd[l][j] = dd[l - 1][j + 1] - dd[l - 1][j];
+                    int shift = 0;
+                    for (int l = 0; l < order - 1; ++l) {
+                        const double ddRight = dd[l][c];
+                        const double ddLeft = dd[l][c - 1];
+                        if (fabs(ddLeft) < fabs(ddRight)) shift++;
+                    }
+                    const double* cL;
+                    const double* cR;
+                    if (order == 2) { cL = ENO2C[shift]; cR = ENO2C[shift + 1]; }
+                    else if (order == 3) { cL = ENO3C[shift]; cR = ENO3C[shift + 1]; }
+                    else { cL = ENO4C[shift]; cR = ENO4C[shift + 1]; }
+                    for (int v = 0; v < nvar; ++v) {
+                        const double* u = U + v * total;
+                        double leftValue = 0.0, rightValue = 0.0;
+                        for (int j = 0; j < order; ++j) {
+                            const double value = u[i - (long)(shift - j) * stride];
+                            leftValue += cL[j] * value;
+                            rightValue += cR[j] * value;
+                        }
+                        left[v * total + i] = leftValue;
+                        right[v * total + i] = rightValue;
+                    }
+                }
+            }
+        }
+    }
+}
+
+int fv_reconstruct(const char* equation, const char* recon, const int n[3], double gamma,
+                   int direction, const double* U, double* left, double* right) {
+    const int eq = parse_eq(equation), rc = parse_recon(recon);
+    if (eq < 0 || rc < 0) return fail(-1, "bad equation/reconstruction");
+    grid_t G;
+    make_grid(&G, eq, n, recon_ghosts(rc), gamma);
+    if (direction < 0 || direction >= G.dim) return fail(-1, "bad direction %d", direction);
+    reconstruct(&G, rc, direction, U, left, right);
+    return 0;
+}
+
+/* -------------------------------------------------------------- net flux */
+
+/* computeNetFlux<Flux, Equation, direction> (alsfvm/src/numflux/NumericalFluxCPU.cpp:
+ * 32-118): face x between cells x and x+1 for x in [ng-1, n-ng) stores -F into
+ * temp; then out[x+1] += temp[x+1] + (-temp[x]). Returns the maximum face speed. */
+static double net_flux(const grid_t* G, int fl, int dir, const double* left, const double* right,
+                       double* out, double* temp) {
+    const long total = G->total;
+    const int nvar = G->nvar, nsd = G->nsd;
+    const long stride = dir == 0 ? 1 : (dir == 1 ? G->t[0] : (long)G->t[0] * G->t[1]);
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const int act = d == dir;
+        lo[d] = G->g[d] - act;
+        hi[d] = G->t[d] - G->g[d];
+    }
+    double ws = 0;
+    for (int z = lo[2]; z < hi[2]; ++z) {
+        double wsz = 0;
+#pragma omp parallel for schedule(static) reduction(max : wsz)
+        for (int y = lo[1]; y < hi[1]; ++y) {
+            for (int x = lo[0]; x < hi[0]; ++x) {
+                const long i = IDX(G, x, y, z);
+                double F[5];
+                double wl;
+                if (G->eq == EQ_BURGERS) {
+                    wl = flux_godunov(right[i], left[i + stride], F);
+                } else {
+                    euler_all A, B;
+                    euler_fetch(&A, right, total, i, nsd, G->gamma);
+                    euler_fetch(&B, left, total, i + stride, nsd, G->gamma);
+                    wl = fl == FL_HLL3 ? flux_hll3(&A, &B, dir, nsd, G->gamma, F)
+                                       : flux_hll(&A, &B, dir, nsd, G->gamma, F);
+                }
+                for (int v = 0; v < nvar; ++v) temp[v * total + i] = (-1.0) * F[v];
+                wsz = (wsz < wl) ? wl : wsz; /* std::max */
+            }
+        }
+        ws = (ws < wsz) ? wsz : ws;
+    }
+    for (int d = 0; d < 3; ++d) hi[d] -= d == dir;
+    for (int z = lo[2]; z < hi[2]; ++z) {
+#pragma omp parallel for schedule(static)
+        for (int y = lo[1]; y < hi[1]; ++y) {
+            for (int x = lo[0]; x < hi[0]; ++x) {
+                const long i = IDX(G, x, y, z);
+                for (int v = 0; v < nvar; ++v) {
+                    const double fmr = temp[v * total + i + stride];
+                    const double flm = (-1.0) * temp[v * total + i];
+                    out[v * total + i + stride] += fmr + flm;
+                }
+            }
+        }
+    }
+    return ws;
+}
+
+typedef struct {
+    grid_t G;
+    int fl, rc;
+    double *left, *right, *temp;
+} flux_ctx;
+
+static int flux_ctx_init(flux_ctx* c, int eq, int fl, int rc, const int n[3], double gamma) {
+    make_grid(&c->G, eq, n, recon_ghosts(rc), gamma);
+    c->fl = fl;
+    c->rc = rc;
+    const size_t bytes = (size_t)c->G.nvar * c->G.total * sizeof(double);
+    c->left = (double*)calloc(1, bytes);
+    c->right = (double*)calloc(1, bytes);
+    c->temp = (double*)calloc(1, bytes);
+    if (!c->left || !c->right || !c->temp) return fail(-3, "out of host memory");
+    return 0;
+}
+
+static void flux_ctx_free(flux_ctx* c) {
+    free(c->left);
+    free(c->right);
+    free(c->temp);
+}
+
+/* NumericalFluxCPU::computeFlux over the whole domain (makeZero, then per
+ * direction reconstruct + net flux; alsfvm/src/numflux/NumericalFluxCPU.cpp:
+ * 170-221). ConservedSystem's interior + side-strip calls cover the same faces
+ * and cells, so the result equals a single whole-domain call. */
+static void compute_flux(flux_ctx* c, const double* U, double* out, double ws[3]) {
+    const grid_t* G = &c->G;
+    const long total = G->total;
+    for (int z = G->g[2]; z < G->t[2] - G->g[2]; ++z) {
+#pragma omp parallel for schedule(static)
+        for (int y = G->g[1]; y < G->t[1] - G->g[1]; ++y)
+            for (int x = G->g[0]; x < G->t[0] - G->g[0]; ++x)
+                for (int v = 0; v < G->nvar; ++v) out[v * total + IDX(G, x, y, z)] = 0;
+    }
+    ws[0] = ws[1] = ws[2] = 0;
+    for (int d = 0; d < G->dim; ++d) {
+        reconstruct(G, c->rc, d, U, c->left, c->right);
+        ws[d] = net_flux(G, c->fl, d, c->left, c->right, out, c->temp);
+    }
+}
+
+int fv_compute_flux(const char* equation, const char* flux, const char* recon, const int n[3],
+                    double gamma, const double* U, double* out, double ws[3]) {
+    const int eq = parse_eq(equation), fl = parse_flux(flux), rc = parse_recon(recon);
+    if (eq < 0 || fl < 0 || rc < 0) return fail(-1, "bad equation/flux/reconstruction");
+    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV)) return fail(-1, "flux %s not for %s", flux, equation);
+    flux_ctx c;
+    int r = flux_ctx_init(&c, eq, fl, rc, n, gamma);
+    if (r == 0) compute_flux(&c, U, out, ws);
+    flux_ctx_free(&c);
+    return r;
+}
+
+/* -------------------------------------------------------------- boundary */
+
+/* BoundaryCPU<Neumann|Periodic>::applyBoundaryConditions
+ * (alsfvm/src/boundary/BoundaryCPU.cpp:30-106): per variable, per dimension,
+ * bottom then top side, over every cell of the other dimensions (ghosts
+ * included). Neumann ghost k copies interior k-1 from the edge (a mirror,
+ * Neumann.hpp:24-35); periodic copies from the opposite side (Periodic.hpp:24-42). */
+static void apply_boundary(const grid_t* G, int bc, double* U) {
+    const long total = G->total;
+    for (int v = 0; v < G->nvar; ++v) {
+        double* u = U + v * total;
+        for (int d = 0; d < G->dim; ++d) {
+            const int ng = G->g[d];
+            const long stride = d == 0 ? 1 : (d == 1 ? G->t[0] : (long)G->t[0] * G->t[1]);
+            const int nint = G->t[d] - 2 * ng;
+            for (int side = 0; side < 2; ++side) {
+                const int sign = side == 1 ? -1 : 1;
+                const int edge = side == 0 ? ng : G->t[d] - ng - 1;
+                int lo[3] = {0, 0, 0}, hi[3] = {G->t[0], G->t[1], G->t[2]};
+                lo[d] = edge;
+                hi[d] = edge + 1;
+                for (int z = lo[2]; z < hi[2]; ++z)
+                    for (int y = lo[1]; y < hi[1]; ++y)
+                        for (int x = lo[0]; x < hi[0]; ++x) {
+                            const long i = IDX(G, x, y, z);
+                            for (int k = 1; k <= ng; ++k) {
+                                const long dst = i - (long)sign * k * stride;
+                                const long src = bc == BC_NEUMANN ? i + (long)sign * (k - 1) * stride
+                                                                  : i + (long)sign * (nint - k) * stride;
+                                u[dst] = u[src];
+                            }
+                        }
+            }
+        }
+    }
+}
+
+int fv_boundary(const char* boundary, const int n[3], int ghosts, int nvar, double* U) {
+    const int bc = parse_bc(boundary);
+    if (bc < 0) return fail(-1, "unknown boundary %s", boundary);
+    grid_t G;
+    make_grid(&G, nvar == 1 ? EQ_BURGERS : nvar - 2, n, ghosts, 1.4);
+    for (int d = 0; d < G.dim; ++d)
+        if (G.t[d] < 2 * ghosts) return fail(-1, "too few cells for the boundary");
+    apply_boundary(&G, bc, U);
+    return 0;
+}
+
+/* ----------------------------------------------------------- cell ops */
+
+/* Euler<nsd>::computeConserved: m = rho u, E = p/(gamma-1) + 0.5 rho u.u
+ * (Euler.hpp:236-245); Burgers copies u. Primitive order (rho, u..., p). */
+int fv_prim_to_cons(const char* equation, const int n[3], int ghosts, double gamma,
+                    const double* prim, double* cons) {
+    const int eq = parse_eq(equation);
+    if (eq < 0) return fail(-1, "unknown equation %s", equation);
+    grid_t G;
+    make_grid(&G, eq, n, ghosts, gamma);
+    const long total = G.total;
+    const int nsd = G.nsd;
+    for (long i = 0; i < total; ++i) {
+        if (eq == EQ_BURGERS) {
+            cons[i] = prim[i];
+            continue;
+        }
+        const double rho = prim[i];
+        double u[3], dot;
+        for (int k = 0; k < nsd; ++k) u[k] = prim[(1 + k) * total + i];
+        const double p = prim[(1 + nsd) * total + i];
+        dot = u[0] * u[0];
+        for (int k = 1; k < nsd; ++k) dot = dot + u[k] * u[k];
+        cons[i] = rho;
+        for (int k = 0; k < nsd; ++k) cons[(1 + k) * total + i] = u[k] * rho;
+        cons[(1 + nsd) * total + i] = p / (gamma - 1) + 0.5 * rho * dot;
+    }
+    return 0;
+}
+
+/* CPUCellComputer::obeysConstraints: every cell, ghosts included, has finite
+ * conserved and extra variables, rho > 0 and p > 0 (Euler) or finite u
+ * (Burgers) (alsfvm/src/equation/CPUCellComputer.cpp:79-125, Euler.hpp:269-277). */
+static int obeys(const grid_t* G, const double* U) {
+    const long total = G->total;
+    int ok = 1;
+#pragma omp parallel for schedule(static) reduction(&& : ok)
+    for (long i = 0; i < total; ++i) {
+        if (G->eq == EQ_BURGERS) {
+            const double u = U[i];
+            ok = ok && isfinite(u);
+            continue;
+        }
+        euler_all a;
+        euler_fetch(&a, U, total, i, G->nsd, G->gamma);
+        int c = isfinite(a.rho) && isfinite(a.E) && isfinite(a.p);
+        for (int k = 0; k < G->nsd; ++k) c = c && isfinite(a.m[k]) && isfinite(a.u[k]);
+        c = c && a.rho > 0 && a.p > 0;
+        ok = ok && c;
+    }
+    return ok;
+}
+
+int fv_obeys_constraints(const char* equation, const int n[3], int ghosts, double gamma,
+                         const double* U) {
+    const int eq = parse_eq(equation);
+    if (eq < 0) return fail(-1, "unknown equation %s", equation);
+    grid_t G;
+    make_grid(&G, eq, n, ghosts, gamma);
+    return obeys(&G, U);
+}
+
+/* ------------------------------------------------------------ simulation */
+
+/* Simulator::performStep / incrementSolution (alsfvm/src/simulator/Simulator.cpp:
+ * 81-85, 191-214) with RungeKutta3/RungeKutta2/ForwardEuler::performSubstep
+ * (alsfvm/src/integrator/RungeKutta3.cpp:49-86, RungeKutta2.cpp:37-67,
+ * ForwardEuler.cpp:32-51), Integrator::computeTimestep (Integrator.cpp:20-46),
+ * the FixedIntervalWriter dt clamp (alsfvm/src/io/FixedIntervalWriter.cpp:
+ * 45-53), Grid cell lengths (alsfvm/src/grid/Grid.cpp:24-42) and the
+ * constraint check after every step. */
+int fv_run(const char* equation, const char* flux, const char* recon, const char* integrator,
+           const char* boundary, const int n[3], const double lower[3], const double upper[3],
+           double gamma, double cfl, double end_time, int number_of_saves, int max_steps,
+           const double* prim, double* out, double* t_out, int* steps_out, double* dts,
+           int max_dts) {
+    const int eq = parse_eq(equation), fl = parse_flux(flux), rc = parse_recon(recon);
+    const int in = parse_integrator(integrator), bc = parse_bc(boundary);
+    if (eq < 0 || fl < 0 || rc < 0 || in < 0 || bc < 0) return fail(-1, "bad configuration name");
+    flux_ctx c;
+    int r = flux_ctx_init(&c, eq, fl, rc, n, gamma);
+    if (r) { flux_ctx_free(&c); return r; }
+    const grid_t* G = &c.G;
+    const long total = G->total;
+    const int nvar = G->nvar;
+    const int nsub = in == IN_FE ? 1 : (in == IN_RK2 ? 2 : 3);
+    double* U[4];
+    double* primPad = (double*)calloc((size_t)nvar * total, sizeof(double));
+    for (int s = 0; s <= nsub; ++s) U[s] = (double*)calloc((size_t)nvar * total, sizeof(double));
+
+    /* initial data: interior primitives -> padded primitive volume -> conserved
+     * over every cell (CPUCellComputer::computeFromPrimitive, CPUCellComputer.cpp:
+     * 127-140), then the boundary (Simulator.cpp:117-162). */
+    const long cells = (long)n[0] * n[1] * n[2];
+    for (int v = 0; v < nvar; ++v)
+        for (int z = 0; z < n[2]; ++z)
+            for (int y = 0; y < n[1]; ++y)
+                for (int x = 0; x < n[0]; ++x)
+                    primPad[v * total + IDX(G, x + G->g[0], y + G->g[1], z + G->g[2])] =
+                        prim[v * cells + ((long)z * n[1] + y) * n[0] + x];
+    int gh = G->g[0];
+    fv_prim_to_cons(equation, n, gh, gamma, primPad, U[0]);
+    apply_boundary(G, bc, U[0]);
+
+    double cellLengths[3];
+    for (int d = 0; d < 3; ++d) cellLengths[d] = (upper[d] - lower[d]) / n[d];
+    if (n[1] == 1) cellLengths[1] = 1;
+    if (n[2] == 1) cellLengths[2] = 1;
+
+    const double timeInterval = number_of_saves > 0 ? end_time / number_of_saves : 0;
+    long numberSaved = 1;
+    double t = 0;
+    int steps = 0;
+    while (!(t >= end_time) && (max_steps <= 0 || steps < max_steps)) {
+        double dt = 0;
+        for (int s = 0; s < nsub; ++s) {
+            double* o = U[s + 1];
+            double ws[3];
+            compute_flux(&c, U[s], o, ws);
+            if (s == 0) {
+                double waveSpeedTotal = 0;
+                for (int d = 0; d < 3; ++d) {
+                    if (cellLengths[d] == 0) continue;
+                    waveSpeedTotal += ws[d] / cellLengths[d];
+                }
+                dt = cfl / waveSpeedTotal;
+                if (number_of_saves > 0) {
+                    const double nextSaveTime = numberSaved * timeInterval + 0.0;
+                    const double lim = nextSaveTime - t;
+                    dt = lim < dt ? lim : dt;
+                }
+            }
+            const double scale = dt / cellLengths[0];
+            const double* us = U[s];
+            const double* u0 = U[0];
+#pragma omp parallel for schedule(static)
+            for (long i = 0; i < (long)nvar * total; ++i) {
+                double v = o[i];
+                v *= scale;
+                v += us[i];
+                if (in == IN_RK3) {
+                    if (s == 1) {
+                        v *= 1. / 3.;
+                        v += u0[i];
+                        v *= 3. / 4.;
+                    } else if (s == 2) {
+                        v *= 2;
+                        v += u0[i];
+                        v *= 1. / 3.;
+                    }
+                } else if (in == IN_RK2 && s == 1) {
+                    v += u0[i];
+                    v *= 0.5;
+                }
+                o[i] = v;
+            }
+            apply_boundary(G, bc, o);
+        }
+        double* tmp = U[0];
+        U[0] = U[nsub];
+        U[nsub] = tmp;
+        t += dt;
+        if (dts && steps < max_dts) dts[steps] = dt;
+        ++steps;
+        if (!obeys(G, U[0])) {
+            r = fail(-2, "Simulation state does not obey constraints! At time %.17g, number of timesteps performed %d",
+                     t, steps);
+            break;
+        }
+        if (number_of_saves > 0 && t >= numberSaved * timeInterval + 0.0) numberSaved++;
+    }
+    memcpy(out, U[0], (size_t)nvar * total * sizeof(double));
+    *t_out = t;
+    *steps_out = steps;
+    for (int s = 0; s <= nsub; ++s) free(U[s]);
+    free(primPad);
+    flux_ctx_free(&c);
+    return r;
+}
+
+/* ---------------------------------------------------------- generator */
+
+/* 64-bit Mersenne Twister, MT19937-64 (Matsumoto and Nishimura; the
+ * parameters of std::mt19937_64), default seed 5489. */
+typedef struct {
+    uint64_t mt[312];
+    int mti;
+} mt64;
+
+static void mt64_seed(mt64* g, uint64_t seed) {
+    g->mt[0] = seed;
+    for (int i = 1; i < 312; ++i)
+        g->mt[i] = 6364136223846793005ULL * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + (uint64_t)i;
+    g->mti = 312;
+}
+
+static uint64_t mt64_next(mt64* g) {
+    const uint64_t UM = 0xFFFFFFFF80000000ULL, LM = 0x7FFFFFFFULL;
+    const uint64_t A = 0xB5026F5AA96619E9ULL;
+    if (g->mti >= 312) {
+        for (int i = 0; i < 312; ++i) {
+            const uint64_t x = (g->mt[i] & UM) | (g->mt[(i + 1) % 312] & LM);
+            g->mt[i] = g->mt[(i + 156) % 312] ^ (x >> 1) ^ ((x & 1ULL) ? A : 0ULL);
+        }
+        g->mti = 0;
+    }
+    uint64_t x = g->mt[g->mti++];
+    x ^= (x >> 29) & 0x5555555555555555ULL;
+    x ^= (x << 17) & 0x71D67FFFEDA60000ULL;
+    x ^= (x << 37) & 0xFFF7EEE000000000ULL;
+    x ^= x >> 43;
+    return x;
+}
+
+/* std::uniform_real_distribution<double>(0,1) over a 64-bit engine uses one
+ * draw: double(x) / 2^64, and nextafter(1,0) if that rounds to 1 (libstdc++
+ * generate_canonical). Uniform::scale maps it to x (b - a) + a
+ * (alsuq/src/distribution/Uniform.cpp:27-34). Draw number sample*dimension +
+ * component of the default-seeded engine, as STLMersenne fast-forwards
+ * (alsuq/src/generator/STLMersenne.cpp:38-85). */
+int fv_uniform(int dimension, int sample, double lower, double upper, double* out) {
+    if (dimension <= 0 || sample < 0) return fail(-1, "bad dimension/sample");
+    mt64 g;
+    mt64_seed(&g, 5489ULL);
+    for (long k = 0; k < (long)sample * dimension; ++k) mt64_next(&g);
+    for (int c = 0; c < dimension; ++c) {
+        double r = (double)mt64_next(&g) / 18446744073709551616.0;
+        if (r >= 1.0) r = nextafter(1.0, 0.0);
+        const double x = r * (1.0 - 0.0) + 0.0;
+        out[c] = x * (upper - lower) + lower;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------- statistics */
+
+/* MeanVariance::computeStatistics adds u and pow(u,2) per sample
+ * (alsuq/src/stats/MeanVariance.cpp:30-53); StatisticsHelper::combineStatistics
+ * divides by the sample count (StatisticsHelper.cpp:35-79); finalizeStatistics
+ * subtracts pow(mean,2) (MeanVariance.cpp:55-67). */
+int fv_meanvar(long count, int nsamples, const double* const* samples, double* mean,
+               double* var) {
+    if (count < 0 || nsamples <= 0) return fail(-1, "bad sizes");
+    /* the exponent is read at run time so the compiler keeps the libm pow call
+     * the reference makes (HostMemory::addPower takes the power as an argument) */
+    volatile double two_v = 2.0;
+    const double two = two_v;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < count; ++i) {
+        double m = 0, v = 0;
+        for (int s = 0; s < nsamples; ++s) {
+            m += samples[s][i];
+            v += pow(samples[s][i], two);
+        }
+        m /= (double)nsamples;
+        v /= (double)nsamples;
+        v -= pow(m, two);
+        mean[i] = m;
+        var[i] = v;
+    }
+    return 0;
+}

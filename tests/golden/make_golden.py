@@ -1,0 +1,139 @@
+"""Generates the golden fixtures in this directory from the reference's own
+CPU implementation, built unmodified from its sources by oracle/refbuild
+(make -C oracle/refbuild REF=<path to alsvinn>) into oracle/_ref/libalsref.so.
+
+Run once from the repository root:  python tests/golden/make_golden.py
+The fixtures are small .npz files; the tests compare the C oracle (and through
+it the CUDA path) against them, so they pin the oracle to the reference itself.
+The generator draws must be requested in increasing sample order in one fresh
+process (the reference's mt19937_64 is process-wide).
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+import workloads  # noqa: E402
+
+LIB = os.path.join(ROOT, "oracle", "_ref", "libalsref.so")
+R = ctypes.CDLL(LIB)
+R.ref_last_error.restype = ctypes.c_char_p
+D = ctypes.c_double
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def i3(v):
+    return (ctypes.c_int * 3)(*v)
+
+
+def d3(v):
+    return (ctypes.c_double * 3)(*v)
+
+
+def check(rc):
+    if rc != 0:
+        raise RuntimeError(R.ref_last_error().decode())
+
+
+def padded_shape(n, g):
+    dim = 3 if n[2] > 1 else (2 if n[1] > 1 else 1)
+    return [n[d] + 2 * g if d < dim else n[d] for d in range(3)]
+
+
+def flux_cases():
+    rng = np.random.default_rng(20240601)
+    out = {}
+    grids = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
+    fluxes = {"euler1": ["hll", "hll3"], "euler2": ["hll", "hll3"], "euler3": ["hll", "hll3"],
+              "burgers": ["godunov"]}
+    for eq, n in grids.items():
+        for fl in fluxes[eq]:
+            for rc in workloads.RECONSTRUCTIONS:
+                g = workloads.ghost_cells(rc)
+                t = padded_shape(n, g)
+                U = workloads.smooth_random_state(eq, t, rng)
+                o = np.zeros_like(U)
+                ws = (D * 3)()
+                check(R.ref_compute_flux(eq.encode(), fl.encode(), rc.encode(), i3(n), D(1.4), P(U), P(o), ws))
+                key = f"{eq}_{fl}_{rc}"
+                out[key + "_U"] = U
+                out[key + "_L"] = o
+                out[key + "_ws"] = np.array(list(ws))
+    np.savez_compressed(os.path.join(HERE, "flux.npz"), **out)
+
+
+def boundary_cases():
+    out = {}
+    for bc in ("neumann", "periodic"):
+        for n in ((7, 1, 1), (6, 5, 1), (5, 6, 4)):
+            for g in (1, 2, 3, 4):
+                t = padded_shape(n, g)
+                if any(t[d] < 2 * g for d in range(3) if n[d] > 1):
+                    continue
+                tot = t[0] * t[1] * t[2]
+                U = np.arange(tot, dtype=np.float64).reshape(1, tot) + 0.25
+                check(R.ref_boundary(bc.encode(), i3(n), g, 1, P(U)))
+                out[f"{bc}_{n[0]}x{n[1]}x{n[2]}_g{g}"] = U
+    np.savez_compressed(os.path.join(HERE, "boundary.npz"), **out)
+
+
+def generator_cases():
+    out = {}
+    for s in range(6):
+        a = np.zeros(40)
+        check(R.ref_uniform(40, s, D(0.0), D(1.0), P(a)))
+        out[f"uniform40_s{s}"] = a
+    np.savez_compressed(os.path.join(HERE, "generator.npz"), **out)
+
+
+def meanvar_cases():
+    rng = np.random.default_rng(7)
+    n, g = (8, 6, 1), 2
+    tot = 12 * 10
+    S = [rng.uniform(0.5, 2.0, (4, tot)) for _ in range(9)]
+    arr = (ctypes.c_void_p * len(S))(*[P(s) for s in S])
+    m = np.zeros((4, tot))
+    v = np.zeros((4, tot))
+    check(R.ref_meanvar(b"euler2", i3(n), g, len(S), arr, P(m), P(v)))
+    np.savez_compressed(os.path.join(HERE, "meanvar.npz"), samples=np.array(S), mean=m, var=v)
+
+
+def run_cases():
+    out = {}
+    for name, case in workloads.GOLDEN_RUNS.items():
+        prim = case["prim"]()
+        g = workloads.ghost_cells(case["recon"])
+        t = padded_shape(case["n"], g)
+        nv = workloads.NVAR[case["equation"]]
+        U = np.zeros((nv, t[0] * t[1] * t[2]))
+        tt = D()
+        st = ctypes.c_int()
+        check(R.ref_run(case["equation"].encode(), case["flux"].encode(), case["recon"].encode(),
+                        case["integrator"].encode(), case["boundary"].encode(), i3(case["n"]),
+                        d3(case["lower"]), d3(case["upper"]), D(case["gamma"]), D(case["cfl"]),
+                        D(case["end_time"]), case["number_of_saves"], case["max_steps"], P(prim), P(U),
+                        ctypes.byref(tt), ctypes.byref(st), None, 0))
+        out[name + "_prim"] = prim
+        out[name + "_U"] = U
+        out[name + "_t"] = np.array([tt.value])
+        out[name + "_steps"] = np.array([st.value])
+    np.savez_compressed(os.path.join(HERE, "runs.npz"), **out)
+
+
+if __name__ == "__main__":
+    R.ref_set_threads(4)
+    generator_cases()
+    flux_cases()
+    boundary_cases()
+    meanvar_cases()
+    run_cases()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
