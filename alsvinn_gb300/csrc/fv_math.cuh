@@ -1,0 +1,377 @@
+// Device arithmetic of the finite-volume step: Euler and Burgers point
+// quantities, the HLL / HLL3 / Godunov numerical fluxes and the WENO2 / ENO2-4 /
+// none reconstructions.
+//
+// Two policies share this header:
+//  * Exact (FV_EXACT defined, translation unit built with -fmad=false): every
+//    expression keeps the reference's operand order with IEEE-rounded + - * /
+//    and sqrt, so results are bit-identical to the reference CPU path.
+//  * Fast: the same mathematics with reciprocals shared between uses and the
+//    WENO weights reduced to two reciprocals per cell; FMA contraction allowed.
+//    Results agree with the reference to rounding level (relative 1e-15 per
+//    operation), well inside the 1e-10 relative L1 contract.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fv_types.h"
+
+// Kernel code is compiled once per arithmetic variant; each variant's
+// templates live in their own namespace so that identically named
+// instantiations of different translation units never merge at link time.
+#ifndef GBFV_VARIANT_NS
+#define GBFV_VARIANT_NS common
+#endif
+
+namespace gbfv {
+namespace GBFV_VARIANT_NS {
+
+#ifdef FV_EXACT
+constexpr bool kExact = true;
+#else
+constexpr bool kExact = false;
+#endif
+
+template <class R> __device__ __forceinline__ R rsqrt_(R x);
+template <> __device__ __forceinline__ double rsqrt_<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return rsqrtf(x); }
+
+template <class R> __device__ __forceinline__ R rcp_(R x) { return R(1) / x; }
+
+// ---------------------------------------------------------------- Euler
+
+// Conserved variables of one cell side plus the derived pressure and velocity
+// (Euler<nsd>::computeExtra, alsfvm/include/alsfvm/equation/euler/Euler.hpp:204-211).
+template <class R, int NSD> struct EulerState {
+    R rho, m[NSD], E, p, u[NSD];
+    R rinv;  // 1/rho (fast policy only)
+};
+
+template <class R, int NSD>
+__device__ __forceinline__ void euler_extra(EulerState<R, NSD>& a, R gamma) {
+    R dot = a.m[0] * a.m[0];
+#pragma unroll
+    for (int k = 1; k < NSD; ++k) dot = dot + a.m[k] * a.m[k];
+    if (kExact) {
+        const R ie = a.E - R(0.5) * dot / a.rho;
+#pragma unroll
+        for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] / a.rho;
+        a.p = (gamma - R(1)) * ie;
+    } else {
+        a.rinv = rcp_(a.rho);
+#pragma unroll
+        for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] * a.rinv;
+        a.p = (gamma - R(1)) * (a.E - R(0.5) * dot * a.rinv);
+    }
+}
+
+// Euler<nsd>::computePointFlux (Euler.hpp:172-181).
+template <class R, int NSD, int D>
+__device__ __forceinline__ void euler_point_flux(const EulerState<R, NSD>& a, R* F) {
+    F[0] = a.m[D];
+#pragma unroll
+    for (int k = 0; k < NSD; ++k) F[1 + k] = a.u[D] * a.m[k];
+    F[1 + D] += a.p;
+    F[1 + NSD] = (a.E + a.p) * a.u[D];
+}
+
+template <class R, int NSD>
+__device__ __forceinline__ void euler_conserved(const EulerState<R, NSD>& a, R* c) {
+    c[0] = a.rho;
+#pragma unroll
+    for (int k = 0; k < NSD; ++k) c[1 + k] = a.m[k];
+    c[1 + NSD] = a.E;
+}
+
+// HLL3 (HLLC-type) flux F(left, right) in direction D with the reference's
+// extended speed estimate and its speedLeft == 0 -> F = 0 rule
+// (alsfvm/include/alsfvm/numflux/euler/HLL3.hpp:52-148). Returns
+// max(|speedLeft|, |speedRight|).
+template <class R, int NSD, int D>
+__device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerState<R, NSD>& Rs,
+                                       R gamma, R* F) {
+    constexpr int NV = NSD + 2;
+    R speedLeft, speedRight;
+    if (kExact) {
+        const R waveLeft = sqrt(L.rho);
+        const R waveRight = sqrt(Rs.rho);
+        const R rho = (L.rho + Rs.rho) / R(2);
+        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) / (waveLeft + waveRight);
+        const R p = (waveLeft * L.p + waveRight * Rs.p) / (waveLeft + waveRight);
+        const R cfLeft = sqrt(gamma * L.p / L.rho);
+        const R cfRight = sqrt(gamma * Rs.p / Rs.rho);
+        const R correct = R(0.5) * fmax(R(0), L.u[D] - Rs.u[D]);
+        const R cs = sqrt(gamma * p / rho);
+        speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
+        speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
+    } else {
+        const R waveLeft = sqrt(L.rho);
+        const R waveRight = sqrt(Rs.rho);
+        const R winv = rcp_(waveLeft + waveRight);
+        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
+        const R p = (waveLeft * L.p + waveRight * Rs.p) * winv;
+        const R cfLeft = sqrt(gamma * L.p * L.rinv);
+        const R cfRight = sqrt(gamma * Rs.p * Rs.rinv);
+        const R correct = R(0.5) * fmax(R(0), L.u[D] - Rs.u[D]);
+        const R cs = sqrt(R(2) * gamma * p / (L.rho + Rs.rho));
+        speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
+        speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
+    }
+    R fluxLeft[NV], fluxRight[NV];
+    euler_point_flux<R, NSD, D>(L, fluxLeft);
+    euler_point_flux<R, NSD, D>(Rs, fluxRight);
+    const R udl = L.u[D] - speedLeft;
+    const R udr = Rs.u[D] - speedRight;
+    const R aa = udr * Rs.rho - udl * L.rho;
+    const R sm = (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) / aa;
+    if (speedLeft == R(0)) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = R(0);
+    } else if (speedLeft > R(0)) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = fluxLeft[k];
+    } else if (speedRight < R(0)) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = fluxRight[k];
+    } else {
+        // Star state on the side of the contact speed sm.
+        const bool leftSide = sm >= R(0);
+        const EulerState<R, NSD>& S = leftSide ? L : Rs;
+        const R s = leftSide ? speedLeft : speedRight;
+        const R ud = leftSide ? udl : udr;
+        const R* fS = leftSide ? fluxLeft : fluxRight;
+        R mid[NV], c[NV];
+        if (kExact) {
+            R us[NSD];
+#pragma unroll
+            for (int k = 0; k < NSD; ++k)
+                us[k] = (fluxRight[1 + k] - fluxLeft[1 + k] - speedRight * Rs.m[k] + speedLeft * L.m[k]) / aa;
+            us[D] = sm;
+            mid[0] = S.rho * ud / (sm - s);
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) mid[1 + k] = mid[0] * us[k];
+            const R pp = S.p + S.rho * (S.u[D] - sm) * ud;
+            mid[1 + NSD] = (ud * S.E + S.p * S.u[D] - pp * sm) / (sm - s);
+        } else {
+            const R ainv = rcp_(aa);
+            const R sinv = rcp_(sm - s);
+            mid[0] = S.rho * ud * sinv;
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) {
+                const R usk = (k == D) ? sm
+                                       : (fluxRight[1 + k] - fluxLeft[1 + k] - speedRight * Rs.m[k] +
+                                          speedLeft * L.m[k]) * ainv;
+                mid[1 + k] = mid[0] * usk;
+            }
+            const R pp = S.p + S.rho * (S.u[D] - sm) * ud;
+            mid[1 + NSD] = (ud * S.E + S.p * S.u[D] - pp * sm) * sinv;
+        }
+        euler_conserved<R, NSD>(S, c);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = fS[k] + s * (mid[k] - c[k]);
+    }
+    return fmax(fabs(speedLeft), fabs(speedRight));
+}
+
+// HLL flux (alsfvm/include/alsfvm/numflux/euler/HLL.hpp:51-115).
+template <class R, int NSD, int D>
+__device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerState<R, NSD>& Rs,
+                                      R gamma, R* F) {
+    constexpr int NV = NSD + 2;
+    R speedLeft, speedRight;
+    const R waveLeft = sqrt(L.rho);
+    const R waveRight = sqrt(Rs.rho);
+    if (kExact) {
+        const R rho = (L.rho + Rs.rho) / R(2);
+        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) / (waveLeft + waveRight);
+        const R p = (L.p * waveLeft + Rs.p * waveRight) / (waveLeft + waveRight);
+        const R cs = sqrt(gamma * p / rho);
+        speedLeft = fmin(L.u[D] - sqrt(gamma * L.p / L.rho), ud - cs);
+        speedRight = fmax(Rs.u[D] + sqrt(gamma * Rs.p / Rs.rho), ud + cs);
+    } else {
+        const R winv = rcp_(waveLeft + waveRight);
+        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
+        const R p = (L.p * waveLeft + Rs.p * waveRight) * winv;
+        const R cs = sqrt(R(2) * gamma * p / (L.rho + Rs.rho));
+        speedLeft = fmin(L.u[D] - sqrt(gamma * L.p * L.rinv), ud - cs);
+        speedRight = fmax(Rs.u[D] + sqrt(gamma * Rs.p * Rs.rinv), ud + cs);
+    }
+    if (speedLeft == R(0)) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = R(0);
+    } else if (speedLeft > R(0)) {
+        euler_point_flux<R, NSD, D>(L, F);
+    } else if (speedRight < R(0)) {
+        euler_point_flux<R, NSD, D>(Rs, F);
+    } else {
+        R fl[NV], fr[NV], cl[NV], cr[NV];
+        euler_point_flux<R, NSD, D>(L, fl);
+        euler_point_flux<R, NSD, D>(Rs, fr);
+        euler_conserved<R, NSD>(L, cl);
+        euler_conserved<R, NSD>(Rs, cr);
+        if (kExact) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                F[k] = (speedRight * fl[k] - speedLeft * fr[k] + speedRight * speedLeft * (cr[k] - cl[k])) /
+                       (speedRight - speedLeft);
+        } else {
+            const R inv = rcp_(speedRight - speedLeft);
+            const R srl = speedRight * speedLeft;
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                F[k] = (speedRight * fl[k] - speedLeft * fr[k] + srl * (cr[k] - cl[k])) * inv;
+        }
+    }
+    return fmax(fabs(speedLeft), fabs(speedRight));
+}
+
+// Godunov flux for Burgers: F = max(f(max(uL,0)), f(min(uR,0))), f = u^2/2,
+// wave speed max(|uL|,|uR|) (alsfvm/include/alsfvm/numflux/burgers/Godunov.hpp:40-60).
+template <class R>
+__device__ __forceinline__ R flux_godunov(R uL, R uR, R* F) {
+    const R a = fmax(uL, R(0));
+    const R b = fmin(uR, R(0));
+    F[0] = fmax(a * a / R(2), b * b / R(2));
+    return fmax(fabs(uL), fabs(uR));
+}
+
+// ------------------------------------------------------- reconstruction
+
+
+template <int RC> struct ReconTraits;
+template <> struct ReconTraits<RC_NONE> { static constexpr int ghosts = 1; static constexpr int reach = 0; };
+template <> struct ReconTraits<RC_WENO2> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
+template <> struct ReconTraits<RC_ENO2> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
+template <> struct ReconTraits<RC_ENO3> { static constexpr int ghosts = 3; static constexpr int reach = 2; };
+template <> struct ReconTraits<RC_ENO4> { static constexpr int ghosts = 4; static constexpr int reach = 3; };
+
+// ENO coefficient rows (alsfvm/src/reconstruction/ENOCoefficients.cpp:21-49):
+// row r weights the stencil starting r cells to the left for the value at the
+// cell's left face; row r+1 gives the right-face value.
+template <int ORDER> struct EnoC;
+template <> struct EnoC<2> {
+    static __device__ __forceinline__ double c(int r, int j) {
+        const double t[3][2] = {{3.0 / 2.0, -1.0 / 2.0}, {1.0 / 2.0, 1.0 / 2.0}, {-1.0 / 2.0, 3.0 / 2.0}};
+        return t[r][j];
+    }
+};
+template <> struct EnoC<3> {
+    static __device__ __forceinline__ double c(int r, int j) {
+        const double t[4][3] = {{11.0 / 6.0, -7.0 / 6.0, 1.0 / 3.0},
+                                {1.0 / 3.0, 5.0 / 6.0, -1.0 / 6.0},
+                                {-1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0},
+                                {1.0 / 3.0, -7.0 / 6.0, 11.0 / 6.0}};
+        return t[r][j];
+    }
+};
+template <> struct EnoC<4> {
+    static __device__ __forceinline__ double c(int r, int j) {
+        const double t[5][4] = {{25.0 / 12.0, -23.0 / 12.0, 13.0 / 12.0, -1.0 / 4.0},
+                                {1.0 / 4.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0},
+                                {-1.0 / 12.0, 7.0 / 12.0, 7.0 / 12.0, -1.0 / 12.0},
+                                {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 1.0 / 4.0},
+                                {-1.0 / 4.0, 13.0 / 12.0, -23.0 / 12.0, 25.0 / 12.0}};
+        return t[r][j];
+    }
+};
+
+#define FV_WENO_EPSILON 1e-8  // alsfvm/include/alsfvm/reconstruction/WENOCoefficients.hpp:21
+
+// Reconstructs the values of one cell at its left (i-1/2) and right (i+1/2)
+// faces for all NV variables. `u` points at the cell's variable 0 in a strided
+// store: variable k sits at u[k * vs], neighbour j along the direction at
+// u[j * ds]. Variable 0 is the WENO weight / ENO indicator (rho for Euler,
+// u for Burgers: Euler.hpp:286-288).
+template <class R, int NV, int RC>
+__device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs, int ds, R* left, R* right) {
+    if constexpr (RC == RC_NONE) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) left[k] = right[k] = u[k * vs];
+    } else if constexpr (RC == RC_WENO2) {
+        // WENO2::reconstruct (alsfvm/include/alsfvm/reconstruction/WENO2.hpp:31-91).
+        const R i0 = u[0];
+        const R d0 = u[ds] - i0;
+        const R d1 = i0 - u[-ds];
+        const R b0 = d0 * d0;
+        const R b1 = d1 * d1;
+        R w0Left, w1Left, w0Right, w1Right;
+        if (kExact) {
+            const R eps = R(FV_WENO_EPSILON);
+            const R a0Left = R(1) / (R(3) * (eps + b0) * (eps + b0));
+            const R a1Left = R(2) / (R(3) * (eps + b1) * (eps + b1));
+            w0Left = a0Left / (a0Left + a1Left);
+            w1Left = a1Left / (a0Left + a1Left);
+            const R a0Right = R(2) / (R(3) * (eps + b0) * (eps + b0));
+            const R a1Right = R(1) / (R(3) * (eps + b1) * (eps + b1));
+            w0Right = a0Right / (a0Right + a1Right);
+            w1Right = a1Right / (a0Right + a1Right);
+        } else {
+            // alpha0 ~ 1/(eps+b0)^2, alpha1 ~ 2/(eps+b1)^2 (left face), and the
+            // mirrored pair on the right face; normalising gives weights in
+            // terms of s_k = (eps+b_k)^2 with one reciprocal per face.
+            const R eps = R(FV_WENO_EPSILON);
+            const R s0 = (eps + b0) * (eps + b0);
+            const R s1 = (eps + b1) * (eps + b1);
+            const R iL = rcp_(s1 + R(2) * s0);
+            const R iR = rcp_(R(2) * s1 + s0);
+            w0Left = s1 * iL;
+            w1Left = R(2) * s0 * iL;
+            w0Right = R(2) * s1 * iR;
+            w1Right = s0 * iR;
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const R* v = u + k * vs;
+            const R um = v[-ds], uc = v[0], up = v[ds];
+            left[k] = R(0.5) * (w1Left * um + (R(3) * w0Left + w1Left) * uc - w0Left * up);
+            right[k] = R(0.5) * (w0Right * up + (R(3) * w1Right + w0Right) * uc - w1Right * um);
+        }
+    } else {
+        // ENOCPU<order> (alsfvm/src/reconstruction/ENOCPU.cpp:41-171): undivided
+        // differences of variable 0; at each level the shift grows when the
+        // left difference is smaller in magnitude than the right one.
+        constexpr int ORDER = RC;  // RC_ENO2 == 2, ...
+        constexpr int W = 2 * ORDER - 1;
+        R w[W];
+#pragma unroll
+        for (int j = 0; j < W; ++j) w[j] = u[(j - (ORDER - 1)) * ds];
+        R dd[W];
+#pragma unroll
+        for (int j = 0; j < W - 1; ++j) dd[j] = w[j + 1] - w[j];
+        int shift = 0;
+        constexpr int c = ORDER - 1;
+#pragma unroll
+        for (int l = 0; l < ORDER - 1; ++l) {
+            if (fabs(dd[c - 1]) < fabs(dd[c])) shift++;
+            if (l + 1 < ORDER - 1) {
+#pragma unroll
+                for (int j = 0; j < W - 2 - l; ++j) dd[j] = dd[j + 1] - dd[j];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const R* v = u + k * vs;
+            R lv = R(0), rv = R(0);
+#pragma unroll
+            for (int j = 0; j < ORDER; ++j) {
+                // both rows for every shift, selected without divergence
+                R cl = R(0), cr = R(0);
+#pragma unroll
+                for (int s = 0; s < ORDER; ++s) {
+                    if (s == shift) {
+                        cl = R(EnoC<ORDER>::c(s, j));
+                        cr = R(EnoC<ORDER>::c(s + 1, j));
+                    }
+                }
+                const R value = v[(j - shift) * ds];
+                lv += cl * value;
+                rv += cr * value;
+            }
+            left[k] = lv;
+            right[k] = rv;
+        }
+    }
+}
+
+}  // namespace GBFV_VARIANT_NS
+}  // namespace gbfv

@@ -1,0 +1,34 @@
+// Table of kernel launchers, filled by the per-variant translation units
+// (fv_variant.cu compiled once per arithmetic variant and equation).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fv_types.h"
+
+namespace gbfv {
+
+// Arithmetic variants of the step.
+enum Variant { VAR_F64 = 0, VAR_F64_EXACT = 1, VAR_F32 = 2, NUM_VARIANTS = 3 };
+enum Equation { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3, NUM_EQ = 4 };
+enum Flux { FL_HLL = 0, FL_HLL3 = 1, FL_GODUNOV = 2, NUM_FLUX = 3 };
+constexpr int NUM_RECON = 5;
+
+typedef int (*StageLauncher)(const StageArgs& a, cudaStream_t s);
+typedef int (*ApplyLauncher)(const StageArgs& a, cudaStream_t s);
+
+typedef int (*ReconLauncher)(const ReconArgs& a, cudaStream_t s);
+
+typedef int (*CheckLauncher)(const CheckArgs& a, cudaStream_t s);
+
+struct Registry {
+    // [variant][equation][flux][recon][dim-1]
+    StageLauncher stage[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
+    ApplyLauncher apply[NUM_VARIANTS][NUM_EQ];
+    ReconLauncher recon[NUM_VARIANTS][NUM_EQ][NUM_RECON];
+    CheckLauncher check[NUM_VARIANTS][NUM_EQ];
+    size_t stage_smem[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
+};
+
+Registry& registry();
+
+}  // namespace gbfv

@@ -1,0 +1,357 @@
+// Fused Runge-Kutta stage kernel and the small per-step kernels.
+//
+// One launch of stage_kernel advances one RK stage of the whole grid: each CTA
+// stages its tile plus a halo of g cells of every conserved variable in shared
+// memory, reconstructs each direction, evaluates the face fluxes, forms the
+// flux difference L (the reference's computeFlux output: sum over directions
+// of F_{i-1/2} - F_{i+1/2}, unscaled), combines it with the stage inputs as the
+// reference integrators do, and writes the cell together with its ghost
+// images (the Neumann / periodic boundary as an index map), so the next stage
+// reads a complete padded array. Face wave speeds are reduced by warp shuffles
+// and one atomic per CTA and direction.
+//
+// Stage modes (RK3 = SSP-RK3, RK2 = SSP-RK2, FE = forward Euler, c = dt/dx.x):
+//   MODE_L        in = U                 out = L(in)           (stage 0 of all)
+//   MODE_RK3_S1   in = L0*c + U0         out = ((L(in)*c + in)*(1/3) + U0)*(3/4)
+//   MODE_RK3_S2   in = U                 out = ((L(in)*c + in)*2 + U0)*(1/3)
+//   MODE_RK2_S1   in = L0*c + U0         out = ((L(in)*c + in) + U0)*0.5
+// (alsfvm/src/integrator/RungeKutta3.cpp:49-86, RungeKutta2.cpp:37-67). Stage 1
+// rebuilds U1 on the fly from U0 and L0, so U1 is never stored and an RK3 step
+// moves the algorithmic 8 * nvar state words per cell.
+#pragma once
+#include "fv_math.cuh"
+#include "fv_types.h"
+
+namespace gbfv {
+namespace GBFV_VARIANT_NS {
+
+template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
+template <> __device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <class R> __device__ __forceinline__ R add_rn(R a, R b);
+template <> __device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// Conserved-variable count and the flux between two reconstructed states.
+template <class R, int EQ, int FLUX> struct Physics {
+    static constexpr int NSD = EQ == 0 ? 1 : EQ;
+    static constexpr int NV = EQ == 0 ? 1 : EQ + 2;
+    template <int D>
+    static __device__ __forceinline__ R face_flux(const R* a, const R* b, R gamma, R* F) {
+        if constexpr (EQ == 0) {
+            return flux_godunov<R>(a[0], b[0], F);
+        } else {
+            EulerState<R, NSD> L, Rr;
+            L.rho = a[0];
+            Rr.rho = b[0];
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) {
+                L.m[k] = a[1 + k];
+                Rr.m[k] = b[1 + k];
+            }
+            L.E = a[1 + NSD];
+            Rr.E = b[1 + NSD];
+            euler_extra<R, NSD>(L, gamma);
+            euler_extra<R, NSD>(Rr, gamma);
+            if constexpr (FLUX == 1)
+                return flux_hll3<R, NSD, D>(L, Rr, gamma, F);
+            else
+                return flux_hll<R, NSD, D>(L, Rr, gamma, F);
+        }
+    }
+    // Constraint check of one cell (CPUCellComputer::obeysConstraints,
+    // alsfvm/src/equation/CPUCellComputer.cpp:79-125): finite values, rho > 0, p > 0.
+    static __device__ __forceinline__ bool obeys(const R* c, R gamma) {
+        if constexpr (EQ == 0) {
+            return isfinite(c[0]);
+        } else {
+            EulerState<R, NSD> s;
+            s.rho = c[0];
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) s.m[k] = c[1 + k];
+            s.E = c[1 + NSD];
+            euler_extra<R, NSD>(s, gamma);
+            bool ok = isfinite(s.rho) && isfinite(s.E) && isfinite(s.p) && s.rho > R(0) && s.p > R(0);
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) ok = ok && isfinite(s.m[k]) && isfinite(s.u[k]);
+            return ok;
+        }
+    }
+};
+
+template <int DIM, int TX, int TY, int TZ> struct Tile {
+    static constexpr int NT = TX * TY * TZ;
+    static constexpr int T[3] = {TX, TY, TZ};
+};
+
+template <class R, int NV, int G, int DIM, int TX, int TY, int TZ>
+struct SmemLayout {
+    static constexpr int GX = G, GY = DIM > 1 ? G : 0, GZ = DIM > 2 ? G : 0;
+    static constexpr int HX = TX + 2 * GX, HY = TY + 2 * GY, HZ = TZ + 2 * GZ;
+    static constexpr int HALO = HX * HY * HZ;
+    // per-direction line buffers: reconstructed left/right values of the
+    // (T_d + 2) cells along d and the (T_d + 1) face fluxes, times the tile's
+    // extent in the other dimensions
+    static constexpr int REC0 = (TX + 2) * TY * TZ;
+    static constexpr int REC1 = DIM > 1 ? TX * (TY + 2) * TZ : 0;
+    static constexpr int REC2 = DIM > 2 ? TX * TY * (TZ + 2) : 0;
+    static constexpr int REC = REC0 > REC1 ? (REC0 > REC2 ? REC0 : REC2) : (REC1 > REC2 ? REC1 : REC2);
+    static constexpr int FAC0 = (TX + 1) * TY * TZ;
+    static constexpr int FAC1 = DIM > 1 ? TX * (TY + 1) * TZ : 0;
+    static constexpr int FAC2 = DIM > 2 ? TX * TY * (TZ + 1) : 0;
+    static constexpr int FAC = FAC0 > FAC1 ? (FAC0 > FAC2 ? FAC0 : FAC2) : (FAC1 > FAC2 ? FAC1 : FAC2);
+    static constexpr size_t bytes = sizeof(R) * ((size_t)NV * HALO + 2 * (size_t)NV * REC + (size_t)NV * FAC);
+};
+
+
+// One direction D of the tile: reconstruct, face fluxes, accumulate into acc.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int D>
+__device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc, R* acc, int tid,
+                                               const int* org, const Grid& G, R gamma, double& wsmax) {
+    using Ph = Physics<R, EQ, FLUX>;
+    constexpr int NV = Ph::NV;
+    using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;
+    constexpr int TD = D == 0 ? TX : (D == 1 ? TY : TZ);
+    constexpr int O1 = D == 0 ? TY : TX;          // extent of the first other dimension
+    constexpr int LEN = TD + 2;
+    constexpr int NREC = LEN * (NT / TD);
+    constexpr int NFACE = (TD + 1) * (NT / TD);
+    constexpr int DS = D == 0 ? 1 : (D == 1 ? SL::HX : SL::HX * SL::HY);
+    constexpr int VS = SL::HALO;
+
+    // reconstruction of cells -1 .. TD along D
+    for (int w = tid; w < NREC; w += NT) {
+        const int a = w % LEN;
+        const int o = w / LEN;
+        const int p = o % O1, q = o / O1;
+        int c[3];
+        c[D] = a - 1;
+        if (D == 0) { c[1] = p; c[2] = q; }
+        else if (D == 1) { c[0] = p; c[2] = q; }
+        else { c[0] = p; c[1] = q; }
+        const int s = ((c[2] + SL::GZ) * SL::HY + (c[1] + SL::GY)) * SL::HX + (c[0] + SL::GX);
+        R l[NV], r[NV];
+        reconstruct_cell<R, NV, RC>(su + s, VS, DS, l, r);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            rl[k * NREC + w] = l[k];
+            rr[k * NREC + w] = r[k];
+        }
+    }
+    __syncthreads();
+    // face b is the left face of tile cell b along D (between cells b-1 and b)
+    for (int f = tid; f < NFACE; f += NT) {
+        const int b = f % (TD + 1);
+        const int o = f / (TD + 1);
+        const int p = o % O1, q = o / O1;
+        R a[NV], bb[NV], F[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            a[k] = rr[k * NREC + o * LEN + b];       // cell b-1 at its right face
+            bb[k] = rl[k * NREC + o * LEN + b + 1];  // cell b at its left face
+        }
+        const R w = Ph::template face_flux<D>(a, bb, gamma, F);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) fc[k * NFACE + f] = F[k];
+        // the face counts if both neighbours lie in the grid's interior range
+        int c[3];
+        c[D] = b;
+        if (D == 0) { c[1] = p; c[2] = q; }
+        else if (D == 1) { c[0] = p; c[2] = q; }
+        else { c[0] = p; c[1] = q; }
+        bool valid = org[D] + c[D] <= G.n[D];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (d != D) valid = valid && (org[d] + c[d] < G.n[d]);
+        if (valid) wsmax = fmax(wsmax, (double)w);
+    }
+    __syncthreads();
+    // this thread's cell: acc += (-F_{i+1/2}) + F_{i-1/2}
+    {
+        const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
+        const int cd = D == 0 ? cx : (D == 1 ? cy : cz);
+        const int p = D == 0 ? cy : cx;
+        const int q = D == 2 ? cy : cz;
+        const int o = p + O1 * q;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const R fl = fc[k * NFACE + o * (TD + 1) + cd];
+            const R fr = fc[k * NFACE + o * (TD + 1) + cd + 1];
+            acc[k] = acc[k] + ((-fr) + fl);
+        }
+    }
+    __syncthreads();
+}
+
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
+    using Ph = Physics<R, EQ, FLUX>;
+    constexpr int NV = Ph::NV;
+    constexpr int G = ReconTraits<RC>::ghosts;
+    using SL = SmemLayout<R, NV, G, DIM, TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* su = reinterpret_cast<R*>(smem_raw);
+    R* rl = su + NV * SL::HALO;
+    R* rr = rl + NV * SL::REC;
+    R* fc = rr + NV * SL::REC;
+    __shared__ double wred[NT / 32][3];
+
+    if (A.st->done) return;
+    const Grid& Gd = A.G;
+    const int tid = threadIdx.x;
+    const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
+    const R* in = reinterpret_cast<const R*>(A.in);
+    const R* u0 = reinterpret_cast<const R*>(A.u0);
+    const R* l0 = reinterpret_cast<const R*>(A.l0);
+    R* out = reinterpret_cast<R*>(A.out);
+    const long long total = Gd.total;
+    const int mode = A.mode;
+    const R scale = (R)A.st->scale;
+
+    // 1. tile + halo: padded cells [org, org + T + 2g) per active dimension
+    for (int w = tid; w < SL::HALO; w += NT) {
+        const int hx = w % SL::HX, hy = (w / SL::HX) % SL::HY, hz = w / (SL::HX * SL::HY);
+        const int px = org[0] + hx, py = org[1] + hy, pz = org[2] + hz;
+        if (px < Gd.t[0] && py < Gd.t[1] && pz < Gd.t[2]) {
+            const long long gi = gidx(Gd, px, py, pz);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                R v;
+                if (mode == MODE_RK3_S1 || mode == MODE_RK2_S1) {
+                    // U1 = L0 * c + U0, rounded as the reference's *= then +=
+                    v = add_rn(mul_rn(l0[k * total + gi], scale), in[k * total + gi]);
+                } else {
+                    v = in[k * total + gi];
+                }
+                su[k * SL::HALO + w] = v;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = R(1);
+        }
+    }
+    __syncthreads();
+
+    // 2. flux difference per direction
+    R acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = R(0);
+    double wsd[3] = {0.0, 0.0, 0.0};
+    const R gamma = (R)A.gamma;
+    tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
+    if constexpr (DIM > 1)
+        tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
+    if constexpr (DIM > 2)
+        tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
+
+    // 3. wave speeds (stage 0 only): warp max, CTA max, one atomic per direction
+    if (mode == MODE_L) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            double v = wsd[d];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+            if ((tid & 31) == 0) wred[tid >> 5][d] = v;
+        }
+        __syncthreads();
+        if (tid < DIM) {
+            double v = 0.0;
+            for (int w = 0; w < NT / 32; ++w) v = fmax(v, wred[w][tid]);
+            atomic_max_nonneg(&A.st->ws_bits[tid], v);
+        }
+    }
+
+    // 4. this thread's cell: combine and write with its ghost images
+    const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
+    const int ix = org[0] + cx, iy = org[1] + cy, iz = org[2] + cz;
+    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) return;
+    const int sidx = ((cz + SL::GZ) * SL::HY + (cy + SL::GY)) * SL::HX + (cx + SL::GX);
+    const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
+    R res[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        if (mode == MODE_L) {
+            res[k] = acc[k];
+        } else {
+            const R uin = su[k * SL::HALO + sidx];
+            const R base = u0[k * total + own];
+            R v = add_rn(mul_rn(acc[k], scale), uin);
+            if (mode == MODE_RK3_S1) {
+                v = mul_rn(v, R(1. / 3.));
+                v = add_rn(v, base);
+                v = mul_rn(v, R(3. / 4.));
+            } else if (mode == MODE_RK3_S2) {
+                v = mul_rn(v, R(2));
+                v = add_rn(v, base);
+                v = mul_rn(v, R(1. / 3.));
+            } else {  // MODE_RK2_S1
+                v = add_rn(v, base);
+                v = mul_rn(v, R(0.5));
+            }
+            res[k] = v;
+        }
+    }
+    if (A.check && !Ph::obeys(res, gamma)) {
+        if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
+    }
+    int px[3], py[3], pz[3];
+    const bool per = A.periodic != 0;
+    const int cxn = images(ix, Gd.n[0], Gd.g[0], per, px);
+    const int cyn = images(iy, Gd.n[1], Gd.g[1], per, py);
+    const int czn = images(iz, Gd.n[2], Gd.g[2], per, pz);
+    for (int a = 0; a < czn; ++a)
+        for (int b = 0; b < cyn; ++b)
+            for (int c = 0; c < cxn; ++c) {
+                const long long gi = gidx(Gd, px[c], py[b], pz[a]);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) out[k * total + gi] = res[k];
+            }
+}
+
+// Forward-Euler update U += L0 * c in place with ghost images
+// (alsfvm/src/integrator/ForwardEuler.cpp:32-51).
+template <class R, int EQ>
+__global__ void fe_apply_kernel(StageArgs A) {
+    using Ph = Physics<R, EQ, 1>;
+    constexpr int NV = Ph::NV;
+    if (A.st->done) return;
+    const Grid& Gd = A.G;
+    const long long ncell = (long long)Gd.n[0] * Gd.n[1] * Gd.n[2];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncell) return;
+    const int ix = (int)(i % Gd.n[0]);
+    const int iy = (int)((i / Gd.n[0]) % Gd.n[1]);
+    const int iz = (int)(i / ((long long)Gd.n[0] * Gd.n[1]));
+    const R* l0 = reinterpret_cast<const R*>(A.l0);
+    R* out = reinterpret_cast<R*>(A.out);
+    const long long total = Gd.total;
+    const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
+    const R scale = (R)A.st->scale;
+    R res[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) res[k] = add_rn(mul_rn(l0[k * total + own], scale), out[k * total + own]);
+    if (A.check && !Ph::obeys(res, (R)A.gamma)) {
+        if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
+    }
+    int px[3], py[3], pz[3];
+    const bool per = A.periodic != 0;
+    const int cxn = images(ix, Gd.n[0], Gd.g[0], per, px);
+    const int cyn = images(iy, Gd.n[1], Gd.g[1], per, py);
+    const int czn = images(iz, Gd.n[2], Gd.g[2], per, pz);
+    for (int a = 0; a < czn; ++a)
+        for (int b = 0; b < cyn; ++b)
+            for (int c = 0; c < cxn; ++c) {
+                const long long gi = gidx(Gd, px[c], py[b], pz[a]);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) out[k * total + gi] = res[k];
+            }
+}
+
+}  // namespace GBFV_VARIANT_NS
+}  // namespace gbfv

@@ -1,0 +1,100 @@
+// Types shared by the kernel translation units and the C-ABI layer: grid
+// geometry, the device-resident step state and the launch argument blocks.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace gbfv {
+
+enum Recon { RC_NONE = 0, RC_WENO2 = 1, RC_ENO2 = 2, RC_ENO3 = 3, RC_ENO4 = 4 };
+
+enum Mode { MODE_L = 0, MODE_RK3_S1 = 1, MODE_RK3_S2 = 2, MODE_RK2_S1 = 3 };
+
+// Device-resident step state shared by the per-step kernels (one per solve).
+struct StepState {
+    unsigned long long ws_bits[3];  // max face wave speed per direction (non-negative doubles)
+    double t;                       // current time
+    double dt;                      // dt of the step in flight
+    double scale;                   // dt / dx.x
+    long long steps;                // steps performed
+    long long number_saved;         // FixedIntervalWriter counter (starts at 1)
+    int status;                     // 0 ok, 1 constraint violated
+    int failed_step;                // first step whose state broke the constraints
+    int done;                       // 1: the advance has reached its end; kernels return at once
+    int pad_;
+    double end_time;                // advance target time
+    long long step_limit;           // advance step limit (< 0: none)
+};
+
+struct StepParams {
+    double cfl;
+    double cell_lengths[3];
+    double end_time;
+    double time_interval;  // 0: no save-time clamp
+    int dim;
+};
+
+struct Grid {
+    int n[3];   // interior cells
+    int g[3];   // ghosts per dimension (0 in inactive dimensions)
+    int t[3];   // padded extents
+    long long total;
+    int dim;
+};
+
+__device__ __forceinline__ long long gidx(const Grid& G, int x, int y, int z) {
+    return ((long long)z * G.t[1] + y) * G.t[0] + x;
+}
+
+// Padded positions holding the value of interior cell i (interior coordinate)
+// along one dimension: the cell itself plus its ghost images
+// (Neumann mirror: alsfvm/include/alsfvm/boundary/Neumann.hpp:24-35;
+// periodic wrap: Periodic.hpp:24-42). Returns the count (1..3).
+__device__ __forceinline__ int images(int i, int n, int g, bool periodic, int* pos) {
+    int c = 0;
+    pos[c++] = i + g;
+    if (g == 0) return c;
+    if (periodic) {
+        if (i < g) pos[c++] = i + g + n;
+        if (i >= n - g) pos[c++] = i + g - n;
+    } else {
+        if (i < g) pos[c++] = g - 1 - i;
+        if (i >= n - g) pos[c++] = 2 * n + g - 1 - i;
+    }
+    return c;
+}
+
+
+struct StageArgs {
+    const void* in;   // U (MODE_L, MODE_RK3_S2) or U0 (stage-1 modes)
+    const void* u0;   // U0 for the combination
+    const void* l0;   // L0 for stage-1 modes
+    void* out;
+    StepState* st;
+    Grid G;
+    double gamma;
+    int mode;
+    int periodic;
+    int check;        // run the constraint check on the output
+};
+
+// Reconstruction of one direction over the reference's cell range
+// (cells [g-1, t-g+1) along dir, interior in the other dimensions; every cell
+// for the "none" reconstruction, which copies the whole volume).
+struct ReconArgs {
+    const void* in;
+    void* left;
+    void* right;
+    Grid G;
+    int dir;
+};
+
+// Constraint check over every padded cell (ghosts included, as the reference
+// scans the whole volume); sets *flag to 0 when a cell fails.
+struct CheckArgs {
+    const void* in;
+    int* flag;
+    Grid G;
+    double gamma;
+};
+
+}  // namespace gbfv

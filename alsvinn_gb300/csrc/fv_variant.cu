@@ -1,0 +1,161 @@
+// Kernel instantiations for one arithmetic variant and one equation. This file
+// is compiled once per (FV_VARIANT, FV_EQ) pair; the exact variant is built
+// with -fmad=false and FV_EXACT so that no multiply-add is contracted.
+//   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic
+//   FV_EQ:      0 burgers, 1 euler1, 2 euler2, 3 euler3
+#define FV_NS_CAT2(a, b) a##b
+#define FV_NS_CAT(a, b) FV_NS_CAT2(a, b)
+#define GBFV_VARIANT_NS FV_NS_CAT(v, FV_VARIANT)
+#include "fv_registry.h"
+#include "fv_stage.cuh"
+
+#ifndef FV_VARIANT
+#error "FV_VARIANT must be defined"
+#endif
+#ifndef FV_EQ
+#error "FV_EQ must be defined"
+#endif
+
+#if FV_VARIANT == 2
+typedef float Real;
+#else
+typedef double Real;
+#endif
+
+#define FV_CAT2(a, b, c, d) a##b##c##d
+#define FV_CAT(a, b, c, d) FV_CAT2(a, b, c, d)
+#define FV_REGISTER_FN FV_CAT(gbfv_register_v, FV_VARIANT, _e, FV_EQ)
+
+namespace gbfv {
+namespace GBFV_VARIANT_NS {
+
+template <int DIM> struct TileShape;
+template <> struct TileShape<1> { static constexpr int X = 128, Y = 1, Z = 1; };
+template <> struct TileShape<2> { static constexpr int X = 32, Y = 8, Z = 1; };
+template <> struct TileShape<3> { static constexpr int X = 8, Y = 8, Z = 4; };
+
+template <int EQ, int FLUX, int RC, int DIM>
+struct StageEntry {
+    using TS = TileShape<DIM>;
+    using SL = SmemLayout<Real, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    static int launch(const StageArgs& a, cudaStream_t s) {
+        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z>;
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
+            if (e != cudaSuccess) return (int)e;
+            configured = 1;
+        }
+        dim3 grid((a.G.n[0] + TS::X - 1) / TS::X, (a.G.n[1] + TS::Y - 1) / TS::Y, (a.G.n[2] + TS::Z - 1) / TS::Z);
+        k<<<grid, TS::X * TS::Y * TS::Z, SL::bytes, s>>>(a);
+        return (int)cudaGetLastError();
+    }
+};
+
+template <int EQ>
+static int launch_apply(const StageArgs& a, cudaStream_t s) {
+    const long long ncell = (long long)a.G.n[0] * a.G.n[1] * a.G.n[2];
+    const int bs = 256;
+    fe_apply_kernel<Real, EQ><<<(unsigned)((ncell + bs - 1) / bs), bs, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+// Standalone reconstruction in one direction, global memory in and out.
+template <int NV, int RC>
+__global__ void recon_kernel(ReconArgs A) {
+    const Grid& G = A.G;
+    constexpr int g = ReconTraits<RC>::ghosts;
+    (void)g;
+    const int d = A.dir;
+    int lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        // "none" copies every cell (NoReconstruction.cpp:52-64)
+        lo[k] = RC == RC_NONE ? 0 : G.g[k] - (k == d);
+        hi[k] = RC == RC_NONE ? G.t[k] : G.t[k] - G.g[k] + (k == d);
+    }
+    const long long ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ex * ey * ez) return;
+    const int x = lo[0] + (int)(i % ex);
+    const int y = lo[1] + (int)((i / ex) % ey);
+    const int z = lo[2] + (int)(i / (ex * ey));
+    const long long gi = gidx(G, x, y, z);
+    const int ds = d == 0 ? 1 : (d == 1 ? G.t[0] : G.t[0] * G.t[1]);
+    const Real* in = reinterpret_cast<const Real*>(A.in);
+    Real l[NV], r[NV];
+    reconstruct_cell<Real, NV, RC>(in + gi, (int)G.total, ds, l, r);
+    Real* L = reinterpret_cast<Real*>(A.left);
+    Real* Rr = reinterpret_cast<Real*>(A.right);
+    for (int k = 0; k < NV; ++k) {
+        L[k * G.total + gi] = l[k];
+        Rr[k * G.total + gi] = r[k];
+    }
+}
+
+template <int EQ, int RC>
+static int launch_recon(const ReconArgs& a, cudaStream_t s) {
+    constexpr int NV = EQ == 0 ? 1 : EQ + 2;
+    long long cnt = 1;
+    for (int k = 0; k < 3; ++k)
+        cnt *= RC == RC_NONE ? a.G.t[k] : (a.G.t[k] - 2 * a.G.g[k] + 2 * (k == a.dir));
+    const int bs = 256;
+    recon_kernel<NV, RC><<<(unsigned)((cnt + bs - 1) / bs), bs, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int EQ>
+__global__ void check_kernel(CheckArgs A) {
+    constexpr int NV = EQ == 0 ? 1 : EQ + 2;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.G.total) return;
+    const Real* in = reinterpret_cast<const Real*>(A.in);
+    Real c[NV];
+    for (int k = 0; k < NV; ++k) c[k] = in[k * A.G.total + i];
+    if (!Physics<Real, EQ, 1>::obeys(c, (Real)A.gamma)) *A.flag = 0;
+}
+
+template <int EQ>
+static int launch_check(const CheckArgs& a, cudaStream_t s) {
+    const int bs = 256;
+    check_kernel<EQ><<<(unsigned)((a.G.total + bs - 1) / bs), bs, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int FLUX, int DIM>
+static void reg_dim(Registry& R) {
+    constexpr int V = FV_VARIANT, E = FV_EQ;
+    R.stage[V][E][FLUX][RC_NONE][DIM - 1] = &StageEntry<E, FLUX, RC_NONE, DIM>::launch;
+    R.stage[V][E][FLUX][RC_WENO2][DIM - 1] = &StageEntry<E, FLUX, RC_WENO2, DIM>::launch;
+    R.stage[V][E][FLUX][RC_ENO2][DIM - 1] = &StageEntry<E, FLUX, RC_ENO2, DIM>::launch;
+    R.stage[V][E][FLUX][RC_ENO3][DIM - 1] = &StageEntry<E, FLUX, RC_ENO3, DIM>::launch;
+    R.stage[V][E][FLUX][RC_ENO4][DIM - 1] = &StageEntry<E, FLUX, RC_ENO4, DIM>::launch;
+    R.stage_smem[V][E][FLUX][RC_NONE][DIM - 1] = StageEntry<E, FLUX, RC_NONE, DIM>::SL::bytes;
+    R.stage_smem[V][E][FLUX][RC_WENO2][DIM - 1] = StageEntry<E, FLUX, RC_WENO2, DIM>::SL::bytes;
+    R.stage_smem[V][E][FLUX][RC_ENO2][DIM - 1] = StageEntry<E, FLUX, RC_ENO2, DIM>::SL::bytes;
+    R.stage_smem[V][E][FLUX][RC_ENO3][DIM - 1] = StageEntry<E, FLUX, RC_ENO3, DIM>::SL::bytes;
+    R.stage_smem[V][E][FLUX][RC_ENO4][DIM - 1] = StageEntry<E, FLUX, RC_ENO4, DIM>::SL::bytes;
+}
+
+}  // namespace GBFV_VARIANT_NS
+}  // namespace gbfv
+
+extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
+    using namespace gbfv;
+    using namespace gbfv::GBFV_VARIANT_NS;
+    constexpr int V = FV_VARIANT, E = FV_EQ;
+#if FV_EQ == 0
+    reg_dim<FL_GODUNOV, 1>(*R);
+    reg_dim<FL_GODUNOV, 2>(*R);
+    reg_dim<FL_GODUNOV, 3>(*R);
+#else
+    reg_dim<FL_HLL, FV_EQ>(*R);
+    reg_dim<FL_HLL3, FV_EQ>(*R);
+#endif
+    R->apply[V][E] = &launch_apply<E>;
+    R->check[V][E] = &launch_check<E>;
+    R->recon[V][E][RC_NONE] = &launch_recon<E, RC_NONE>;
+    R->recon[V][E][RC_WENO2] = &launch_recon<E, RC_WENO2>;
+    R->recon[V][E][RC_ENO2] = &launch_recon<E, RC_ENO2>;
+    R->recon[V][E][RC_ENO3] = &launch_recon<E, RC_ENO3>;
+    R->recon[V][E][RC_ENO4] = &launch_recon<E, RC_ENO4>;
+}

@@ -1,0 +1,678 @@
+// C ABI of the GB300 finite-volume step (include/gbfv.h): solver handles, the
+// per-step driver and the operator-level entry points. Built with -fmad=false
+// (device) and -ffp-contract=off (host) so the time-step arithmetic and the
+// primitive-to-conserved conversion round exactly as the reference does.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "fv_registry.h"
+#include "gbfv.h"
+
+#define GBFV_REGISTER_DECL(v, e) extern "C" void gbfv_register_v##v##_e##e(gbfv::Registry*);
+GBFV_REGISTER_DECL(0, 0) GBFV_REGISTER_DECL(0, 1) GBFV_REGISTER_DECL(0, 2) GBFV_REGISTER_DECL(0, 3)
+GBFV_REGISTER_DECL(1, 0) GBFV_REGISTER_DECL(1, 1) GBFV_REGISTER_DECL(1, 2) GBFV_REGISTER_DECL(1, 3)
+GBFV_REGISTER_DECL(2, 0) GBFV_REGISTER_DECL(2, 1) GBFV_REGISTER_DECL(2, 2) GBFV_REGISTER_DECL(2, 3)
+
+namespace gbfv {
+
+Registry& registry() {
+    static Registry R = [] {
+        Registry r;
+        std::memset(&r, 0, sizeof r);
+        gbfv_register_v0_e0(&r); gbfv_register_v0_e1(&r); gbfv_register_v0_e2(&r); gbfv_register_v0_e3(&r);
+        gbfv_register_v1_e0(&r); gbfv_register_v1_e1(&r); gbfv_register_v1_e2(&r); gbfv_register_v1_e3(&r);
+        gbfv_register_v2_e0(&r); gbfv_register_v2_e1(&r); gbfv_register_v2_e2(&r); gbfv_register_v2_e3(&r);
+        return r;
+    }();
+    return R;
+}
+
+// ------------------------------------------------------- step kernels
+
+// dt = cfl / sum_d ws_d / dx_d, then the save-time clamp
+// (Integrator::computeTimestep, alsfvm/src/integrator/Integrator.cpp:20-46;
+// FixedIntervalWriter::adjustTimestep, alsfvm/src/io/FixedIntervalWriter.cpp:45-53).
+__global__ void dt_kernel(StepState* st, StepParams P) {
+    if (st->done) return;
+    double ws[3];
+    for (int d = 0; d < 3; ++d) ws[d] = d < P.dim ? __longlong_as_double((long long)st->ws_bits[d]) : 0.0;
+    double waveSpeedTotal = 0;
+    for (int d = 0; d < 3; ++d) {
+        if (P.cell_lengths[d] == 0) continue;
+        waveSpeedTotal += ws[d] / P.cell_lengths[d];
+    }
+    double dt = P.cfl / waveSpeedTotal;
+    if (P.time_interval > 0) {
+        const double nextSaveTime = (double)st->number_saved * P.time_interval + 0.0;
+        const double lim = nextSaveTime - st->t;
+        dt = lim < dt ? lim : dt;
+    }
+    st->dt = dt;
+    st->scale = dt / P.cell_lengths[0];
+}
+
+// t += dt (TimestepInformation::incrementTime), the writer's save counter, and
+// the loop condition t < end_time (Simulator::atEnd, Simulator.cpp:77-79).
+__global__ void finish_kernel(StepState* st, StepParams P) {
+    if (st->done) return;
+    st->t = st->t + st->dt;
+    st->steps += 1;
+    if (P.time_interval > 0 && st->t >= (double)st->number_saved * P.time_interval + 0.0) st->number_saved += 1;
+    st->ws_bits[0] = st->ws_bits[1] = st->ws_bits[2] = 0ull;
+    if (!(st->t < st->end_time) || (st->step_limit >= 0 && st->steps >= st->step_limit) || st->status != 0)
+        st->done = 1;
+}
+
+__global__ void begin_kernel(StepState* st, double end_time, long long step_limit) {
+    st->end_time = end_time;
+    st->step_limit = step_limit;
+    st->ws_bits[0] = st->ws_bits[1] = st->ws_bits[2] = 0ull;
+    st->done = (!(st->t < end_time) || (step_limit >= 0 && st->steps >= step_limit) || st->status != 0) ? 1 : 0;
+}
+
+// Copies V into U (end of an RK2 step), skipped once the advance is done.
+template <class R>
+__global__ void copy_state_kernel(const StepState* st, const R* __restrict__ src, R* __restrict__ dst, long long n) {
+    if (st->done) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// Ghost fill: every ghost cell copies the interior cell its per-dimension index
+// maps select; the composition equals the reference's dimension-by-dimension
+// fill (alsfvm/src/boundary/BoundaryCPU.cpp:30-106).
+__device__ __forceinline__ int src_index(int p, int n, int g, bool periodic) {
+    if (p < g) return periodic ? p + n : 2 * g - 1 - p;
+    if (p >= n + g) return periodic ? p - n : 2 * (n + g) - 1 - p;
+    return p;
+}
+
+template <class R>
+__global__ void boundary_kernel(R* U, Grid G, int nvar, int periodic) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= G.total) return;
+    const int x = (int)(i % G.t[0]);
+    const int y = (int)((i / G.t[0]) % G.t[1]);
+    const int z = (int)(i / ((long long)G.t[0] * G.t[1]));
+    const bool per = periodic != 0;
+    const int sx = src_index(x, G.n[0], G.g[0], per);
+    const int sy = src_index(y, G.n[1], G.g[1], per);
+    const int sz = src_index(z, G.n[2], G.g[2], per);
+    if (sx == x && sy == y && sz == z) return;
+    const long long s = gidx(G, sx, sy, sz);
+    for (int k = 0; k < nvar; ++k) U[k * G.total + i] = U[k * G.total + s];
+}
+
+}  // namespace gbfv
+
+using namespace gbfv;
+
+// ---------------------------------------------------------------- errors
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int gbfv_internal_fail(int code, const char* msg) { return fail(code, msg); }
+
+#define CUDA_TRY(x)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (x);                                                                \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(GBFV_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+#define LAUNCH_TRY(x)                                                                        \
+    do {                                                                                     \
+        int r_ = (x);                                                                        \
+        if (r_ != 0)                                                                         \
+            return fail(GBFV_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString((cudaError_t)r_)); \
+    } while (0)
+
+// ---------------------------------------------------------------- names
+
+static int parse_eq(const char* s) {
+    if (!s) return -1;
+    if (!strcmp(s, "burgers")) return EQ_BURGERS;
+    if (!strcmp(s, "euler1")) return EQ_EULER1;
+    if (!strcmp(s, "euler2")) return EQ_EULER2;
+    if (!strcmp(s, "euler3")) return EQ_EULER3;
+    return -1;
+}
+static int parse_flux(const char* s) {
+    if (!s) return -1;
+    if (!strcmp(s, "hll")) return FL_HLL;
+    if (!strcmp(s, "hll3")) return FL_HLL3;
+    if (!strcmp(s, "godunov")) return FL_GODUNOV;
+    return -1;
+}
+static int parse_recon(const char* s) {
+    if (!s) return -1;
+    if (!strcmp(s, "none")) return RC_NONE;
+    if (!strcmp(s, "weno2")) return RC_WENO2;
+    if (!strcmp(s, "eno2")) return RC_ENO2;
+    if (!strcmp(s, "eno3")) return RC_ENO3;
+    if (!strcmp(s, "eno4")) return RC_ENO4;
+    return -1;
+}
+enum { IN_FE = 0, IN_RK2 = 1, IN_RK3 = 2 };
+static int parse_integrator(const char* s) {
+    if (!s) return -1;
+    if (!strcmp(s, "forwardeuler")) return IN_FE;
+    if (!strcmp(s, "rungekutta2")) return IN_RK2;
+    if (!strcmp(s, "rungekutta3")) return IN_RK3;
+    return -1;
+}
+static int parse_bc(const char* s) {
+    if (!s) return -1;
+    if (!strcmp(s, "neumann")) return 0;
+    if (!strcmp(s, "periodic")) return 1;
+    return -1;
+}
+static const int kReconGhosts[5] = {1, 2, 2, 3, 4};
+
+// ---------------------------------------------------------------- solver
+
+struct gbfv_solver {
+    int eq, fl, rc, in, periodic, var, nvar, elem;
+    double gamma, cfl;
+    double cell_lengths[3];
+    Grid G;
+    void* U = nullptr;  // current state (padded)
+    void* V = nullptr;  // second state buffer
+    void* L = nullptr;  // stage-0 flux difference
+    StepState* st = nullptr;     // device step state
+    StepState* st_op = nullptr;  // device scratch for operator-level calls
+    StepState* st_host = nullptr;  // pinned mirror
+    int* flag = nullptr;           // device scratch flag
+    int* flag_host = nullptr;
+    void* staging = nullptr;       // pinned host staging (FP32 conversions)
+    cudaStream_t stream = nullptr;
+    double time_interval = 0;
+    long long launches = 0;         // kernels launched since creation
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;  // stage launches while profiling
+    std::vector<cudaEvent_t> event_pool;
+};
+
+static size_t state_bytes(const gbfv_solver* s) { return (size_t)s->nvar * s->G.total * s->elem; }
+
+static void release(gbfv_solver* s) {
+    if (!s) return;
+    for (auto& e : s->events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    for (auto e : s->event_pool) cudaEventDestroy(e);
+    if (s->U) cudaFree(s->U);
+    if (s->V) cudaFree(s->V);
+    if (s->L) cudaFree(s->L);
+    if (s->st) cudaFree(s->st);
+    if (s->st_op) cudaFree(s->st_op);
+    if (s->flag) cudaFree(s->flag);
+    if (s->st_host) cudaFreeHost(s->st_host);
+    if (s->flag_host) cudaFreeHost(s->flag_host);
+    if (s->staging) cudaFreeHost(s->staging);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+extern "C" {
+
+const char* gbfv_last_error(void) { return g_err.c_str(); }
+const char* gbfv_version(void) { return "gbfv 0.1 sm_103a"; }
+
+int gbfv_ghost_cells(const char* reconstruction) {
+    const int rc = parse_recon(reconstruction);
+    if (rc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown reconstruction");
+    return kReconGhosts[rc];
+}
+
+int gbfv_num_variables(const char* equation) {
+    const int eq = parse_eq(equation);
+    if (eq < 0) return fail(GBFV_ERR_ARGUMENT, "unknown equation");
+    return eq == EQ_BURGERS ? 1 : eq + 2;
+}
+
+int gbfv_create(const gbfv_desc* d, gbfv_solver** out) {
+    if (!d || !out) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    const int eq = parse_eq(d->equation), fl = parse_flux(d->flux), rc = parse_recon(d->reconstruction);
+    const int in = parse_integrator(d->integrator), bc = parse_bc(d->boundary);
+    if (eq < 0) return fail(GBFV_ERR_ARGUMENT, "unknown equation");
+    if (fl < 0) return fail(GBFV_ERR_ARGUMENT, "unknown flux");
+    if (rc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown reconstruction");
+    if (in < 0) return fail(GBFV_ERR_ARGUMENT, "unknown integrator");
+    if (bc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown boundary");
+    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV))
+        return fail(GBFV_ERR_UNSUPPORTED, "flux does not apply to this equation");
+    if (d->precision < 0 || d->precision >= NUM_VARIANTS) return fail(GBFV_ERR_ARGUMENT, "bad precision");
+    for (int k = 0; k < 3; ++k)
+        if (d->n[k] < 1) return fail(GBFV_ERR_ARGUMENT, "grid dimensions must be >= 1");
+    const int dim = d->n[2] > 1 ? 3 : (d->n[1] > 1 ? 2 : 1);
+    if (eq != EQ_BURGERS && eq != dim)
+        return fail(GBFV_ERR_UNSUPPORTED, "euler<d> needs a d-dimensional grid");
+    const int g = kReconGhosts[rc];
+    for (int k = 0; k < dim; ++k)
+        if (d->n[k] < g) return fail(GBFV_ERR_UNSUPPORTED, "every active dimension needs at least as many cells as ghost cells");
+    Registry& R = registry();
+    if (!R.stage[d->precision][eq][fl][rc][dim - 1]) return fail(GBFV_ERR_UNSUPPORTED, "no kernel for this combination");
+
+    gbfv_solver* s = new gbfv_solver();
+    s->eq = eq; s->fl = fl; s->rc = rc; s->in = in; s->periodic = bc; s->var = d->precision;
+    s->nvar = eq == EQ_BURGERS ? 1 : eq + 2;
+    s->elem = d->precision == VAR_F32 ? 4 : 8;
+    s->gamma = d->gamma;
+    s->cfl = d->cfl;
+    s->G.dim = dim;
+    long long total = 1;
+    for (int k = 0; k < 3; ++k) {
+        s->G.n[k] = d->n[k];
+        s->G.g[k] = k < dim ? g : 0;
+        s->G.t[k] = d->n[k] + 2 * s->G.g[k];
+        total *= s->G.t[k];
+    }
+    s->G.total = total;
+    // Grid cell lengths; inactive dimensions get 1 (alsfvm/src/grid/Grid.cpp:24-42).
+    for (int k = 0; k < 3; ++k) s->cell_lengths[k] = (d->upper[k] - d->lower[k]) / d->n[k];
+    if (d->n[1] == 1) s->cell_lengths[1] = 1;
+    if (d->n[2] == 1) s->cell_lengths[2] = 1;
+
+    const size_t bytes = state_bytes(s);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&s->U, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->V, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->L, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->st, sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMalloc(&s->st_op, sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMalloc(&s->flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->st_host, sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->flag_host, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->U, 0, bytes, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->V, 0, bytes, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->L, 0, bytes, s->stream);
+    if (e == cudaSuccess) {
+        StepState z;
+        std::memset(&z, 0, sizeof z);
+        z.number_saved = 1;
+        z.done = 1;
+        *s->st_host = z;
+        e = cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    }
+    if (e != cudaSuccess) {
+        const int code = (e == cudaErrorMemoryAllocation) ? GBFV_ERR_MEMORY : GBFV_ERR_CUDA;
+        release(s);
+        return fail(code, std::string("gbfv_create: ") + cudaGetErrorString(e));
+    }
+    *out = s;
+    return GBFV_OK;
+}
+
+int gbfv_destroy(gbfv_solver* s) {
+    if (!s) return GBFV_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    release(s);
+    return GBFV_OK;
+}
+
+int gbfv_extents(const gbfv_solver* s, int t[3], long long* total) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    if (t)
+        for (int k = 0; k < 3; ++k) t[k] = s->G.t[k];
+    if (total) *total = s->G.total;
+    return GBFV_OK;
+}
+
+static int reset_time(gbfv_solver* s) {
+    StepState z;
+    std::memset(&z, 0, sizeof z);
+    z.number_saved = 1;
+    z.done = 1;
+    *s->st_host = z;
+    CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return GBFV_OK;
+}
+
+static int upload(gbfv_solver* s, const double* host) {
+    const size_t n = (size_t)s->nvar * s->G.total;
+    if (s->elem == 8) {
+        CUDA_TRY(cudaMemcpyAsync(s->U, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        if (!s->staging) CUDA_TRY(cudaMallocHost(&s->staging, n * 4));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        float* f = static_cast<float*>(s->staging);
+        for (size_t i = 0; i < n; ++i) f[i] = (float)host[i];
+        CUDA_TRY(cudaMemcpyAsync(s->U, f, n * 4, cudaMemcpyHostToDevice, s->stream));
+    }
+    return GBFV_OK;
+}
+
+static int download(gbfv_solver* s, double* host) {
+    const size_t n = (size_t)s->nvar * s->G.total;
+    if (s->elem == 8) {
+        CUDA_TRY(cudaMemcpyAsync(host, s->U, n * 8, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+    } else {
+        if (!s->staging) CUDA_TRY(cudaMallocHost(&s->staging, n * 4));
+        CUDA_TRY(cudaMemcpyAsync(s->staging, s->U, n * 4, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        const float* f = static_cast<const float*>(s->staging);
+        for (size_t i = 0; i < n; ++i) host[i] = (double)f[i];
+    }
+    return GBFV_OK;
+}
+
+static int launch_boundary(gbfv_solver* s, void* U) {
+    const int bs = 256;
+    const unsigned nb = (unsigned)((s->G.total + bs - 1) / bs);
+    if (s->elem == 8)
+        boundary_kernel<double><<<nb, bs, 0, s->stream>>>((double*)U, s->G, s->nvar, s->periodic);
+    else
+        boundary_kernel<float><<<nb, bs, 0, s->stream>>>((float*)U, s->G, s->nvar, s->periodic);
+    CUDA_TRY(cudaGetLastError());
+    return GBFV_OK;
+}
+
+int gbfv_set_state(gbfv_solver* s, const double* host) {
+    if (!s || !host) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    int r = upload(s, host);
+    if (r) return r;
+    return reset_time(s);
+}
+
+int gbfv_get_state(gbfv_solver* s, double* host) {
+    if (!s || !host) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    return download(s, host);
+}
+
+int gbfv_state_device(gbfv_solver* s, void** dev) {
+    if (!s || !dev) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *dev = s->U;
+    return GBFV_OK;
+}
+
+// Primitive -> conserved for interior cells, then the ghost fill: the values
+// Simulator::setInitialValue produces (conversion CPUCellComputer::
+// computeFromPrimitive with Euler::computeConserved, Euler.hpp:236-245).
+int gbfv_set_primitive(gbfv_solver* s, const double* prim) {
+    if (!s || !prim) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    const Grid& G = s->G;
+    const long long total = G.total;
+    const long long cells = (long long)G.n[0] * G.n[1] * G.n[2];
+    std::vector<double> cons((size_t)s->nvar * total, 0.0);
+    const int nsd = s->eq == EQ_BURGERS ? 1 : s->eq;
+    const double gamma = s->gamma;
+    for (int z = 0; z < G.n[2]; ++z)
+        for (int y = 0; y < G.n[1]; ++y)
+            for (int x = 0; x < G.n[0]; ++x) {
+                const long long ic = ((long long)z * G.n[1] + y) * G.n[0] + x;
+                const long long ip = ((long long)(z + G.g[2]) * G.t[1] + (y + G.g[1])) * G.t[0] + (x + G.g[0]);
+                if (s->eq == EQ_BURGERS) {
+                    cons[ip] = prim[ic];
+                    continue;
+                }
+                const double rho = prim[ic];
+                double u[3];
+                for (int k = 0; k < nsd; ++k) u[k] = prim[(1 + k) * cells + ic];
+                const double p = prim[(1 + nsd) * cells + ic];
+                double dot = u[0] * u[0];
+                for (int k = 1; k < nsd; ++k) dot = dot + u[k] * u[k];
+                cons[ip] = rho;
+                for (int k = 0; k < nsd; ++k) cons[(1 + k) * total + ip] = u[k] * rho;
+                cons[(1 + nsd) * total + ip] = p / (gamma - 1) + 0.5 * rho * dot;
+            }
+    int r = upload(s, cons.data());
+    if (r) return r;
+    r = launch_boundary(s, s->U);
+    if (r) return r;
+    return reset_time(s);
+}
+
+static StageArgs stage_args(gbfv_solver* s, StepState* st, const void* in, const void* u0, const void* l0,
+                            void* out, int mode, int check) {
+    StageArgs a;
+    a.in = in;
+    a.u0 = u0;
+    a.l0 = l0;
+    a.out = out;
+    a.st = st;
+    a.G = s->G;
+    a.gamma = s->gamma;
+    a.mode = mode;
+    a.periodic = s->periodic;
+    a.check = check;
+    return a;
+}
+
+static cudaEvent_t take_event(gbfv_solver* s) {
+    if (!s->event_pool.empty()) {
+        cudaEvent_t e = s->event_pool.back();
+        s->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// One stage launch, bracketed by events while profiling.
+static int launch_stage(gbfv_solver* s, StageLauncher stage, const StageArgs& a) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (s->profiling) {
+        e0 = take_event(s);
+        e1 = take_event(s);
+        CUDA_TRY(cudaEventRecord(e0, s->stream));
+    }
+    LAUNCH_TRY(stage(a, s->stream));
+    s->launches += 1;
+    if (s->profiling) {
+        CUDA_TRY(cudaEventRecord(e1, s->stream));
+        s->events.emplace_back(e0, e1);
+    }
+    return GBFV_OK;
+}
+
+#define STAGE_TRY(x)       \
+    do {                   \
+        int r_ = (x);      \
+        if (r_) return r_; \
+    } while (0)
+
+// Enqueues one time step; every kernel returns at once when st->done is set.
+static int enqueue_step(gbfv_solver* s, const StepParams& P) {
+    Registry& R = registry();
+    const StageLauncher stage = R.stage[s->var][s->eq][s->fl][s->rc][s->G.dim - 1];
+    cudaStream_t q = s->stream;
+    STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->U, s->U, nullptr, s->L, MODE_L, 0)));
+    dt_kernel<<<1, 1, 0, q>>>(s->st, P);
+    CUDA_TRY(cudaGetLastError());
+    s->launches += 2;  // dt + finish
+    if (s->in == IN_RK3) {
+        STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->U, s->U, s->L, s->V, MODE_RK3_S1, 0)));
+        STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->V, s->U, nullptr, s->U, MODE_RK3_S2, 1)));
+    } else if (s->in == IN_RK2) {
+        STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->U, s->U, s->L, s->V, MODE_RK2_S1, 1)));
+        s->launches += 1;
+        const long long n = (long long)s->nvar * s->G.total;
+        if (s->elem == 8)
+            copy_state_kernel<double><<<1184, 256, 0, q>>>(s->st, (const double*)s->V, (double*)s->U, n);
+        else
+            copy_state_kernel<float><<<1184, 256, 0, q>>>(s->st, (const float*)s->V, (float*)s->U, n);
+        CUDA_TRY(cudaGetLastError());
+    } else {
+        LAUNCH_TRY(R.apply[s->var][s->eq](stage_args(s, s->st, s->U, s->U, s->L, s->U, MODE_L, 1), q));
+        s->launches += 1;
+    }
+    finish_kernel<<<1, 1, 0, q>>>(s->st, P);
+    CUDA_TRY(cudaGetLastError());
+    return GBFV_OK;
+}
+
+int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const long long limit = max_steps > 0 ? s->st_host->steps + max_steps : -1;
+    if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
+    StepParams P;
+    P.cfl = s->cfl;
+    for (int k = 0; k < 3; ++k) P.cell_lengths[k] = s->cell_lengths[k];
+    P.end_time = end_time;
+    P.time_interval = number_of_saves > 0 ? s->time_interval : 0.0;
+    P.dim = s->G.dim;
+    begin_kernel<<<1, 1, 0, s->stream>>>(s->st, end_time, limit);
+    CUDA_TRY(cudaGetLastError());
+    s->launches += 1;
+    int chunk = 1;
+    for (;;) {
+        for (int i = 0; i < chunk; ++i) {
+            int r = enqueue_step(s, P);
+            if (r) return r;
+        }
+        CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if (s->st_host->done) break;
+        if (chunk < 64) chunk *= 2;
+    }
+    if (s->st_host->status != 0) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "Simulation state does not obey constraints! At time %.17g, number of timesteps performed %d",
+                 s->st_host->t, s->st_host->failed_step);
+        return fail(GBFV_ERR_CONSTRAINT, msg);
+    }
+    return GBFV_OK;
+}
+
+int gbfv_stream(gbfv_solver* s, void** stream) {
+    if (!s || !stream) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *stream = (void*)s->stream;
+    return GBFV_OK;
+}
+
+int gbfv_profile(gbfv_solver* s, int enable) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    s->profiling = enable != 0;
+    return GBFV_OK;
+}
+
+int gbfv_profile_read(gbfv_solver* s, double* stage_ms, long long* stage_launches, long long* kernel_launches) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double total = 0;
+    for (auto& e : s->events) {
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e.first, e.second));
+        total += ms;
+        s->event_pool.push_back(e.first);
+        s->event_pool.push_back(e.second);
+    }
+    if (stage_ms) *stage_ms = total;
+    if (stage_launches) *stage_launches = (long long)s->events.size();
+    if (kernel_launches) *kernel_launches = s->launches;
+    s->events.clear();
+    return GBFV_OK;
+}
+
+int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (t) *t = s->st_host->t;
+    if (steps) *steps = s->st_host->steps;
+    if (last_dt) *last_dt = s->st_host->dt;
+    return GBFV_OK;
+}
+
+int gbfv_advance_host(gbfv_solver* s, double* host, double end_time, int number_of_saves, int max_steps) {
+    if (!s || !host) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    int r = upload(s, host);
+    if (r) return r;
+    r = gbfv_advance(s, end_time, number_of_saves, max_steps);
+    const int r2 = download(s, host);
+    return r ? r : r2;
+}
+
+// ------------------------------------------------------ operator level
+
+int gbfv_compute_flux(gbfv_solver* s, const void* U, void* out, double ws[3]) {
+    if (!s || !U || !out) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    StepState z;
+    std::memset(&z, 0, sizeof z);
+    CUDA_TRY(cudaMemcpyAsync(s->st_op, &z, sizeof z, cudaMemcpyHostToDevice, s->stream));
+    Registry& R = registry();
+    LAUNCH_TRY(R.stage[s->var][s->eq][s->fl][s->rc][s->G.dim - 1](
+        stage_args(s, s->st_op, U, U, nullptr, out, MODE_L, 0), s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st_op, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (ws)
+        for (int d = 0; d < 3; ++d) {
+            unsigned long long b = s->st_host->ws_bits[d];
+            double v;
+            std::memcpy(&v, &b, sizeof v);
+            ws[d] = d < s->G.dim ? v : 0.0;
+        }
+    return GBFV_OK;
+}
+
+int gbfv_reconstruct(gbfv_solver* s, int direction, const void* U, void* left, void* right) {
+    if (!s || !U || !left || !right) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    if (direction < 0 || direction >= s->G.dim) return fail(GBFV_ERR_ARGUMENT, "bad direction");
+    ReconArgs a;
+    a.in = U;
+    a.left = left;
+    a.right = right;
+    a.G = s->G;
+    a.dir = direction;
+    LAUNCH_TRY(registry().recon[s->var][s->eq][s->rc](a, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return GBFV_OK;
+}
+
+int gbfv_apply_boundary(gbfv_solver* s, void* U) {
+    if (!s || !U) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    int r = launch_boundary(s, U);
+    if (r) return r;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return GBFV_OK;
+}
+
+int gbfv_obeys_constraints(gbfv_solver* s, const void* U, int* ok) {
+    if (!s || !U || !ok) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *s->flag_host = 1;
+    CUDA_TRY(cudaMemcpyAsync(s->flag, s->flag_host, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    CheckArgs a;
+    a.in = U;
+    a.flag = s->flag;
+    a.G = s->G;
+    a.gamma = s->gamma;
+    LAUNCH_TRY(registry().check[s->var][s->eq](a, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->flag_host, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *ok = *s->flag_host;
+    return GBFV_OK;
+}
+
+// ------------------------------------------------------- generator
+
+int gbfv_uniform(int dimension, int sample, double lower, double upper, double* out) {
+    if (dimension <= 0 || sample < 0 || !out) return fail(GBFV_ERR_ARGUMENT, "bad arguments");
+    std::mt19937_64 gen;  // default seed, as the reference's process-wide engine
+    gen.discard((unsigned long long)sample * (unsigned long long)dimension);
+    std::uniform_real_distribution<double> dist{0.0, 1.0};
+    for (int c = 0; c < dimension; ++c) out[c] = dist(gen) * (upper - lower) + lower;
+    return GBFV_OK;
+}
+
+}  // extern "C"

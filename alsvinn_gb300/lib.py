@@ -1,0 +1,283 @@
+"""ctypes binding of the gbfv C ABI (include/gbfv.h).
+
+The library is the in-tree alsvinn_gb300/lib/libgbfv.so. There is no CPU
+fallback: loading fails loudly when the library is missing, and every call
+that returns a negative status raises GbfvError with the library's message.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libgbfv.so")
+
+FP64, FP64_EXACT, FP32 = 0, 1, 2
+OK, ERR_ARGUMENT, ERR_CUDA, ERR_CONSTRAINT, ERR_MEMORY, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5
+
+_c_int3 = ctypes.c_int * 3
+_c_double3 = ctypes.c_double * 3
+
+
+class GbfvError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("gbfv error %d: %s" % (code, message))
+        self.code = code
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [
+        ("equation", ctypes.c_char_p),
+        ("flux", ctypes.c_char_p),
+        ("reconstruction", ctypes.c_char_p),
+        ("integrator", ctypes.c_char_p),
+        ("boundary", ctypes.c_char_p),
+        ("n", ctypes.c_int * 3),
+        ("lower", ctypes.c_double * 3),
+        ("upper", ctypes.c_double * 3),
+        ("gamma", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("precision", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGNATURES = {
+    "gbfv_last_error": (ctypes.c_char_p, []),
+    "gbfv_version": (ctypes.c_char_p, []),
+    "gbfv_ghost_cells": (ctypes.c_int, [ctypes.c_char_p]),
+    "gbfv_num_variables": (ctypes.c_int, [ctypes.c_char_p]),
+    "gbfv_create": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_extents": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_set_primitive": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_set_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_state_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_advance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
+    "gbfv_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_profile_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)]),
+    "gbfv_advance_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_int]),
+    "gbfv_compute_flux": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_double)]),
+    "gbfv_reconstruct": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "gbfv_apply_boundary": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_obeys_constraints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_stats_create": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_stats_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_stats_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_stats_add_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_stats_add_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_stats_merge": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_stats_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_void_p]),
+}
+
+
+def exported_names():
+    """The entry points include/gbfv.h declares."""
+    return sorted(_SIGNATURES)
+
+
+def load():
+    """Loads libgbfv.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("alsvinn_gb300 native library missing: %s (run __graft_entry__.build())" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc < 0:
+        raise GbfvError(rc, load().gbfv_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def ghost_cells(reconstruction):
+    return _check(load().gbfv_ghost_cells(reconstruction.encode()))
+
+
+def num_variables(equation):
+    return _check(load().gbfv_num_variables(equation.encode()))
+
+
+def uniform(dimension, sample, lower=0.0, upper=1.0):
+    out = np.zeros(dimension)
+    _check(load().gbfv_uniform(dimension, sample, lower, upper, _ptr(out)))
+    return out
+
+
+class Solver:
+    """One grid on the GPU: the handle of gbfv_create."""
+
+    def __init__(self, equation, flux, reconstruction, integrator, boundary, n, lower, upper,
+                 gamma=1.4, cfl=0.475, precision=FP64):
+        lib = load()
+        self._keep = [s.encode() for s in (equation, flux, reconstruction, integrator, boundary)]
+        d = _Desc()
+        d.equation, d.flux, d.reconstruction, d.integrator, d.boundary = self._keep
+        d.n = _c_int3(*n)
+        d.lower = _c_double3(*lower)
+        d.upper = _c_double3(*upper)
+        d.gamma = gamma
+        d.cfl = cfl
+        d.precision = precision
+        h = ctypes.c_void_p()
+        _check(lib.gbfv_create(ctypes.byref(d), ctypes.byref(h)))
+        self.h = h
+        self.equation = equation
+        self.precision = precision
+        self.n = tuple(n)
+        self.nvar = num_variables(equation)
+        t = _c_int3()
+        total = ctypes.c_longlong()
+        _check(lib.gbfv_extents(h, t, ctypes.byref(total)))
+        self.padded = tuple(t)
+        self.total = total.value
+        self.dtype = np.float32 if precision == FP32 else np.float64
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_primitive(self, prim):
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        _check(load().gbfv_set_primitive(self.h, _ptr(prim)))
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.size == self.nvar * self.total
+        _check(load().gbfv_set_state(self.h, _ptr(U)))
+
+    def get_state(self):
+        U = np.zeros((self.nvar, self.total))
+        _check(load().gbfv_get_state(self.h, _ptr(U)))
+        return U
+
+    def state_device(self):
+        p = ctypes.c_void_p()
+        _check(load().gbfv_state_device(self.h, ctypes.byref(p)))
+        return p.value
+
+    def advance(self, end_time, number_of_saves=0, max_steps=0):
+        return _check(load().gbfv_advance(self.h, end_time, number_of_saves, max_steps))
+
+    def advance_host(self, U, end_time, number_of_saves=0, max_steps=0):
+        assert U.dtype == np.float64 and U.flags.c_contiguous and U.size == self.nvar * self.total
+        return _check(load().gbfv_advance_host(self.h, _ptr(U), end_time, number_of_saves, max_steps))
+
+    def time(self):
+        t = ctypes.c_double()
+        s = ctypes.c_longlong()
+        dt = ctypes.c_double()
+        _check(load().gbfv_time(self.h, ctypes.byref(t), ctypes.byref(s), ctypes.byref(dt)))
+        return t.value, s.value, dt.value
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        _check(load().gbfv_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+    def profile(self, enable=True):
+        _check(load().gbfv_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        k = ctypes.c_longlong()
+        _check(load().gbfv_profile_read(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(k)))
+        return ms.value, n.value, k.value
+
+    def compute_flux(self, state_dev, out_dev):
+        ws = _c_double3()
+        _check(load().gbfv_compute_flux(self.h, ctypes.c_void_p(state_dev), ctypes.c_void_p(out_dev), ws))
+        return list(ws)
+
+    def reconstruct(self, direction, state_dev, left_dev, right_dev):
+        _check(load().gbfv_reconstruct(self.h, direction, ctypes.c_void_p(state_dev), ctypes.c_void_p(left_dev),
+                                       ctypes.c_void_p(right_dev)))
+
+    def apply_boundary(self, state_dev):
+        _check(load().gbfv_apply_boundary(self.h, ctypes.c_void_p(state_dev)))
+
+    def obeys_constraints(self, state_dev):
+        ok = ctypes.c_int()
+        _check(load().gbfv_obeys_constraints(self.h, ctypes.c_void_p(state_dev), ctypes.byref(ok)))
+        return bool(ok.value)
+
+
+class Stats:
+    """Streaming FP64 mean / variance (gbfv_stats_*)."""
+
+    def __init__(self, count):
+        h = ctypes.c_void_p()
+        _check(load().gbfv_stats_create(count, ctypes.byref(h)))
+        self.h = h
+        self.count = count
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_stats_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self):
+        _check(load().gbfv_stats_reset(self.h))
+
+    def add_device(self, ptr, precision=FP64):
+        _check(load().gbfv_stats_add_device(self.h, ctypes.c_void_p(ptr), precision))
+
+    def add_host(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        assert x.size == self.count
+        _check(load().gbfv_stats_add_host(self.h, _ptr(x)))
+
+    def merge(self, other):
+        _check(load().gbfv_stats_merge(self.h, other.h))
+
+    def result(self):
+        m = np.zeros(self.count)
+        v = np.zeros(self.count)
+        n = ctypes.c_longlong()
+        _check(load().gbfv_stats_result(self.h, _ptr(m), _ptr(v), ctypes.byref(n)))
+        return m, v, n.value

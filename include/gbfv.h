@@ -1,0 +1,193 @@
+/* gbfv: GB300 finite-volume step and ensemble statistics, C ABI.
+ *
+ * A drop-in for the hot path of alsvinn's alsfvm explicit finite-volume step
+ * (reconstruction, numerical flux, flux divergence, SSP Runge-Kutta stages,
+ * ghost cells, CFL time step) and alsuq's mean/variance statistics, running on
+ * one GB300 GPU. Plain pointers and sizes only; no C++ or torch types.
+ *
+ * Conventions
+ *  - Every function returns 0 (GBFV_OK) or a negative gbfv_status; nothing
+ *    throws across this boundary. gbfv_last_error() gives the message of the
+ *    calling thread's last failure.
+ *  - State layout is the reference Volume's: one padded array per conserved
+ *    variable, x fastest, (nx+2g)(ny+2g)(nz+2g) values, ghost cells only in
+ *    active dimensions, the nvar arrays back to back
+ *    (alsfvm/src/volume/Volume.cpp:44-60, alsfvm/include/alsfvm/memory/View.hpp:116-118).
+ *  - Host buffers are owned by the caller; device buffers named *_dev are
+ *    device pointers owned by the caller; a handle owns its internal device
+ *    state. A handle is used by one host thread at a time and issues its work
+ *    on its own CUDA stream.
+ *  - Names are the reference's XML spellings (alsfvm/src/config/SimulatorSetup.cpp:
+ *    122-132): equation "euler1|euler2|euler3|burgers", flux "hll|hll3|godunov",
+ *    reconstruction "none|weno2|eno2|eno3|eno4", integrator
+ *    "forwardeuler|rungekutta2|rungekutta3", boundary "neumann|periodic".
+ */
+#ifndef GBFV_H
+#define GBFV_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBFV_OK = 0,
+    GBFV_ERR_ARGUMENT = -1,     /* bad name, size or pointer */
+    GBFV_ERR_CUDA = -2,         /* a CUDA runtime call failed */
+    GBFV_ERR_CONSTRAINT = -3,   /* the state broke rho > 0, p > 0 or finiteness */
+    GBFV_ERR_MEMORY = -4,       /* device or host allocation failed */
+    GBFV_ERR_UNSUPPORTED = -5   /* combination not provided */
+} gbfv_status;
+
+/* Arithmetic of the state and of the step. */
+typedef enum {
+    GBFV_FP64 = 0,        /* FP64 state, FP64 arithmetic: the drop-in path */
+    GBFV_FP64_EXACT = 1,  /* FP64, reference operation order, no contraction:
+                             bit-identical to the reference CPU path */
+    GBFV_FP32 = 2         /* FP32 state and arithmetic; dt, wave speeds and
+                             statistics in FP64 */
+} gbfv_precision;
+
+typedef struct {
+    const char* equation;
+    const char* flux;
+    const char* reconstruction;
+    const char* integrator;
+    const char* boundary;
+    int n[3];             /* interior cells; 1 in inactive dimensions */
+    double lower[3];      /* grid lower corner (Grid origin) */
+    double upper[3];      /* grid upper corner */
+    double gamma;         /* Euler gamma (EulerParameters, default 1.4) */
+    double cfl;           /* CFL number */
+    int precision;        /* gbfv_precision */
+} gbfv_desc;
+
+typedef struct gbfv_solver gbfv_solver;
+
+const char* gbfv_last_error(void);
+const char* gbfv_version(void);
+
+/* Ghost cells the reference allocates for a reconstruction:
+ * max(flux stencil - 1, reconstruction ghosts)
+ * (replaces NumericalFluxCPU::getNumberOfGhostCells,
+ * alsfvm/src/numflux/NumericalFluxCPU.cpp:226-231). */
+int gbfv_ghost_cells(const char* reconstruction);
+
+/* Number of conserved variables of an equation (3, 4, 5 or 1). */
+int gbfv_num_variables(const char* equation);
+
+/* ----------------------------------------------------------- solver */
+
+/* Creates a solver: device state, scratch and stream for one grid
+ * (replaces the Simulator construction, alsfvm/src/simulator/Simulator.cpp:26-64). */
+int gbfv_create(const gbfv_desc* desc, gbfv_solver** out);
+int gbfv_destroy(gbfv_solver* s);
+
+/* Padded extents (t[3]) and total cells per variable. */
+int gbfv_extents(const gbfv_solver* s, int t[3], long long* total);
+
+/* Sets the state from interior primitive variables (rho, u..., p) or (u),
+ * nvar * nx*ny*nz doubles, x fastest: converts to conserved variables and
+ * fills the ghost cells (replaces Simulator::setInitialValue,
+ * alsfvm/src/simulator/Simulator.cpp:117-162). Resets time and step count. */
+int gbfv_set_primitive(gbfv_solver* s, const double* prim_host);
+
+/* Sets / reads the padded conserved state (nvar * total doubles) from / to
+ * host memory (replaces Simulator::setSimulationState, Simulator.cpp:104-107,
+ * and the Volume copy to host). gbfv_set_state resets time and step count. */
+int gbfv_set_state(gbfv_solver* s, const double* state_host);
+int gbfv_get_state(gbfv_solver* s, double* state_host);
+
+/* Device pointer of the current padded state (nvar * total values of the
+ * solver's precision); valid until the next step. */
+int gbfv_state_device(gbfv_solver* s, void** state_dev);
+
+/* Advances up to max_steps time steps (max_steps <= 0: no step limit) or until
+ * t >= end_time, whichever comes first (replaces the alsvinncli loop
+ * `while (!atEnd()) performStep()`, alsvinncli/src/main.cpp:217-232, with
+ * Simulator::performStep, Simulator.cpp:81-85, 191-214). number_of_saves > 0
+ * attaches the FixedIntervalWriter dt clamp with interval end_time /
+ * number_of_saves (alsfvm/src/io/FixedIntervalWriter.cpp:45-53); the clamp
+ * persists across calls. Returns GBFV_ERR_CONSTRAINT if a step broke the
+ * constraint check (CPUCellComputer::obeysConstraints). */
+int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps);
+
+/* The CUDA stream (cudaStream_t) the solver issues its work on. */
+int gbfv_stream(gbfv_solver* s, void** stream);
+
+/* Per-launch timing of the step kernels with CUDA events on the solver's
+ * stream (the GB300 counterpart of the reference's ALSVINN_TIME_BLOCK timers,
+ * alsutils/include/alsutils/timer/Timer.hpp:9-50). While enabled, every stage
+ * launch is bracketed by events; gbfv_profile_read sums their durations and
+ * resets the record. kernel_launches counts every kernel the solver launched
+ * since creation. */
+int gbfv_profile(gbfv_solver* s, int enable);
+int gbfv_profile_read(gbfv_solver* s, double* stage_ms, long long* stage_launches, long long* kernel_launches);
+
+/* Time, step count and the dt of the last step. */
+int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt);
+
+/* Same as gbfv_advance, reading the state from host memory first and writing
+ * it back after: the call a host-side Volume owner makes per step. */
+int gbfv_advance_host(gbfv_solver* s, double* state_host_inout, double end_time, int number_of_saves,
+                      int max_steps);
+
+/* --------------------------------------------------- operator level */
+
+/* One evaluation of the spatial operator on a caller state: out_dev gets
+ * sum_d (F_{i-1/2} - F_{i+1/2}) (unscaled) on interior cells and its ghost
+ * images, ws the maximum face wave speed per direction (0 for inactive
+ * directions). state_dev and out_dev are padded device arrays of the solver's
+ * precision (replaces NumericalFlux::computeFlux,
+ * alsfvm/include/alsfvm/numflux/NumericalFlux.hpp:44-48, as called by
+ * ConservedSystem::operator(), alsfvm/src/simulator/ConservedSystem.cpp:31-103). */
+int gbfv_compute_flux(gbfv_solver* s, const void* state_dev, void* out_dev, double ws[3]);
+
+/* Reconstruction in one direction (indicator variable 0) over the reference's
+ * cell range; left_dev / right_dev padded device arrays (replaces
+ * Reconstruction::performReconstruction,
+ * alsfvm/include/alsfvm/reconstruction/Reconstruction.hpp:46-51). */
+int gbfv_reconstruct(gbfv_solver* s, int direction, const void* state_dev, void* left_dev, void* right_dev);
+
+/* Ghost-cell fill of a padded device state in place (replaces
+ * Boundary::applyBoundaryConditions, alsfvm/include/alsfvm/boundary/Boundary.hpp:30-31). */
+int gbfv_apply_boundary(gbfv_solver* s, void* state_dev);
+
+/* Constraint check over a padded device state: *ok = 1 if every cell is finite
+ * with rho > 0, p > 0 (replaces CellComputer::obeysConstraints,
+ * alsfvm/include/alsfvm/equation/CellComputer.hpp:61). */
+int gbfv_obeys_constraints(gbfv_solver* s, const void* state_dev, int* ok);
+
+/* ------------------------------------------------------- statistics */
+
+typedef struct gbfv_stats gbfv_stats;
+
+/* Streaming FP64 Welford mean / variance over `count` values per sample
+ * (replaces alsuq's MeanVariance with StatisticsHelper::combineStatistics on
+ * one rank, alsuq/src/stats/MeanVariance.cpp:30-67,
+ * alsuq/src/stats/StatisticsHelper.cpp:35-79; the variance is the population
+ * variance). */
+int gbfv_stats_create(long long count, gbfv_stats** out);
+int gbfv_stats_destroy(gbfv_stats* st);
+int gbfv_stats_reset(gbfv_stats* st);
+/* Adds one sample from device memory (precision 0: double, 2: float). */
+int gbfv_stats_add_device(gbfv_stats* st, const void* sample_dev, int precision);
+/* Adds one sample from host memory. */
+int gbfv_stats_add_host(gbfv_stats* st, const double* sample_host);
+/* Merges another accumulator into st (Chan et al. pairwise combination). */
+int gbfv_stats_merge(gbfv_stats* st, const gbfv_stats* other);
+/* Writes mean and variance to host arrays of `count` doubles. */
+int gbfv_stats_result(gbfv_stats* st, double* mean_host, double* var_host, long long* samples);
+
+/* ------------------------------------------------------- generator */
+
+/* Uniform draws of the reference's sample generator: draw number
+ * sample * dimension + c of the default-seeded mt19937_64 through
+ * uniform_real_distribution(0,1), scaled to [lower, upper]
+ * (replaces STLMersenne + Uniform, alsuq/src/generator/STLMersenne.cpp:38-85,
+ * alsuq/src/distribution/Uniform.cpp:27-34). */
+int gbfv_uniform(int dimension, int sample, double lower, double upper, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,123 @@
+"""ctypes binding of the CPU oracle (oracle/libfvoracle.so).
+
+TEST INFRASTRUCTURE: imported only by tests/, the smoke check and the CPU
+baseline leg of bench.py, as the checker. Signatures mirror oracle/fvoracle.h.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfvoracle.so")
+D = ctypes.c_double
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            import sys
+            sys.path.insert(0, os.path.dirname(HERE))
+            from alsvinn_gb300 import _build
+            _build.build_oracle()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.fv_last_error.restype = ctypes.c_char_p
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _i3(v):
+    return (ctypes.c_int * 3)(*v)
+
+
+def _d3(v):
+    return (ctypes.c_double * 3)(*v)
+
+
+def _check(rc):
+    if rc < 0:
+        raise RuntimeError("oracle: " + load().fv_last_error().decode())
+    return rc
+
+
+def set_threads(n):
+    load().fv_set_threads(int(n))
+
+
+def get_threads():
+    return load().fv_get_threads()
+
+
+def ghost_cells(recon):
+    return _check(load().fv_ghost_cells(recon.encode()))
+
+
+def boundary(bc, n, ghosts, U):
+    U = np.ascontiguousarray(U, dtype=np.float64).copy()
+    _check(load().fv_boundary(bc.encode(), _i3(n), ghosts, U.shape[0], _p(U)))
+    return U
+
+
+def compute_flux(equation, flux, recon, n, gamma, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    out = np.zeros_like(U)
+    ws = (D * 3)()
+    _check(load().fv_compute_flux(equation.encode(), flux.encode(), recon.encode(), _i3(n), D(gamma), _p(U),
+                                  _p(out), ws))
+    return out, list(ws)
+
+
+def reconstruct(equation, recon, n, gamma, direction, U, left=None, right=None):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    left = np.zeros_like(U) if left is None else left.copy()
+    right = np.zeros_like(U) if right is None else right.copy()
+    _check(load().fv_reconstruct(equation.encode(), recon.encode(), _i3(n), D(gamma), direction, _p(U),
+                                 _p(left), _p(right)))
+    return left, right
+
+
+def run(equation, flux, recon, integrator, bc, n, lower, upper, gamma, cfl, end_time, number_of_saves,
+        max_steps, prim, ghosts, nvar):
+    dim = 3 if n[2] > 1 else (2 if n[1] > 1 else 1)
+    t = [n[d] + 2 * ghosts if d < dim else n[d] for d in range(3)]
+    out = np.zeros((nvar, t[0] * t[1] * t[2]))
+    prim = np.ascontiguousarray(prim, dtype=np.float64)
+    tt = D()
+    st = ctypes.c_int()
+    rc = load().fv_run(equation.encode(), flux.encode(), recon.encode(), integrator.encode(), bc.encode(),
+                       _i3(n), _d3(lower), _d3(upper), D(gamma), D(cfl), D(end_time), number_of_saves,
+                       max_steps, _p(prim), _p(out), ctypes.byref(tt), ctypes.byref(st), None, 0)
+    return rc, out, tt.value, st.value
+
+
+def prim_to_cons(equation, n, ghosts, gamma, prim_padded):
+    prim_padded = np.ascontiguousarray(prim_padded, dtype=np.float64)
+    out = np.zeros_like(prim_padded)
+    _check(load().fv_prim_to_cons(equation.encode(), _i3(n), ghosts, D(gamma), _p(prim_padded), _p(out)))
+    return out
+
+
+def obeys_constraints(equation, n, ghosts, gamma, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    return bool(_check(load().fv_obeys_constraints(equation.encode(), _i3(n), ghosts, D(gamma), _p(U))))
+
+
+def uniform(dimension, sample, lower=0.0, upper=1.0):
+    out = np.zeros(dimension)
+    _check(load().fv_uniform(dimension, sample, D(lower), D(upper), _p(out)))
+    return out
+
+
+def meanvar(samples):
+    samples = [np.ascontiguousarray(s, dtype=np.float64) for s in samples]
+    count = samples[0].size
+    arr = (ctypes.c_void_p * len(samples))(*[s.ctypes.data for s in samples])
+    m = np.zeros(samples[0].shape)
+    v = np.zeros(samples[0].shape)
+    _check(load().fv_meanvar(ctypes.c_long(count), len(samples), arr, _p(m), _p(v)))
+    return m, v

@@ -1,0 +1,290 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+fixtures generated from the reference itself.
+
+Tolerances (relative L1 per conserved variable over interior cells,
+sum|a-b| / sum|b|):
+  FP64_EXACT  bit-identical (0) to the reference CPU path
+  FP64        <= 1e-10 (the drop-in contract); observed ~1e-14
+  FP32        state-scaled L1 (sum|a-b| over sum|rho|, per variable) <= 1e-4 against
+              the FP64 reference on smooth and Kelvin-Helmholtz runs; 2e-2 for the
+              Burgers ENO4 run through a shock, where FP32 rounding flips a few ENO
+              stencil choices next to the discontinuity
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import workloads
+from alsvinn_gb300 import lib
+from conftest import interior, rel_l1
+from oracle import fvoracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FLUX_GRIDS = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
+TOL = {lib.FP64_EXACT: 0.0, lib.FP64: 1e-10, lib.FP32: 1e-4}
+FP32_TOL = {"burgers96_eno4_rk3": 2e-2}
+
+
+def scaled_l1(a, b):
+    """Per-variable L1 error over the L1 norm of variable 0 (density for Euler,
+    u for Burgers): an error measure that stays meaningful for variables that
+    start at zero."""
+    a = a.reshape(a.shape[0], -1)
+    b = b.reshape(b.shape[0], -1)
+    return np.abs(a - b).sum(axis=1) / np.abs(b[0]).sum()
+
+
+def dev(a, dtype=np.float64):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).cuda()
+
+
+def host(t):
+    return t.double().cpu().numpy()
+
+
+def solver(eq, flux, recon, n, precision, integrator="rungekutta3", boundary="periodic", lower=(0, 0, 0),
+           upper=(1, 1, 1), cfl=0.475, gamma=1.4):
+    return lib.Solver(eq, flux, recon, integrator, boundary, n, lower, upper, gamma=gamma, cfl=cfl,
+                      precision=precision)
+
+
+def flux_keys():
+    z = np.load(os.path.join(GOLDEN, "flux.npz"))
+    return sorted({k.rsplit("_", 1)[0] for k in z.files})
+
+
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP32])
+@pytest.mark.parametrize("key", flux_keys())
+def test_compute_flux_matches_reference(cuda_device, key, precision):
+    z = np.load(os.path.join(GOLDEN, "flux.npz"))
+    eq, fl, rc = key.split("_")
+    n = FLUX_GRIDS[eq]
+    g = workloads.ghost_cells(rc)
+    U = z[key + "_U"]
+    ref, ref_ws = z[key + "_L"], z[key + "_ws"]
+    dt = np.float32 if precision == lib.FP32 else np.float64
+    with solver(eq, fl, rc, n, precision) as s:
+        Ud = dev(U, dt)
+        out = dev(np.zeros_like(U), dt)
+        ws = s.compute_flux(Ud.data_ptr(), out.data_ptr())
+        got = host(out)
+    a, b = interior(got, n, g), interior(ref, n, g)
+    if precision == lib.FP64_EXACT:
+        assert np.array_equal(a, b)
+        assert ws == list(ref_ws)
+    else:
+        # flux differences of a smooth field are small: compare against the
+        # flux magnitude scale rather than the difference itself
+        err = np.abs(a - b).reshape(a.shape[0], -1).sum(1) / np.maximum(np.abs(b).reshape(b.shape[0], -1).sum(1), 1e-30)
+        tol = 1e-10 if precision == lib.FP64 else 5e-3
+        assert (err <= tol).all(), err
+        assert np.allclose(ws, ref_ws, rtol=1e-13 if precision == lib.FP64 else 1e-5, atol=0)
+
+
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64])
+@pytest.mark.parametrize("recon", workloads.RECONSTRUCTIONS)
+@pytest.mark.parametrize("eq", ["euler2", "burgers"])
+def test_reconstruct_matches_oracle(cuda_device, eq, recon, precision):
+    n = (12, 10, 1)
+    g = workloads.ghost_cells(recon)
+    t = workloads.padded_shape(n, g)
+    U = workloads.smooth_random_state(eq, t, np.random.default_rng(5))
+    flux = "godunov" if eq == "burgers" else "hll3"
+    with solver(eq, flux, recon, n, precision) as s:
+        for d in range(2):
+            l_ref, r_ref = fvoracle.reconstruct(eq, recon, n, 1.4, d, U)
+            Ud = dev(U)
+            Ld = dev(np.zeros_like(U))
+            Rd = dev(np.zeros_like(U))
+            s.reconstruct(d, Ud.data_ptr(), Ld.data_ptr(), Rd.data_ptr())
+            if precision == lib.FP64_EXACT:
+                assert np.array_equal(host(Ld), l_ref)
+                assert np.array_equal(host(Rd), r_ref)
+            else:
+                assert np.allclose(host(Ld), l_ref, rtol=1e-13, atol=1e-14)
+                assert np.allclose(host(Rd), r_ref, rtol=1e-13, atol=1e-14)
+
+
+def test_boundary_matches_reference(cuda_device):
+    z = np.load(os.path.join(GOLDEN, "boundary.npz"))
+    recon_for_g = {1: "none", 2: "weno2", 3: "eno3", 4: "eno4"}
+    for key in z.files:
+        bc, dims, gs = key.split("_")
+        n = tuple(int(v) for v in dims.split("x"))
+        g = int(gs[1:])
+        t = workloads.padded_shape(n, g)
+        tot = t[0] * t[1] * t[2]
+        U = np.arange(tot, dtype=np.float64).reshape(1, tot) + 0.25
+        with solver("burgers", "godunov", recon_for_g[g], n, lib.FP64, boundary=bc) as s:
+            Ud = dev(U)
+            s.apply_boundary(Ud.data_ptr())
+            assert np.array_equal(host(Ud), z[key]), key
+
+
+def run_gpu(case, precision, prim=None):
+    with solver(case["equation"], case["flux"], case["recon"], case["n"], precision,
+                integrator=case["integrator"], boundary=case["boundary"], lower=case["lower"],
+                upper=case["upper"], cfl=case["cfl"], gamma=case["gamma"]) as s:
+        s.set_primitive(case["prim"]() if prim is None else prim)
+        s.advance(case["end_time"], case["number_of_saves"], case["max_steps"])
+        t, steps, _ = s.time()
+        return s.get_state(), t, steps
+
+
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP32])
+@pytest.mark.parametrize("name", sorted(workloads.GOLDEN_RUNS))
+def test_run_matches_reference(cuda_device, name, precision):
+    z = np.load(os.path.join(GOLDEN, "runs.npz"))
+    case = workloads.GOLDEN_RUNS[name]
+    g = workloads.ghost_cells(case["recon"])
+    U, t, steps = run_gpu(case, precision, prim=z[name + "_prim"])
+    ref = z[name + "_U"]
+    ref_steps = int(z[name + "_steps"][0])
+    ref_t = float(z[name + "_t"][0])
+    if precision == lib.FP64_EXACT:
+        assert steps == ref_steps and t == ref_t
+        assert np.array_equal(U, ref)
+        return
+    if precision == lib.FP64:
+        assert steps == ref_steps
+        assert abs(t - ref_t) <= 1e-12 * max(1.0, abs(ref_t))
+        err = rel_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+        assert (err <= TOL[precision]).all(), err
+    else:
+        err = scaled_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+        assert (err <= FP32_TOL.get(name, TOL[lib.FP32])).all(), err
+
+
+LARGE = {
+    "sod2048": dict(equation="euler1", flux="hll3", recon="weno2", integrator="rungekutta3", boundary="neumann",
+                    n=(2048, 1, 1), lower=(-5, 0, 0), upper=(5, 1, 1), gamma=1.4, cfl=0.475, end_time=1.3,
+                    number_of_saves=1, max_steps=0, prim=lambda: workloads.sod_prim(2048)),
+    "kh128_50": dict(equation="euler2", flux="hll3", recon="weno2", integrator="rungekutta3", boundary="periodic",
+                     n=(128, 128, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4, cfl=0.4, end_time=2.0,
+                     number_of_saves=0, max_steps=50,
+                     prim=lambda: workloads.kh_prim(128, lib.uniform(40, 0))),
+    "kh_ragged_37x29": dict(equation="euler2", flux="hll", recon="eno3", integrator="rungekutta2",
+                            boundary="neumann", n=(37, 29, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4,
+                            cfl=0.4, end_time=2.0, number_of_saves=0, max_steps=15,
+                            prim=lambda: workloads.kh_prim(37, lib.uniform(40, 1))[:, :37 * 29]),
+    "tg16_10": dict(equation="euler3", flux="hll3", recon="weno2", integrator="rungekutta3", boundary="periodic",
+                    n=(16, 16, 16), lower=(0, 0, 0), upper=(2 * math.pi,) * 3, gamma=1.4, cfl=0.4, end_time=100.0,
+                    number_of_saves=0, max_steps=10, prim=lambda: workloads.tg_prim(16)),
+    "burgers1024": dict(equation="burgers", flux="godunov", recon="weno2", integrator="rungekutta2",
+                        boundary="periodic", n=(1024, 1, 1), lower=(0, 0, 0), upper=(1, 1, 1), gamma=1.4,
+                        cfl=0.475, end_time=0.5, number_of_saves=1, max_steps=0,
+                        prim=lambda: workloads.burgers_prim(1024, 0.25)),
+    "burgers2d_eno2_fe": dict(equation="burgers", flux="godunov", recon="eno2", integrator="forwardeuler",
+                              boundary="neumann", n=(40, 33, 1), lower=(0, 0, 0), upper=(1, 1, 1), gamma=1.4,
+                              cfl=0.4, end_time=0.2, number_of_saves=2, max_steps=0,
+                              prim=lambda: np.sin(np.arange(40 * 33) * 0.05).reshape(1, -1)),
+}
+
+
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64])
+@pytest.mark.parametrize("name", sorted(LARGE))
+def test_larger_runs_match_oracle(cuda_device, name, precision):
+    case = LARGE[name]
+    g = workloads.ghost_cells(case["recon"])
+    prim = case["prim"]()
+    rc, ref, ref_t, ref_steps = fvoracle.run(case["equation"], case["flux"], case["recon"], case["integrator"],
+                                             case["boundary"], case["n"], case["lower"], case["upper"],
+                                             case["gamma"], case["cfl"], case["end_time"],
+                                             case["number_of_saves"], case["max_steps"], prim, g,
+                                             workloads.NVAR[case["equation"]])
+    assert rc == 0
+    U, t, steps = run_gpu(case, precision, prim=prim)
+    if precision == lib.FP64_EXACT:
+        assert (steps, t) == (ref_steps, ref_t)
+        assert np.array_equal(U, ref)
+    else:
+        assert steps == ref_steps
+        err = rel_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+        assert (err <= 1e-10).all(), err
+
+
+def test_fp32_state_error_against_fp64_reference(cuda_device):
+    case = LARGE["kh128_50"]
+    prim = case["prim"]()
+    g = 2
+    rc, ref, _, _ = fvoracle.run(case["equation"], case["flux"], case["recon"], case["integrator"], case["boundary"],
+                                 case["n"], case["lower"], case["upper"], case["gamma"], case["cfl"],
+                                 case["end_time"], 0, 50, prim, g, 4)
+    U, _, steps = run_gpu(case, lib.FP32, prim=prim)
+    assert steps == 50
+    err = scaled_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+    assert (err <= 1e-4).all(), err
+
+
+def test_advance_host_equals_device_path(cuda_device):
+    case = LARGE["kh128_50"]
+    prim = case["prim"]()
+    U_dev, t_dev, _ = run_gpu(dict(case, max_steps=5), lib.FP64, prim=prim)
+    with solver(case["equation"], case["flux"], case["recon"], case["n"], lib.FP64, boundary="periodic",
+                upper=case["upper"], cfl=case["cfl"]) as s:
+        s.set_primitive(prim)
+        U = s.get_state()
+        for _ in range(5):
+            s.advance_host(U, case["end_time"], 0, 1)
+        t, steps, _ = s.time()
+    assert steps == 5 and t == t_dev
+    assert np.array_equal(U, U_dev)
+
+
+def test_constraint_violation_is_reported(cuda_device):
+    prim = workloads.sod_prim(64)
+    prim[2, 30] = -1.0
+    with solver("euler1", "hll3", "weno2", (64, 1, 1), lib.FP64, boundary="neumann", lower=(-5, 0, 0),
+                upper=(5, 1, 1)) as s:
+        s.set_primitive(prim)
+        with pytest.raises(lib.GbfvError) as e:
+            s.advance(1.0, 0, 10)
+        assert e.value.code == lib.ERR_CONSTRAINT
+        _, steps, _ = s.time()
+        assert steps == 1
+        assert not s.obeys_constraints(s.state_device())
+
+
+def test_obeys_constraints_matches_oracle(cuda_device):
+    n = (16, 12, 1)
+    t = workloads.padded_shape(n, 2)
+    U = workloads.smooth_random_state("euler2", t, np.random.default_rng(1))
+    with solver("euler2", "hll3", "weno2", n, lib.FP64) as s:
+        assert s.obeys_constraints(dev(U).data_ptr()) == fvoracle.obeys_constraints("euler2", n, 2, 1.4, U)
+        V = U.copy()
+        V[3, 5] = -100.0  # negative energy -> negative pressure in a ghost cell
+        assert s.obeys_constraints(dev(V).data_ptr()) == fvoracle.obeys_constraints("euler2", n, 2, 1.4, V)
+        assert not fvoracle.obeys_constraints("euler2", n, 2, 1.4, V)
+
+
+def test_statistics_match_reference_fixture(cuda_device):
+    z = np.load(os.path.join(GOLDEN, "meanvar.npz"))
+    S = z["samples"]
+    st = lib.Stats(S[0].size)
+    for s in S:
+        st.add_device(dev(s.ravel()).data_ptr())
+    m, v, n = st.result()
+    assert n == len(S)
+    assert np.allclose(m, z["mean"].ravel(), rtol=1e-14, atol=0)
+    assert np.allclose(v, z["var"].ravel(), rtol=1e-11, atol=1e-15)
+
+
+def test_statistics_merge_equals_single_pass(cuda_device):
+    rng = np.random.default_rng(3)
+    S = rng.normal(1.0, 0.3, (12, 1000))
+    a, b, c = lib.Stats(1000), lib.Stats(1000), lib.Stats(1000)
+    for i, s in enumerate(S):
+        c.add_host(s)
+        (a if i < 5 else b).add_host(s)
+    a.merge(b)
+    ma, va, na = a.result()
+    mc, vc, nc = c.result()
+    m_ref, v_ref = fvoracle.meanvar(list(S))
+    assert na == nc == 12
+    assert np.allclose(ma, mc, rtol=1e-14) and np.allclose(va, vc, rtol=1e-12)
+    assert np.allclose(mc, m_ref, rtol=1e-14) and np.allclose(vc, v_ref, rtol=1e-11)

@@ -1,0 +1,90 @@
+"""The CPU oracle against fixtures generated from the reference's own CPU
+implementation (tests/golden/make_golden.py): every comparison is bit-exact."""
+import os
+
+import numpy as np
+import pytest
+
+import workloads
+from oracle import fvoracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+FLUX_GRIDS = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
+
+
+def flux_keys():
+    z = load("flux.npz")
+    return sorted({k.rsplit("_", 1)[0] for k in z.files})
+
+
+@pytest.mark.parametrize("key", flux_keys())
+def test_flux_matches_reference(key):
+    z = load("flux.npz")
+    eq, fl, rc = key.split("_")
+    out, ws = fvoracle.compute_flux(eq, fl, rc, FLUX_GRIDS[eq], 1.4, z[key + "_U"])
+    assert np.isfinite(out).all()
+    assert np.array_equal(out, z[key + "_L"])
+    assert ws == list(z[key + "_ws"])
+
+
+def test_boundary_matches_reference():
+    z = load("boundary.npz")
+    for key in z.files:
+        bc, dims, g = key.split("_")
+        n = tuple(int(v) for v in dims.split("x"))
+        g = int(g[1:])
+        t = workloads.padded_shape(n, g)
+        tot = t[0] * t[1] * t[2]
+        U = np.arange(tot, dtype=np.float64).reshape(1, tot) + 0.25
+        assert np.array_equal(fvoracle.boundary(bc, n, g, U), z[key]), key
+
+
+def test_generator_matches_reference():
+    z = load("generator.npz")
+    for s in range(6):
+        assert np.array_equal(fvoracle.uniform(40, s), z["uniform40_s%d" % s])
+
+
+def test_meanvar_matches_reference():
+    z = load("meanvar.npz")
+    m, v = fvoracle.meanvar(list(z["samples"]))
+    assert np.array_equal(m, z["mean"])
+    assert np.array_equal(v, z["var"])
+
+
+@pytest.mark.parametrize("name", sorted(workloads.GOLDEN_RUNS))
+def test_run_matches_reference(name):
+    z = load("runs.npz")
+    case = workloads.GOLDEN_RUNS[name]
+    g = workloads.ghost_cells(case["recon"])
+    rc, U, t, steps = fvoracle.run(case["equation"], case["flux"], case["recon"], case["integrator"],
+                                   case["boundary"], case["n"], case["lower"], case["upper"], case["gamma"],
+                                   case["cfl"], case["end_time"], case["number_of_saves"], case["max_steps"],
+                                   z[name + "_prim"], g, workloads.NVAR[case["equation"]])
+    assert rc == 0
+    assert steps == int(z[name + "_steps"][0])
+    assert t == float(z[name + "_t"][0])
+    assert np.array_equal(U, z[name + "_U"])
+
+
+def test_fixture_initial_data_is_reproducible():
+    """The stored initial data equal the workload formulas evaluated here."""
+    z = load("runs.npz")
+    for name, case in workloads.GOLDEN_RUNS.items():
+        assert np.array_equal(case["prim"](), z[name + "_prim"]), name
+
+
+def test_constraint_violation_is_reported():
+    n = (16, 1, 1)
+    prim = workloads.sod_prim(16)
+    prim[2, 7] = -1.0  # negative pressure
+    rc, U, t, steps = fvoracle.run("euler1", "hll3", "weno2", "rungekutta3", "neumann", n, (-5, 0, 0), (5, 1, 1),
+                                   1.4, 0.475, 1.0, 0, 5, prim, 2, 3)
+    assert rc == -2
+    assert steps == 1

@@ -29,18 +29,21 @@ def padded_shape(n, g):
 
 
 def smooth_random_state(eq, t, rng):
-    """A positive, smooth-plus-noise conserved state on a padded grid of shape t."""
-    tot = t[0] * t[1] * t[2]
-    k = np.arange(tot)
+    """A positive conserved state on a padded grid of shape t: smooth waves in
+    every direction plus 1% noise, so high-order reconstructions stay physical."""
+    z, y, x = np.meshgrid(np.arange(t[2]), np.arange(t[1]), np.arange(t[0]), indexing="ij")
+    x, y, z = x.ravel(), y.ravel(), z.ravel()
+    tot = x.size
     nv = NVAR[eq]
     U = np.zeros((nv, tot))
+    wave = np.sin(0.41 * x + 0.2) + np.cos(0.33 * y + 0.5) + np.sin(0.29 * z + 1.1)
     if eq == "burgers":
-        U[0] = np.sin(k * 0.37) * 0.8 + rng.uniform(-0.1, 0.1, tot)
+        U[0] = 0.3 * wave + rng.uniform(-0.01, 0.01, tot)
         return U
     nsd = nv - 2
-    rho = 1 + 0.3 * np.sin(k * 0.37) + rng.uniform(0, 0.05, tot)
-    u = rng.uniform(-0.3, 0.3, (nsd, tot))
-    p = 1 + 0.3 * np.cos(k * 0.21) + rng.uniform(0, 0.05, tot)
+    rho = 1.5 + 0.15 * wave + rng.uniform(0, 0.01, tot)
+    u = 0.2 * np.sin(0.37 * x[None, :] + 0.7 * np.arange(nsd)[:, None]) + rng.uniform(-0.01, 0.01, (nsd, tot))
+    p = 1.5 + 0.15 * np.cos(0.23 * x + 0.31 * y + 0.17 * z) + rng.uniform(0, 0.01, tot)
     U[0] = rho
     U[1:1 + nsd] = rho * u
     U[-1] = p / 0.4 + 0.5 * rho * (u * u).sum(0)
