@@ -676,3 +676,82 @@ int gbfv_uniform(int dimension, int sample, double lower, double upper, double* 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Helpers for the allocation-free entry point (gbfv_noalloc.cu): the same
+// validation as gbfv_create and the same kernel sequence as one gbfv_advance
+// step, on buffers the caller provides.
+
+#include "gbfv_internal.h"
+
+int gbfv_internal_plan(const gbfv_desc* d, GbfvPlan* p) {
+    if (!d || !p) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    const int eq = parse_eq(d->equation), fl = parse_flux(d->flux), rc = parse_recon(d->reconstruction);
+    const int in = parse_integrator(d->integrator), bc = parse_bc(d->boundary);
+    if (eq < 0 || fl < 0 || rc < 0 || in < 0 || bc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown name in descriptor");
+    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV)) return fail(GBFV_ERR_UNSUPPORTED, "flux does not apply to this equation");
+    if (d->precision < 0 || d->precision >= NUM_VARIANTS) return fail(GBFV_ERR_ARGUMENT, "bad precision");
+    for (int k = 0; k < 3; ++k)
+        if (d->n[k] < 1) return fail(GBFV_ERR_ARGUMENT, "grid dimensions must be >= 1");
+    const int dim = d->n[2] > 1 ? 3 : (d->n[1] > 1 ? 2 : 1);
+    if (eq != EQ_BURGERS && eq != dim) return fail(GBFV_ERR_UNSUPPORTED, "euler<d> needs a d-dimensional grid");
+    const int g = kReconGhosts[rc];
+    for (int k = 0; k < dim; ++k)
+        if (d->n[k] < g) return fail(GBFV_ERR_UNSUPPORTED, "every active dimension needs at least as many cells as ghost cells");
+    p->eq = eq; p->fl = fl; p->rc = rc; p->in = in; p->periodic = bc; p->var = d->precision;
+    p->nvar = eq == EQ_BURGERS ? 1 : eq + 2;
+    p->elem = d->precision == VAR_F32 ? 4 : 8;
+    p->gamma = d->gamma;
+    p->cfl = d->cfl;
+    p->G.dim = dim;
+    long long total = 1;
+    for (int k = 0; k < 3; ++k) {
+        p->G.n[k] = d->n[k];
+        p->G.g[k] = k < dim ? g : 0;
+        p->G.t[k] = d->n[k] + 2 * p->G.g[k];
+        total *= p->G.t[k];
+    }
+    p->G.total = total;
+    for (int k = 0; k < 3; ++k) p->cell_lengths[k] = (d->upper[k] - d->lower[k]) / d->n[k];
+    if (d->n[1] == 1) p->cell_lengths[1] = 1;
+    if (d->n[2] == 1) p->cell_lengths[2] = 1;
+    return GBFV_OK;
+}
+
+int gbfv_internal_begin(StepState* st, double end_time, long long step_limit, cudaStream_t q) {
+    begin_kernel<<<1, 1, 0, q>>>(st, end_time, step_limit);
+    CUDA_TRY(cudaGetLastError());
+    return GBFV_OK;
+}
+
+int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* st, const StepParams& P,
+                       cudaStream_t q) {
+    Registry& R = registry();
+    const StageLauncher stage = R.stage[p.var][p.eq][p.fl][p.rc][p.G.dim - 1];
+    auto args = [&](const void* in, const void* u0, const void* l0, void* out, int mode, int check) {
+        StageArgs a;
+        a.in = in; a.u0 = u0; a.l0 = l0; a.out = out; a.st = st; a.G = p.G; a.gamma = p.gamma;
+        a.mode = mode; a.periodic = p.periodic; a.check = check;
+        return a;
+    };
+    LAUNCH_TRY(stage(args(U, U, nullptr, L, MODE_L, 0), q));
+    dt_kernel<<<1, 1, 0, q>>>(st, P);
+    CUDA_TRY(cudaGetLastError());
+    if (p.in == IN_RK3) {
+        LAUNCH_TRY(stage(args(U, U, L, V, MODE_RK3_S1, 0), q));
+        LAUNCH_TRY(stage(args(V, U, nullptr, U, MODE_RK3_S2, 1), q));
+    } else if (p.in == IN_RK2) {
+        LAUNCH_TRY(stage(args(U, U, L, V, MODE_RK2_S1, 1), q));
+        const long long n = (long long)p.nvar * p.G.total;
+        if (p.elem == 8)
+            copy_state_kernel<double><<<1184, 256, 0, q>>>(st, (const double*)V, (double*)U, n);
+        else
+            copy_state_kernel<float><<<1184, 256, 0, q>>>(st, (const float*)V, (float*)U, n);
+        CUDA_TRY(cudaGetLastError());
+    } else {
+        LAUNCH_TRY(R.apply[p.var][p.eq](args(U, U, L, U, MODE_L, 1), q));
+    }
+    finish_kernel<<<1, 1, 0, q>>>(st, P);
+    CUDA_TRY(cudaGetLastError());
+    return GBFV_OK;
+}

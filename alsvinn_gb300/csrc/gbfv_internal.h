@@ -1,0 +1,26 @@
+// Library-internal interface between the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fv_types.h"
+#include "gbfv.h"
+
+namespace gbfv {
+
+// A validated descriptor: parsed names, variant, grid geometry.
+struct GbfvPlan {
+    int eq, fl, rc, in, periodic, var, nvar, elem;
+    double gamma, cfl;
+    double cell_lengths[3];
+    Grid G;
+};
+
+}  // namespace gbfv
+
+int gbfv_internal_fail(int code, const char* msg);
+int gbfv_internal_plan(const gbfv_desc* d, gbfv::GbfvPlan* p);
+int gbfv_internal_begin(gbfv::StepState* st, double end_time, long long step_limit, cudaStream_t q);
+// Enqueues one time step on caller buffers: U state, V second state, L stage-0
+// flux difference (each nvar * total values), st step state.
+int gbfv_internal_step(const gbfv::GbfvPlan& p, void* U, void* V, void* L, gbfv::StepState* st,
+                       const gbfv::StepParams& P, cudaStream_t q);

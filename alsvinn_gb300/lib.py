@@ -81,7 +81,37 @@ _SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_void_p]),
+    "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
+                                            ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
 }
+
+NOALLOC_SCRATCH_BYTES = 32 << 20
+
+
+def make_desc(equation, flux, reconstruction, integrator, boundary, n, lower, upper, gamma=1.4, cfl=0.475,
+              precision=FP64):
+    """A gbfv_desc; the returned tuple keeps the name buffers alive."""
+    keep = [s.encode() for s in (equation, flux, reconstruction, integrator, boundary)]
+    d = _Desc()
+    d.equation, d.flux, d.reconstruction, d.integrator, d.boundary = keep
+    d.n = _c_int3(*n)
+    d.lower = _c_double3(*lower)
+    d.upper = _c_double3(*upper)
+    d.gamma = gamma
+    d.cfl = cfl
+    d.precision = precision
+    return d, keep
+
+
+def advance_noalloc(desc, state_dev, t, steps, end_time, number_of_saves=0, max_steps=0, stream=None):
+    """gbfv_advance_noalloc on a caller-owned device state; returns (t, steps)."""
+    tt = ctypes.c_double(t)
+    ss = ctypes.c_longlong(steps)
+    _check(load().gbfv_advance_noalloc(ctypes.byref(desc), ctypes.c_void_p(state_dev), ctypes.byref(tt),
+                                       ctypes.byref(ss), end_time, number_of_saves, max_steps,
+                                       ctypes.c_void_p(stream)))
+    return tt.value, ss.value
 
 
 def exported_names():

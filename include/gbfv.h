@@ -187,6 +187,35 @@ int gbfv_stats_result(gbfv_stats* st, double* mean_host, double* var_host, long 
  * alsuq/src/distribution/Uniform.cpp:27-34). */
 int gbfv_uniform(int dimension, int sample, double lower, double upper, double* out);
 
+/* ----------------------------------------------- allocation-free stepping */
+
+/* Size of the library's built-in scratch array for gbfv_advance_noalloc. */
+#define GBFV_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* gbfv_advance without any allocation, for callers that cannot call
+ * cudaMalloc (an application whose device memory belongs to a pool or arena
+ * it does not expose, a plug-in that may not allocate after start-up, a host
+ * that works inside a fixed memory budget). No counterpart in the reference:
+ * alsvinn always allocates its scratch volumes.
+ *
+ * The caller owns the padded device state (state_dev, nvar * total values of
+ * desc->precision, ghosts filled), the stream (NULL: the default stream), the
+ * time *t_inout and the step count *steps_inout, which the call advances like
+ * gbfv_advance (same kernels, same results). Scratch -- the stage-0 flux
+ * difference, the second state buffer and the step state -- comes from one
+ * static device array of GBFV_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit; grids needing more (2 * nvar * total * element
+ * size plus under 1 KiB of step state and alignment) are rejected with GBFV_ERR_UNSUPPORTED. The call makes no
+ * cudaMalloc, cudaFree or other allocating call.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the one array and it keeps the last call's contents;
+ *    calls that overlap on the GPU (other streams, other host threads) race.
+ *  - The save-time clamp restarts from *t_inout on every call. */
+int gbfv_advance_noalloc(const gbfv_desc* desc, void* state_dev, double* t_inout, long long* steps_inout,
+                         double end_time, int number_of_saves, int max_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
