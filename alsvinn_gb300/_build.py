@@ -49,6 +49,9 @@ def _units():
     units.append(("gbfv_api.cu", "gbfv_api.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_stats.cu", "gbfv_stats.o", []))
     units.append(("gbfv_noalloc.cu", "gbfv_noalloc.o", []))
+    units.append(("gbfv_batch.cu", "gbfv_batch.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
+    units.append(("gbfv_init.cpp", "gbfv_init.o", ["-Xcompiler", "-ffp-contract=off"]))
+    units.append(("gbfv_serve.cpp", "gbfv_serve.o", []))
     return units
 
 

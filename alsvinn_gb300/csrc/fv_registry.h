@@ -20,12 +20,16 @@ typedef int (*ReconLauncher)(const ReconArgs& a, cudaStream_t s);
 
 typedef int (*CheckLauncher)(const CheckArgs& a, cudaStream_t s);
 
+// Persistent ensemble stage launch: grid = ctas (0: one wave of resident CTAs).
+typedef int (*BatchLauncher)(const BatchArgs& a, int ctas, cudaStream_t s);
+
 struct Registry {
     // [variant][equation][flux][recon][dim-1]
     StageLauncher stage[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
     ApplyLauncher apply[NUM_VARIANTS][NUM_EQ];
     ReconLauncher recon[NUM_VARIANTS][NUM_EQ][NUM_RECON];
     CheckLauncher check[NUM_VARIANTS][NUM_EQ];
+    BatchLauncher batch[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
     size_t stage_smem[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
 };
 

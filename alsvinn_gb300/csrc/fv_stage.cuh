@@ -188,24 +188,24 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     __syncthreads();
 }
 
+// One tile of one stage: shared by the single-grid kernel (one CTA per tile)
+// and the persistent ensemble kernel (each CTA loops over a list of tiles of
+// many grids). Every thread of the CTA calls it; it synchronises internally.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
+__device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
+                                           double (*wred)[3]) {
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     constexpr int G = ReconTraits<RC>::ghosts;
     using SL = SmemLayout<R, NV, G, DIM, TX, TY, TZ>;
     constexpr int NT = TX * TY * TZ;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     R* su = reinterpret_cast<R*>(smem_raw);
     R* rl = su + NV * SL::HALO;
     R* rr = rl + NV * SL::REC;
     R* fc = rr + NV * SL::REC;
-    __shared__ double wred[NT / 32][3];
 
-    if (A.st->done) return;
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;
-    const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
     const R* in = reinterpret_cast<const R*>(A.in);
     const R* u0 = reinterpret_cast<const R*>(A.u0);
     const R* l0 = reinterpret_cast<const R*>(A.l0);
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
     // 4. this thread's cell: combine and write with its ghost images
     const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
     const int ix = org[0] + cx, iy = org[1] + cy, iz = org[2] + cz;
-    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) return;
+    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) return;  // no barrier follows
     const int sidx = ((cz + SL::GZ) * SL::HY + (cy + SL::GY)) * SL::HX + (cx + SL::GX);
     const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
     R res[NV];
@@ -312,6 +312,56 @@ __global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
 #pragma unroll
                 for (int k = 0; k < NV; ++k) out[k * total + gi] = res[k];
             }
+}
+
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double wred[(TX * TY * TZ) / 32][3];
+    if (A.st->done) return;
+    const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
+    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ>(A, org, smem_raw, wred);
+}
+
+// Persistent ensemble stage: each CTA walks the tile list (tiles of every
+// member grid, heterogeneous sizes) with stride gridDim.x. A member whose run
+// is done is skipped as a whole; the per-member wave-speed maxima land in
+// that member's step state (a segmented reduction), so every member gets its
+// own dt.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TX* TY* TZ) batch_stage_kernel(BatchArgs B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double wred[(TX * TY * TZ) / 32][3];
+    const int ntiles = *B.ntiles;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 tile = B.tiles[t];
+        StepState* st = B.states + tile.x;
+        if (st->done) continue;  // the same value for every thread of the CTA
+        const BatchMember& m = B.members[tile.x];
+        // ensemble RK2 alternates the two state buffers instead of copying
+        void* cur = st->parity ? m.v : m.u;
+        void* other = st->parity ? m.u : m.v;
+        StageArgs A;
+        A.G = m.G;
+        A.st = st;
+        A.gamma = B.gamma;
+        A.mode = B.mode;
+        A.periodic = B.periodic;
+        A.check = 0;
+        A.l0 = nullptr;
+        if (B.mode == MODE_L) {
+            A.in = cur; A.u0 = cur; A.out = m.l;
+        } else if (B.mode == MODE_RK3_S1) {
+            A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other;
+        } else if (B.mode == MODE_RK3_S2) {
+            A.in = other; A.u0 = cur; A.out = cur; A.check = 1;
+        } else {  // MODE_RK2_S1
+            A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
+        }
+        const int org[3] = {tile.y, tile.z, tile.w};
+        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ>(A, org, smem_raw, wred);
+        __syncthreads();
+    }
 }
 
 // Forward-Euler update U += L0 * c in place with ghost images

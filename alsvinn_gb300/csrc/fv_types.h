@@ -20,9 +20,11 @@ struct StepState {
     int status;                     // 0 ok, 1 constraint violated
     int failed_step;                // first step whose state broke the constraints
     int done;                       // 1: the advance has reached its end; kernels return at once
-    int pad_;
+    int parity;                     // ensemble RK2: which of the two state buffers holds the state
     double end_time;                // advance target time
     long long step_limit;           // advance step limit (< 0: none)
+    int just_done;                  // ensemble: reached end_time in the step just finished
+    int group;                      // ensemble: statistics group (< 0: none)
 };
 
 struct StepParams {
@@ -95,6 +97,27 @@ struct CheckArgs {
     int* flag;
     Grid G;
     double gamma;
+};
+
+// One member of an ensemble: its grid and its three state-sized buffers.
+struct BatchMember {
+    void* u;  // state (padded)
+    void* v;  // second state buffer
+    void* l;  // stage-0 flux difference
+    Grid G;
+};
+
+// Arguments of one ensemble stage launch. tiles[i] = (member, ox, oy, oz);
+// the tile count is read from device memory so a captured graph stays valid
+// when members join or leave.
+struct BatchArgs {
+    const BatchMember* members;
+    StepState* states;
+    const int4* tiles;
+    const int* ntiles;
+    double gamma;
+    int mode;
+    int periodic;
 };
 
 }  // namespace gbfv

@@ -52,6 +52,28 @@ struct StageEntry {
     }
 };
 
+template <int EQ, int FLUX, int RC, int DIM>
+struct BatchEntry {
+    using TS = TileShape<DIM>;
+    using SL = SmemLayout<Real, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    static int launch(const BatchArgs& a, int ctas, cudaStream_t s) {
+        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z>;
+        static int resident = 0;
+        if (!resident) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
+            if (e != cudaSuccess) return (int)e;
+            int per_sm = 0, dev = 0, sms = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TS::X * TS::Y * TS::Z, SL::bytes);
+            if (e == cudaSuccess) e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return (int)e;
+            resident = (per_sm > 0 ? per_sm : 1) * sms;
+        }
+        k<<<ctas > 0 ? ctas : resident, TS::X * TS::Y * TS::Z, SL::bytes, s>>>(a);
+        return (int)cudaGetLastError();
+    }
+};
+
 template <int EQ>
 static int launch_apply(const StageArgs& a, cudaStream_t s) {
     const long long ncell = (long long)a.G.n[0] * a.G.n[1] * a.G.n[2];
@@ -129,6 +151,11 @@ static void reg_dim(Registry& R) {
     R.stage[V][E][FLUX][RC_ENO2][DIM - 1] = &StageEntry<E, FLUX, RC_ENO2, DIM>::launch;
     R.stage[V][E][FLUX][RC_ENO3][DIM - 1] = &StageEntry<E, FLUX, RC_ENO3, DIM>::launch;
     R.stage[V][E][FLUX][RC_ENO4][DIM - 1] = &StageEntry<E, FLUX, RC_ENO4, DIM>::launch;
+    R.batch[V][E][FLUX][RC_NONE][DIM - 1] = &BatchEntry<E, FLUX, RC_NONE, DIM>::launch;
+    R.batch[V][E][FLUX][RC_WENO2][DIM - 1] = &BatchEntry<E, FLUX, RC_WENO2, DIM>::launch;
+    R.batch[V][E][FLUX][RC_ENO2][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO2, DIM>::launch;
+    R.batch[V][E][FLUX][RC_ENO3][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO3, DIM>::launch;
+    R.batch[V][E][FLUX][RC_ENO4][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO4, DIM>::launch;
     R.stage_smem[V][E][FLUX][RC_NONE][DIM - 1] = StageEntry<E, FLUX, RC_NONE, DIM>::SL::bytes;
     R.stage_smem[V][E][FLUX][RC_WENO2][DIM - 1] = StageEntry<E, FLUX, RC_WENO2, DIM>::SL::bytes;
     R.stage_smem[V][E][FLUX][RC_ENO2][DIM - 1] = StageEntry<E, FLUX, RC_ENO2, DIM>::SL::bytes;

@@ -755,3 +755,56 @@ int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* 
     CUDA_TRY(cudaGetLastError());
     return GBFV_OK;
 }
+
+// Host primitive -> conserved conversion into a padded array (interior cells;
+// ghosts left at zero), as gbfv_set_primitive does.
+int gbfv_internal_prim_to_cons(const GbfvPlan& p, const double* prim, double* cons) {
+    const Grid& G = p.G;
+    const long long total = G.total;
+    const long long cells = (long long)G.n[0] * G.n[1] * G.n[2];
+    const int nsd = p.eq == EQ_BURGERS ? 1 : p.eq;
+    for (int z = 0; z < G.n[2]; ++z)
+        for (int y = 0; y < G.n[1]; ++y)
+            for (int x = 0; x < G.n[0]; ++x) {
+                const long long ic = ((long long)z * G.n[1] + y) * G.n[0] + x;
+                const long long ip = ((long long)(z + G.g[2]) * G.t[1] + (y + G.g[1])) * G.t[0] + (x + G.g[0]);
+                if (p.eq == EQ_BURGERS) {
+                    cons[ip] = prim[ic];
+                    continue;
+                }
+                const double rho = prim[ic];
+                double u[3];
+                for (int k = 0; k < nsd; ++k) u[k] = prim[(1 + k) * cells + ic];
+                const double pr = prim[(1 + nsd) * cells + ic];
+                double dot = u[0] * u[0];
+                for (int k = 1; k < nsd; ++k) dot = dot + u[k] * u[k];
+                cons[ip] = rho;
+                for (int k = 0; k < nsd; ++k) cons[(1 + k) * total + ip] = u[k] * rho;
+                cons[(1 + nsd) * total + ip] = pr / (p.gamma - 1) + 0.5 * rho * dot;
+            }
+    return GBFV_OK;
+}
+
+// Uploads a padded double state into a device state of the plan's precision
+// and fills its ghost cells.
+int gbfv_internal_load_state(const GbfvPlan& p, const double* host, void* dev, cudaStream_t q) {
+    const size_t n = (size_t)p.nvar * p.G.total;
+    if (p.elem == 8) {
+        CUDA_TRY(cudaMemcpyAsync(dev, host, n * 8, cudaMemcpyHostToDevice, q));
+        CUDA_TRY(cudaStreamSynchronize(q));
+    } else {
+        std::vector<float> f(n);
+        for (size_t i = 0; i < n; ++i) f[i] = (float)host[i];
+        CUDA_TRY(cudaMemcpyAsync(dev, f.data(), n * 4, cudaMemcpyHostToDevice, q));
+        CUDA_TRY(cudaStreamSynchronize(q));
+    }
+    const int bs = 256;
+    const unsigned nb = (unsigned)((p.G.total + bs - 1) / bs);
+    if (p.elem == 8)
+        boundary_kernel<double><<<nb, bs, 0, q>>>((double*)dev, p.G, p.nvar, p.periodic);
+    else
+        boundary_kernel<float><<<nb, bs, 0, q>>>((float*)dev, p.G, p.nvar, p.periodic);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(q));
+    return GBFV_OK;
+}

@@ -1,0 +1,735 @@
+// Ensemble engine: many grids (members) of one scheme advanced together.
+//
+// alsuq runs its samples one after another, rebuilding a Simulator per sample
+// (alsuq/src/run/Runner.cpp:39-90). Here every member lives in one device pool
+// and each RK stage of the whole ensemble is one persistent launch over a tile
+// list that spans all members (batch_stage_kernel). Each member keeps its own
+// step state, so its dt comes from its own wave-speed maximum (a segmented
+// CFL reduction) and its own save-time clamp; members that reach end_time stop
+// while the rest continue. One time step of the ensemble is captured once as
+// a CUDA graph and replayed. Final states are folded into FP64 Welford mean /
+// variance accumulators per statistics group (MeanVariance with
+// FixedIntervalStatistics at the end time, alsuq/src/stats/MeanVariance.cpp:
+// 30-67, FixedIntervalStatistics.cpp:33-86), in member order, so the result
+// does not depend on which members finish in the same step.
+//
+// Members join and leave between advance calls (the serving loop's slots);
+// memory for them comes from one pool allocated at creation, so admission is
+// bounded by that pool (the HBM budget).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fv_registry.h"
+#include "gbfv_internal.h"
+
+using namespace gbfv;
+
+namespace {
+
+struct MemberParam {
+    double cell_lengths[3];
+    double time_interval;  // save-time clamp interval (0: none)
+    int dim;
+    int active;
+};
+
+struct GroupAcc {
+    double* mean;
+    double* m2;
+    long long cells;  // nvar * padded total of the group's grid
+    long long count;  // members folded in
+};
+
+// per-member dt (Integrator::computeTimestep + the save-time clamp)
+__global__ void batch_dt_kernel(StepState* st, const MemberParam* mp, int M, double cfl) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= M || !mp[s].active || st[s].done) return;
+    StepState& S = st[s];
+    const MemberParam& P = mp[s];
+    double ws[3];
+    for (int d = 0; d < 3; ++d) ws[d] = d < P.dim ? __longlong_as_double((long long)S.ws_bits[d]) : 0.0;
+    double waveSpeedTotal = 0;
+    for (int d = 0; d < 3; ++d) {
+        if (P.cell_lengths[d] == 0) continue;
+        waveSpeedTotal += ws[d] / P.cell_lengths[d];
+    }
+    double dt = cfl / waveSpeedTotal;
+    if (P.time_interval > 0) {
+        const double nextSaveTime = (double)S.number_saved * P.time_interval + 0.0;
+        const double lim = nextSaveTime - S.t;
+        dt = lim < dt ? lim : dt;
+    }
+    S.dt = dt;
+    S.scale = dt / P.cell_lengths[0];
+}
+
+__global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M, int alternate) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= M || !mp[s].active || st[s].done) return;
+    StepState& S = st[s];
+    const MemberParam& P = mp[s];
+    S.t = S.t + S.dt;
+    S.steps += 1;
+    if (P.time_interval > 0 && S.t >= (double)S.number_saved * P.time_interval + 0.0) S.number_saved += 1;
+    S.ws_bits[0] = S.ws_bits[1] = S.ws_bits[2] = 0ull;
+    if (alternate) S.parity ^= 1;
+    const bool reached = !(S.t < S.end_time);
+    if (reached || (S.step_limit >= 0 && S.steps >= S.step_limit) || S.status != 0) {
+        S.done = 1;
+        S.just_done = (reached && S.status == 0) ? 1 : 0;
+    }
+}
+
+__global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, double end_time, long long max_steps) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= M) return;
+    StepState& S = st[s];
+    if (!mp[s].active) {
+        S.done = 1;
+        return;
+    }
+    S.end_time = end_time;
+    S.step_limit = max_steps > 0 ? S.steps + max_steps : -1;
+    S.ws_bits[0] = S.ws_bits[1] = S.ws_bits[2] = 0ull;
+    S.just_done = 0;
+    S.done = (!(S.t < end_time) || S.status != 0) ? 1 : 0;
+}
+
+// Welford order: members that reached end_time in this step, in member order.
+__global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* groups, int ngroups, int2* list, int* nlist) {
+    int m = 0;
+    for (int s = 0; s < M; ++s) {
+        if (!st[s].just_done) continue;
+        st[s].just_done = 0;
+        const int g = st[s].group;
+        if (g < 0 || g >= ngroups) continue;
+        groups[g].count += 1;
+        list[m++] = make_int2(s, (int)groups[g].count);
+    }
+    *nlist = m;
+}
+
+template <class R>
+__global__ void batch_stats_kernel(const BatchMember* members, const StepState* st, const GroupAcc* groups,
+                                   int ngroups, long long total_cells, const int2* list, const int* nlist) {
+    const int m = *nlist;
+    if (m == 0) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total_cells;
+         i += (long long)gridDim.x * blockDim.x) {
+        int g = 0;
+        long long c = i;
+        while (g < ngroups && c >= groups[g].cells) {
+            c -= groups[g].cells;
+            ++g;
+        }
+        if (g >= ngroups) return;
+        double mean = groups[g].mean[c], m2 = groups[g].m2[c];
+        bool touched = false;
+        for (int k = 0; k < m; ++k) {
+            const int s = list[k].x;
+            if (st[s].group != g) continue;
+            const R* u = reinterpret_cast<const R*>(st[s].parity ? members[s].v : members[s].u);
+            const double x = (double)u[c];
+            const double n = (double)list[k].y;
+            const double delta = x - mean;
+            mean = mean + delta / n;
+            m2 = m2 + delta * (x - mean);
+            touched = true;
+        }
+        if (touched) {
+            groups[g].mean[c] = mean;
+            groups[g].m2[c] = m2;
+        }
+    }
+}
+
+__global__ void batch_count_kernel(const StepState* st, const MemberParam* mp, int M, int* running) {
+    __shared__ int c;
+    if (threadIdx.x == 0) c = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < M; s += blockDim.x)
+        if (mp[s].active && !st[s].done) atomicAdd(&c, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) *running = c;
+}
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct gbfv_batch {
+    GbfvPlan scheme;  // names, variant, dim of the members (grid fields unused)
+    gbfv_desc desc;
+    std::string names[5];
+    int max_members = 0;
+    int dim = 0;
+    // pool
+    char* pool = nullptr;
+    size_t capacity = 0;
+    std::map<size_t, size_t> free_blocks;  // offset -> size
+    // members
+    struct Host {
+        bool active = false;
+        size_t off = 0, bytes = 0;
+        BatchMember m;
+        MemberParam p;
+        int group = -1;
+    };
+    std::vector<Host> members;
+    BatchMember* d_members = nullptr;
+    MemberParam* d_params = nullptr;
+    StepState* d_states = nullptr;
+    StepState* h_states = nullptr;  // pinned
+    // tiles
+    int4* d_tiles = nullptr;
+    int* d_ntiles = nullptr;
+    size_t tile_cap = 0;
+    bool tiles_dirty = true;
+    // statistics
+    std::vector<GroupAcc> groups;
+    std::vector<int> group_dims;  // nvar*total per group
+    GroupAcc* d_groups = nullptr;
+    int2* d_list = nullptr;
+    int* d_nlist = nullptr;
+    long long stats_cells = 0;
+    // running count
+    int* d_running = nullptr;
+    int* h_running = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t step_graph = nullptr;
+    int graph_chunk = 0;
+    long long launches = 0;
+};
+
+namespace {
+
+int bfail(int code, const std::string& m) { return gbfv_internal_fail(code, m.c_str()); }
+
+#define BCUDA(x)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (x);                                                             \
+        if (e_ != cudaSuccess) return bfail(GBFV_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int tile_shape(int dim, int k) {
+    static const int shapes[3][3] = {{128, 1, 1}, {32, 8, 1}, {8, 8, 4}};
+    return shapes[dim - 1][k];
+}
+
+int rebuild_tiles(gbfv_batch* b) {
+    std::vector<int4> tiles;
+    const int tx = tile_shape(b->dim, 0), ty = tile_shape(b->dim, 1), tz = tile_shape(b->dim, 2);
+    for (size_t s = 0; s < b->members.size(); ++s) {
+        const auto& h = b->members[s];
+        if (!h.active) continue;
+        if (b->h_states[s].done && b->h_states[s].t >= b->h_states[s].end_time) continue;
+        for (int z = 0; z < h.m.G.n[2]; z += tz)
+            for (int y = 0; y < h.m.G.n[1]; y += ty)
+                for (int x = 0; x < h.m.G.n[0]; x += tx) tiles.push_back(make_int4((int)s, x, y, z));
+    }
+    if (tiles.size() > b->tile_cap) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        const size_t cap = std::max<size_t>(tiles.size() * 3 / 2, 1024);
+        BCUDA(cudaMalloc(&b->d_tiles, cap * sizeof(int4)));
+        b->tile_cap = cap;
+        if (b->step_graph) {
+            cudaGraphExecDestroy(b->step_graph);
+            b->step_graph = nullptr;
+        }
+    }
+    const int n = (int)tiles.size();
+    if (n) BCUDA(cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaMemcpyAsync(b->d_ntiles, &n, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    b->tiles_dirty = false;
+    return GBFV_OK;
+}
+
+int upload_members(gbfv_batch* b) {
+    const int M = b->max_members;
+    std::vector<BatchMember> m(M);
+    std::vector<MemberParam> p(M);
+    for (int s = 0; s < M; ++s) {
+        m[s] = b->members[s].m;
+        p[s] = b->members[s].p;
+    }
+    BCUDA(cudaMemcpyAsync(b->d_members, m.data(), M * sizeof(BatchMember), cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaMemcpyAsync(b->d_params, p.data(), M * sizeof(MemberParam), cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    return GBFV_OK;
+}
+
+// One ensemble time step (the body of the captured graph).
+int enqueue_batch_step(gbfv_batch* b) {
+    Registry& R = registry();
+    const GbfvPlan& p = b->scheme;
+    const BatchLauncher launch = R.batch[p.var][p.eq][p.fl][p.rc][b->dim - 1];
+    BatchArgs a;
+    a.members = b->d_members;
+    a.states = b->d_states;
+    a.tiles = b->d_tiles;
+    a.ntiles = b->d_ntiles;
+    a.gamma = p.gamma;
+    a.periodic = p.periodic;
+    const int M = b->max_members;
+    const unsigned mb = (unsigned)((M + 127) / 128);
+    cudaStream_t q = b->stream;
+    a.mode = MODE_L;
+    int r = launch(a, 0, q);
+    if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
+    batch_dt_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.cfl);
+    if (p.in == 2) {
+        a.mode = MODE_RK3_S1;
+        r = launch(a, 0, q);
+        if (!r) {
+            a.mode = MODE_RK3_S2;
+            r = launch(a, 0, q);
+        }
+    } else {
+        a.mode = MODE_RK2_S1;
+        r = launch(a, 0, q);
+    }
+    if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
+    batch_finish_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.in == 1 ? 1 : 0);
+    if (!b->groups.empty()) {
+        batch_assign_kernel<<<1, 1, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->d_list,
+                                            b->d_nlist);
+        const long long cells = b->stats_cells;
+        unsigned nb = (unsigned)std::min<long long>((cells + 255) / 256, 152 * 8);
+        if (b->scheme.elem == 8)
+            batch_stats_kernel<double><<<nb, 256, 0, q>>>(b->d_members, b->d_states, b->d_groups,
+                                                          (int)b->groups.size(), cells, b->d_list, b->d_nlist);
+        else
+            batch_stats_kernel<float><<<nb, 256, 0, q>>>(b->d_members, b->d_states, b->d_groups,
+                                                         (int)b->groups.size(), cells, b->d_list, b->d_nlist);
+    }
+    BCUDA(cudaGetLastError());
+    b->launches += (p.in == 2 ? 3 : 2) + 2 + (b->groups.empty() ? 0 : 2);
+    return GBFV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbfv_batch_create(const gbfv_desc* scheme, long long pool_bytes, int max_members, gbfv_batch** out) {
+    if (!scheme || !out || pool_bytes <= 0 || max_members <= 0)
+        return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_create: bad arguments");
+    *out = nullptr;
+    gbfv_batch* b = new gbfv_batch();
+    b->desc = *scheme;
+    const char* src[5] = {scheme->equation, scheme->flux, scheme->reconstruction, scheme->integrator, scheme->boundary};
+    for (int k = 0; k < 5; ++k) b->names[k] = src[k] ? src[k] : "";
+    b->desc.equation = b->names[0].c_str();
+    b->desc.flux = b->names[1].c_str();
+    b->desc.reconstruction = b->names[2].c_str();
+    b->desc.integrator = b->names[3].c_str();
+    b->desc.boundary = b->names[4].c_str();
+    int r = gbfv_internal_plan(&b->desc, &b->scheme);
+    if (r) {
+        delete b;
+        return r;
+    }
+    if (b->scheme.in == 0) {
+        delete b;
+        return bfail(GBFV_ERR_UNSUPPORTED, "gbfv_batch_create: the ensemble engine runs rungekutta2 and rungekutta3");
+    }
+    b->dim = b->scheme.G.dim;
+    b->max_members = max_members;
+    b->members.resize(max_members);
+    for (auto& h : b->members) {
+        std::memset(&h.m, 0, sizeof h.m);
+        std::memset(&h.p, 0, sizeof h.p);
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->pool, (size_t)pool_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_members, max_members * sizeof(BatchMember));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_params, max_members * sizeof(MemberParam));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_states, max_members * sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_states, max_members * sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_list, max_members * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_nlist, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_running, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_running, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_nlist, 0, sizeof(int), b->stream);
+    if (e == cudaSuccess) {
+        std::memset(b->h_states, 0, max_members * sizeof(StepState));
+        for (int s = 0; s < max_members; ++s) {
+            b->h_states[s].done = 1;
+            b->h_states[s].group = -1;
+            b->h_states[s].number_saved = 1;
+        }
+        e = cudaMemcpyAsync(b->d_states, b->h_states, max_members * sizeof(StepState), cudaMemcpyHostToDevice, b->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? GBFV_ERR_MEMORY : GBFV_ERR_CUDA;
+        gbfv_batch_destroy(b);
+        return bfail(code, std::string("gbfv_batch_create: ") + cudaGetErrorString(e));
+    }
+    b->capacity = (size_t)pool_bytes;
+    b->free_blocks[0] = b->capacity;
+    int rr = upload_members(b);
+    if (rr) {
+        gbfv_batch_destroy(b);
+        return rr;
+    }
+    *out = b;
+    return GBFV_OK;
+}
+
+int gbfv_batch_destroy(gbfv_batch* b) {
+    if (!b) return GBFV_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->step_graph) cudaGraphExecDestroy(b->step_graph);
+    for (auto& g : b->groups) {
+        cudaFree(g.mean);
+        cudaFree(g.m2);
+    }
+    cudaFree(b->d_groups);
+    cudaFree(b->pool);
+    cudaFree(b->d_members);
+    cudaFree(b->d_params);
+    cudaFree(b->d_states);
+    cudaFree(b->d_tiles);
+    cudaFree(b->d_ntiles);
+    cudaFree(b->d_list);
+    cudaFree(b->d_nlist);
+    cudaFree(b->d_running);
+    if (b->h_states) cudaFreeHost(b->h_states);
+    if (b->h_running) cudaFreeHost(b->h_running);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GBFV_OK;
+}
+
+// Bytes a member of this grid occupies in the pool (three padded state arrays).
+long long gbfv_batch_member_bytes(const gbfv_batch* b, const int n[3]) {
+    if (!b || !n) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    gbfv_desc d = b->desc;
+    for (int k = 0; k < 3; ++k) d.n[k] = n[k];
+    GbfvPlan p;
+    int r = gbfv_internal_plan(&d, &p);
+    if (r) return r;
+    return (long long)(3 * round256((size_t)p.nvar * p.G.total * p.elem));
+}
+
+int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const double upper[3],
+                   const double* prim_host, int group, int* slot_out) {
+    if (!b || !n || !lower || !upper || !prim_host || !slot_out) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    gbfv_desc d = b->desc;
+    for (int k = 0; k < 3; ++k) {
+        d.n[k] = n[k];
+        d.lower[k] = lower[k];
+        d.upper[k] = upper[k];
+    }
+    GbfvPlan p;
+    int r = gbfv_internal_plan(&d, &p);
+    if (r) return r;
+    if (p.G.dim != b->dim) return bfail(GBFV_ERR_UNSUPPORTED, "all members of an ensemble share one dimension");
+    int slot = -1;
+    for (int s = 0; s < b->max_members; ++s)
+        if (!b->members[s].active) {
+            slot = s;
+            break;
+        }
+    if (slot < 0) return bfail(GBFV_ERR_MEMORY, "gbfv_batch_add: every member slot is in use");
+    const size_t arr = round256((size_t)p.nvar * p.G.total * p.elem);
+    const size_t need = 3 * arr;
+    size_t off = (size_t)-1;
+    for (auto it = b->free_blocks.begin(); it != b->free_blocks.end(); ++it)
+        if (it->second >= need) {
+            off = it->first;
+            const size_t rest = it->second - need;
+            b->free_blocks.erase(it);
+            if (rest) b->free_blocks[off + need] = rest;
+            break;
+        }
+    if (off == (size_t)-1) return bfail(GBFV_ERR_MEMORY, "gbfv_batch_add: the ensemble pool has no room for this member");
+    if (group >= 0) {
+        while ((int)b->groups.size() <= group) {
+            GroupAcc g;
+            std::memset(&g, 0, sizeof g);
+            b->groups.push_back(g);
+            b->group_dims.push_back(0);
+        }
+        GroupAcc& g = b->groups[group];
+        const long long cells = (long long)p.nvar * p.G.total;
+        if (g.mean && g.cells != cells) {
+            b->free_blocks[off] = need;
+            return bfail(GBFV_ERR_ARGUMENT, "members of one statistics group must share their grid");
+        }
+        if (!g.mean) {
+            BCUDA(cudaMalloc(&g.mean, cells * sizeof(double)));
+            BCUDA(cudaMalloc(&g.m2, cells * sizeof(double)));
+            BCUDA(cudaMemsetAsync(g.mean, 0, cells * sizeof(double), b->stream));
+            BCUDA(cudaMemsetAsync(g.m2, 0, cells * sizeof(double), b->stream));
+            g.cells = cells;
+            g.count = 0;
+            if (b->d_groups) cudaFree(b->d_groups);
+            b->d_groups = nullptr;
+            BCUDA(cudaMalloc(&b->d_groups, b->groups.size() * sizeof(GroupAcc)));
+            b->stats_cells = 0;
+            for (auto& x : b->groups) b->stats_cells += x.cells;
+            if (b->step_graph) {
+                cudaGraphExecDestroy(b->step_graph);
+                b->step_graph = nullptr;
+            }
+        }
+        BCUDA(cudaMemcpyAsync(b->d_groups, b->groups.data(), b->groups.size() * sizeof(GroupAcc),
+                              cudaMemcpyHostToDevice, b->stream));
+    }
+    auto& h = b->members[slot];
+    h.active = true;
+    h.off = off;
+    h.bytes = need;
+    h.group = group;
+    h.m.u = b->pool + off;
+    h.m.v = b->pool + off + arr;
+    h.m.l = b->pool + off + 2 * arr;
+    h.m.G = p.G;
+    for (int k = 0; k < 3; ++k) h.p.cell_lengths[k] = p.cell_lengths[k];
+    h.p.time_interval = 0;
+    h.p.dim = p.G.dim;
+    h.p.active = 1;
+
+    // initial data: primitive -> conserved on the host (gbfv_set_primitive's
+    // conversion), upload, ghost fill on the device
+    {
+        std::vector<double> cons((size_t)p.nvar * p.G.total, 0.0);
+        gbfv_internal_prim_to_cons(p, prim_host, cons.data());
+        r = gbfv_internal_load_state(p, cons.data(), h.m.u, b->stream);
+        if (r) {
+            h.active = false;
+            b->free_blocks[off] = need;
+            return r;
+        }
+    }
+    StepState z;
+    std::memset(&z, 0, sizeof z);
+    z.number_saved = 1;
+    z.done = 1;
+    z.group = group;
+    b->h_states[slot] = z;
+    BCUDA(cudaMemcpyAsync(b->d_states + slot, &b->h_states[slot], sizeof(StepState), cudaMemcpyHostToDevice, b->stream));
+    r = upload_members(b);
+    if (r) return r;
+    b->tiles_dirty = true;
+    *slot_out = slot;
+    return GBFV_OK;
+}
+
+int gbfv_batch_remove(gbfv_batch* b, int slot) {
+    if (!b || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_remove: bad slot");
+    BCUDA(cudaStreamSynchronize(b->stream));
+    auto& h = b->members[slot];
+    // return the block and merge neighbours
+    size_t off = h.off, size = h.bytes;
+    auto next = b->free_blocks.lower_bound(off);
+    if (next != b->free_blocks.end() && next->first == off + size) {
+        size += next->second;
+        b->free_blocks.erase(next);
+    }
+    auto prev = b->free_blocks.lower_bound(off);
+    if (prev != b->free_blocks.begin()) {
+        --prev;
+        if (prev->first + prev->second == off) {
+            off = prev->first;
+            size += prev->second;
+            b->free_blocks.erase(prev);
+        }
+    }
+    b->free_blocks[off] = size;
+    h.active = false;
+    std::memset(&h.m, 0, sizeof h.m);
+    std::memset(&h.p, 0, sizeof h.p);
+    int r = upload_members(b);
+    if (r) return r;
+    b->tiles_dirty = true;
+    return GBFV_OK;
+}
+
+int gbfv_batch_free_bytes(const gbfv_batch* b, long long* free_total, long long* largest) {
+    if (!b) return bfail(GBFV_ERR_ARGUMENT, "null batch");
+    long long t = 0, l = 0;
+    for (auto& kv : b->free_blocks) {
+        t += (long long)kv.second;
+        l = std::max(l, (long long)kv.second);
+    }
+    if (free_total) *free_total = t;
+    if (largest) *largest = l;
+    return GBFV_OK;
+}
+
+int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int max_steps) {
+    if (!b) return bfail(GBFV_ERR_ARGUMENT, "null batch");
+    const int M = b->max_members;
+    // save-time clamp per member (FixedIntervalStatistics / FixedIntervalWriter)
+    for (int s = 0; s < M; ++s)
+        if (b->members[s].active) b->members[s].p.time_interval = number_of_saves > 0 ? end_time / number_of_saves : 0;
+    int r = upload_members(b);
+    if (r) return r;
+    const unsigned mb = (unsigned)((M + 127) / 128);
+    batch_begin_kernel<<<mb, 128, 0, b->stream>>>(b->d_states, b->d_params, M, end_time, max_steps);
+    BCUDA(cudaGetLastError());
+    BCUDA(cudaMemcpyAsync(b->h_states, b->d_states, M * sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    b->tiles_dirty = true;
+    r = rebuild_tiles(b);
+    if (r) return r;
+    // first step launched directly (initialises the launchers), the rest from a graph
+    r = enqueue_batch_step(b);
+    if (r) return r;
+    if (!b->step_graph) {
+        cudaGraph_t g = nullptr;
+        BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = b->launches;
+        r = enqueue_batch_step(b);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        b->launches = before;
+        if (r) return r;
+        if (ce != cudaSuccess) return bfail(GBFV_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&b->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return bfail(GBFV_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    }
+    const long long per_step = (b->scheme.in == 2 ? 3 : 2) + 2 + (b->groups.empty() ? 0 : 2);
+    int chunk = 4;
+    int last_running = -1;
+    for (;;) {
+        batch_count_kernel<<<1, 256, 0, b->stream>>>(b->d_states, b->d_params, M, b->d_running);
+        BCUDA(cudaMemcpyAsync(b->h_running, b->d_running, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        BCUDA(cudaStreamSynchronize(b->stream));
+        const int running = *b->h_running;
+        if (running == 0) break;
+        if (last_running >= 0 && running < last_running) {
+            // members finished: drop their tiles from the work list
+            BCUDA(cudaMemcpyAsync(b->h_states, b->d_states, M * sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+            BCUDA(cudaStreamSynchronize(b->stream));
+            r = rebuild_tiles(b);
+            if (r) return r;
+        }
+        last_running = running;
+        for (int i = 0; i < chunk; ++i) {
+            BCUDA(cudaGraphLaunch(b->step_graph, b->stream));
+            b->launches += per_step;
+        }
+        if (chunk < 64) chunk *= 2;
+    }
+    BCUDA(cudaMemcpyAsync(b->h_states, b->d_states, M * sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaMemcpyAsync(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost,
+                          b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    for (int s = 0; s < M; ++s)
+        if (b->members[s].active && b->h_states[s].status != 0) {
+            char msg[256];
+            snprintf(msg, sizeof msg, "member %d does not obey constraints at time %.17g (step %d)", s,
+                     b->h_states[s].t, b->h_states[s].failed_step);
+            return bfail(GBFV_ERR_CONSTRAINT, msg);
+        }
+    return GBFV_OK;
+}
+
+int gbfv_batch_member_time(gbfv_batch* b, int slot, double* t, long long* steps) {
+    if (!b || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "bad slot");
+    BCUDA(cudaMemcpyAsync(&b->h_states[slot], b->d_states + slot, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    if (t) *t = b->h_states[slot].t;
+    if (steps) *steps = b->h_states[slot].steps;
+    return GBFV_OK;
+}
+
+int gbfv_batch_member_state(gbfv_batch* b, int slot, double* host) {
+    if (!b || !host || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "bad slot");
+    BCUDA(cudaMemcpyAsync(&b->h_states[slot], b->d_states + slot, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    const auto& h = b->members[slot];
+    const void* src = b->h_states[slot].parity ? h.m.v : h.m.u;
+    const size_t n = (size_t)b->scheme.nvar * h.m.G.total;
+    if (b->scheme.elem == 8) {
+        BCUDA(cudaMemcpy(host, src, n * 8, cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> f(n);
+        BCUDA(cudaMemcpy(f.data(), src, n * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; ++i) host[i] = (double)f[i];
+    }
+    return GBFV_OK;
+}
+
+int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double* var_host, long long* count) {
+    if (!b || group < 0 || group >= (int)b->groups.size() || !b->groups[group].mean)
+        return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group");
+    BCUDA(cudaStreamSynchronize(b->stream));
+    BCUDA(cudaMemcpy(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost));
+    const GroupAcc& g = b->groups[group];
+    if (count) *count = g.count;
+    if (g.count == 0) return bfail(GBFV_ERR_ARGUMENT, "no member of this group has reached the end time");
+    std::vector<double> m2(g.cells);
+    if (mean_host) BCUDA(cudaMemcpy(mean_host, g.mean, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
+    if (var_host) {
+        BCUDA(cudaMemcpy(m2.data(), g.m2, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < g.cells; ++i) var_host[i] = m2[i] / (double)g.count;
+    }
+    return GBFV_OK;
+}
+
+int gbfv_batch_stats_reset(gbfv_batch* b) {
+    if (!b) return bfail(GBFV_ERR_ARGUMENT, "null batch");
+    BCUDA(cudaStreamSynchronize(b->stream));
+    for (auto& g : b->groups) {
+        if (!g.mean) continue;
+        BCUDA(cudaMemset(g.mean, 0, g.cells * sizeof(double)));
+        BCUDA(cudaMemset(g.m2, 0, g.cells * sizeof(double)));
+        g.count = 0;
+    }
+    if (b->d_groups)
+        BCUDA(cudaMemcpy(b->d_groups, b->groups.data(), b->groups.size() * sizeof(GroupAcc), cudaMemcpyHostToDevice));
+    return GBFV_OK;
+}
+
+int gbfv_batch_finished(gbfv_batch* b, int* slots, int capacity, int* count) {
+    if (!b || !count || (capacity > 0 && !slots)) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    int c = 0;
+    for (int s = 0; s < b->max_members; ++s) {
+        if (!b->members[s].active) continue;
+        const StepState& S = b->h_states[s];
+        if (S.done && S.status == 0 && !(S.t < S.end_time)) {
+            if (c < capacity) slots[c] = s;
+            ++c;
+        }
+    }
+    *count = c;
+    return GBFV_OK;
+}
+
+int gbfv_batch_active(const gbfv_batch* b, int* count) {
+    if (!b || !count) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    int c = 0;
+    for (int s = 0; s < b->max_members; ++s) c += b->members[s].active ? 1 : 0;
+    *count = c;
+    return GBFV_OK;
+}
+
+int gbfv_batch_launches(gbfv_batch* b, long long* launches) {
+    if (!b || !launches) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    *launches = b->launches;
+    return GBFV_OK;
+}
+
+int gbfv_batch_stream(gbfv_batch* b, void** stream) {
+    if (!b || !stream) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    *stream = (void*)b->stream;
+    return GBFV_OK;
+}
+
+}  // extern "C"

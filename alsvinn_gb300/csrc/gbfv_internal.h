@@ -22,5 +22,7 @@ int gbfv_internal_plan(const gbfv_desc* d, gbfv::GbfvPlan* p);
 int gbfv_internal_begin(gbfv::StepState* st, double end_time, long long step_limit, cudaStream_t q);
 // Enqueues one time step on caller buffers: U state, V second state, L stage-0
 // flux difference (each nvar * total values), st step state.
+int gbfv_internal_prim_to_cons(const gbfv::GbfvPlan& p, const double* prim, double* cons);
+int gbfv_internal_load_state(const gbfv::GbfvPlan& p, const double* host, void* dev, cudaStream_t q);
 int gbfv_internal_step(const gbfv::GbfvPlan& p, void* U, void* V, void* L, gbfv::StepState* st,
                        const gbfv::StepParams& P, cudaStream_t q);

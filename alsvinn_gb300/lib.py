@@ -84,6 +84,34 @@ _SIGNATURES = {
     "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                             ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_batch_create": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_longlong, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_batch_member_bytes": (ctypes.c_longlong, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_batch_free_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                             ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_batch_remove": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_batch_advance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
+    "gbfv_batch_member_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_member_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_batch_stats_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_stats_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_batch_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_init_sod": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "gbfv_init_kelvin_helmholtz": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
+    "gbfv_init_taylor_green": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "gbfv_init_burgers_sine": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_void_p]),
 }
 
 NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -157,6 +185,34 @@ def uniform(dimension, sample, lower=0.0, upper=1.0):
     out = np.zeros(dimension)
     _check(load().gbfv_uniform(dimension, sample, lower, upper, _ptr(out)))
     return out
+
+
+def init_sod(n, lower=(-5.0, 0.0, 0.0), upper=(5.0, 1.0, 1.0)):
+    prim = np.zeros((3, n))
+    _check(load().gbfv_init_sod(_c_int3(n, 1, 1), _c_double3(*lower), _c_double3(*upper), _ptr(prim)))
+    return prim
+
+
+def init_kelvin_helmholtz(n, sample=0, X=None, lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 0.0)):
+    """KH initial data; X defaults to the generator's 40 draws of `sample`."""
+    X = uniform(40, sample) if X is None else np.ascontiguousarray(X, dtype=np.float64)
+    prim = np.zeros((4, n * n))
+    _check(load().gbfv_init_kelvin_helmholtz(_c_int3(n, n, 1), _c_double3(*lower), _c_double3(*upper), _ptr(X),
+                                             _ptr(prim)))
+    return prim
+
+
+def init_taylor_green(n, lower=(0.0, 0.0, 0.0), upper=(2 * np.pi, 2 * np.pi, 2 * np.pi)):
+    prim = np.zeros((5, n ** 3))
+    _check(load().gbfv_init_taylor_green(_c_int3(n, n, n), _c_double3(*lower), _c_double3(*upper), _ptr(prim)))
+    return prim
+
+
+def init_burgers_sine(n, phase, lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0)):
+    prim = np.zeros((1, n))
+    _check(load().gbfv_init_burgers_sine(_c_int3(n, 1, 1), _c_double3(*lower), _c_double3(*upper), phase,
+                                         _ptr(prim)))
+    return prim
 
 
 class Solver:
@@ -311,3 +367,177 @@ class Stats:
         n = ctypes.c_longlong()
         _check(load().gbfv_stats_result(self.h, _ptr(m), _ptr(v), ctypes.byref(n)))
         return m, v, n.value
+
+
+class Batch:
+    """An ensemble of grids advanced together (gbfv_batch_*)."""
+
+    def __init__(self, equation, flux, reconstruction, integrator, boundary, pool_bytes, max_members,
+                 gamma=1.4, cfl=0.475, precision=FP64, dim=2):
+        n = (8, 8 if dim > 1 else 1, 8 if dim > 2 else 1)
+        self._desc, self._keep = make_desc(equation, flux, reconstruction, integrator, boundary, n, (0, 0, 0),
+                                           (1, 1, 1), gamma=gamma, cfl=cfl, precision=precision)
+        h = ctypes.c_void_p()
+        _check(load().gbfv_batch_create(ctypes.byref(self._desc), int(pool_bytes), int(max_members),
+                                        ctypes.byref(h)))
+        self.h = h
+        self.nvar = num_variables(equation)
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def member_bytes(self, n):
+        return _check(load().gbfv_batch_member_bytes(self.h, _c_int3(*n)))
+
+    def free_bytes(self):
+        t = ctypes.c_longlong()
+        lg = ctypes.c_longlong()
+        _check(load().gbfv_batch_free_bytes(self.h, ctypes.byref(t), ctypes.byref(lg)))
+        return t.value, lg.value
+
+    def add(self, n, lower, upper, prim, group=-1):
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        slot = ctypes.c_int()
+        _check(load().gbfv_batch_add(self.h, _c_int3(*n), _c_double3(*lower), _c_double3(*upper), _ptr(prim),
+                                     int(group), ctypes.byref(slot)))
+        return slot.value
+
+    def remove(self, slot):
+        _check(load().gbfv_batch_remove(self.h, int(slot)))
+
+    def advance(self, end_time, number_of_saves=0, max_steps=0):
+        _check(load().gbfv_batch_advance(self.h, end_time, number_of_saves, max_steps))
+
+    def member_time(self, slot):
+        t = ctypes.c_double()
+        s = ctypes.c_longlong()
+        _check(load().gbfv_batch_member_time(self.h, int(slot), ctypes.byref(t), ctypes.byref(s)))
+        return t.value, s.value
+
+    def member_state(self, slot, total):
+        U = np.zeros((self.nvar, total))
+        _check(load().gbfv_batch_member_state(self.h, int(slot), _ptr(U)))
+        return U
+
+    def stats(self, group, total):
+        m = np.zeros((self.nvar, total))
+        v = np.zeros((self.nvar, total))
+        c = ctypes.c_longlong()
+        _check(load().gbfv_batch_stats_result(self.h, int(group), _ptr(m), _ptr(v), ctypes.byref(c)))
+        return m, v, c.value
+
+    def stats_reset(self):
+        _check(load().gbfv_batch_stats_reset(self.h))
+
+    def launches(self):
+        n = ctypes.c_longlong()
+        _check(load().gbfv_batch_launches(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        _check(load().gbfv_batch_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+
+REQUEST_BURGERS, REQUEST_KELVIN_HELMHOLTZ = 0, 1
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("n", ctypes.c_int), ("end_time", ctypes.c_double),
+                ("phase", ctypes.c_double), ("sample", ctypes.c_int), ("arrival", ctypes.c_double),
+                ("keep", ctypes.c_int)]
+
+
+_SIGNATURES.update({
+    "gbfv_batch_finished": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_batch_active": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_server_create": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_server_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_server_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_server_final_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong]),
+    "gbfv_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_server_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+})
+
+
+class Server:
+    """Continuous-batching request loop (gbfv_server_*)."""
+
+    def __init__(self, budget_bytes, precision=FP32, max_slots=4096):
+        h = ctypes.c_void_p()
+        _check(load().gbfv_server_create(int(budget_bytes), precision, int(max_slots), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, kind, n, end_time, phase=0.0, sample=0, arrival=0.0, keep=False):
+        r = _Request(kind, n, end_time, phase, sample, arrival, 1 if keep else 0)
+        i = ctypes.c_int()
+        _check(load().gbfv_server_submit(self.h, ctypes.byref(r), ctypes.byref(i)))
+        return i.value
+
+    def run(self, steps_per_chunk=16):
+        _check(load().gbfv_server_run(self.h, int(steps_per_chunk)))
+
+    def result(self, rid):
+        a, ad, f = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        s = ctypes.c_longlong()
+        st = ctypes.c_int()
+        _check(load().gbfv_server_result(self.h, int(rid), ctypes.byref(a), ctypes.byref(ad), ctypes.byref(f),
+                                         ctypes.byref(s), ctypes.byref(st)))
+        return {"arrival": a.value, "admit": ad.value, "finish": f.value, "steps": s.value, "status": st.value}
+
+    def final_state(self, rid, size):
+        U = np.zeros(size)
+        _check(load().gbfv_server_final_state(self.h, int(rid), _ptr(U), int(size)))
+        return U
+
+    def stats(self, kind, n, size):
+        m = np.zeros(size)
+        v = np.zeros(size)
+        c = ctypes.c_longlong()
+        _check(load().gbfv_server_stats(self.h, int(kind), int(n), _ptr(m), _ptr(v), ctypes.byref(c)))
+        return m, v, c.value
+
+    def launches(self):
+        n = ctypes.c_longlong()
+        _check(load().gbfv_server_launches(self.h, ctypes.byref(n)))
+        return n.value

@@ -286,8 +286,197 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_uq(args):
+    """Batched UQ ensemble: `--uq-samples` Kelvin-Helmholtz samples, each with
+    its own seeded perturbation (generator sample = member index), grid sizes
+    drawn uniformly from {128^2, 256^2, 512^2} (log-uniform in size) with a
+    fixed seed, FP32 state, FP64 Welford statistics per grid size at T = 2.
+    The whole ensemble advances `--steps` time steps per timed region, each
+    member with its own dt. samples/s is extrapolated to T = 2 from the
+    measured ensemble cell-update rate and each size's initial dt; the plain
+    FP64 one-solve-at-a-time path is timed per size the same way and
+    extrapolated identically, so the ratio compares equal work."""
+    import numpy as np
+    import torch
+    from alsvinn_gb300 import lib
+
+    S = args.uq_samples
+    sizes_choice = (128, 256, 512)
+    rng = np.random.default_rng(20240611)
+    sizes = rng.choice(sizes_choice, size=S)
+    T = 2.0
+    scheme = ("euler2", "hll3", "weno2", "rungekutta3", "periodic")
+    b0 = lib.Batch(*scheme, 1 << 20, 1, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    pool = sum(b0.member_bytes((int(n), int(n), 1)) for n in sizes) + (64 << 20)
+    b0.close()
+    t0 = time.perf_counter()
+    b = lib.Batch(*scheme, pool, S, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    slots = []
+    for s in range(S):
+        n = int(sizes[s])
+        slots.append(b.add((n, n, 1), (0, 0, 0), (1, 1, 0), lib.init_kelvin_helmholtz(n, sample=s),
+                           group=sizes_choice.index(n)))
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.advance(T, 1, args.warmup)
+    torch.cuda.synchronize()
+    # each size's dt after warm-up -> steps to T
+    dts = {}
+    for s in range(S):
+        n = int(sizes[s])
+        if n not in dts:
+            t, st = b.member_time(slots[s])
+            dts[n] = t / st
+    launches0 = b.launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        e0.record(stream)
+        b.advance(T, 1, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = b.launches() - launches0
+    cells = float(sum(int(n) ** 2 for n in sizes))
+    rate = cells * args.steps / (ms * 1e-3)
+    work_to_T = sum((int(n) ** 2) * (T / dts[int(n)]) for n in sizes)
+    samples_per_s = S * rate / work_to_T
+    b.close()
+
+    # plain FP64, one solve at a time, each size
+    plain_step_ms = {}
+    for n in sizes_choice:
+        sv = lib.Solver(*scheme, (n, n, 1), (0, 0, 0), (1, 1, 0), gamma=1.4, cfl=0.4, precision=lib.FP64)
+        sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=0))
+        sv.advance(T, 1, 3)
+        st = torch.cuda.ExternalStream(sv.stream())
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        k = max(5, args.steps // 2)
+        a0.record(st)
+        sv.advance(T, 1, k)
+        a1.record(st)
+        torch.cuda.synchronize()
+        plain_step_ms[n] = a0.elapsed_time(a1) / k
+        sv.close()
+    plain_time_to_T = sum(plain_step_ms[int(n)] * 1e-3 * (T / dts[int(n)]) for n in sizes)
+    plain_samples_per_s = S / plain_time_to_T
+    line = {"metric": "UQ samples/s", "value": samples_per_s, "unit": "samples/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state, f64 statistics",
+            "data": "synthetic (seeded KH perturbation per member, generator sample = member index)",
+            "config": {"workload": "uq_kh_%d_samples_128_256_512_fp32" % S, "samples": S,
+                       "size_counts": {str(n): int((sizes == n).sum()) for n in sizes_choice},
+                       "end_time": T, "l2": "working set %.1f GB >> L2" % (pool / 1e9)},
+            "batched_cell_updates_per_s": rate,
+            "plain_fp64_one_at_a_time_samples_per_s": plain_samples_per_s,
+            "speedup_vs_plain_fp64": samples_per_s / plain_samples_per_s,
+            "plain_fp64_step_ms": {str(k): v for k, v in plain_step_ms.items()},
+            "initial_dt": {str(k): v for k, v in dts.items()},
+            "extrapolation": "samples/s = samples * measured rate / sum_i n_i^2 * (T / dt_i(initial))",
+            "setup_s": setup_s, "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Serving stream: `--serve-requests` solve requests with Poisson arrivals
+    at `--serve-rate` per second (fixed seed), half 1D Burgers (1024-8192 cells,
+    periodic, Godunov, WENO2, RK2, T=0.5, random phase U[-1,1]) and half 2D
+    Kelvin-Helmholtz (128^2-1024^2, seeded perturbation, T=1.0), grid sizes
+    log-uniform, FP32 state, FP64 statistics, 120 GB HBM budget. Latency is
+    completion minus arrival. The plain FP64 one-at-a-time comparison uses
+    measured FP64 step times per (kind, size) and each request's step count,
+    served first-come first-served one after another on the same arrivals."""
+    import numpy as np
+    import torch
+    from alsvinn_gb300 import lib
+
+    rng = np.random.default_rng(20240612)
+    R = args.serve_requests
+    gaps = rng.exponential(1.0 / args.serve_rate, size=R)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    kinds = rng.integers(0, 2, size=R)
+    reqs = []
+    for i in range(R):
+        if kinds[i] == lib.REQUEST_BURGERS:
+            n = int(rng.choice([1024, 2048, 4096, 8192]))
+            reqs.append((lib.REQUEST_BURGERS, n, 0.5, float(rng.uniform(-1, 1)), 0, float(arrivals[i])))
+        else:
+            n = int(rng.choice([128, 256, 512, 1024]))
+            reqs.append((lib.REQUEST_KELVIN_HELMHOLTZ, n, 1.0, 0.0, i, float(arrivals[i])))
+    budget = 120 * (1 << 30)
+    s = lib.Server(budget, precision=lib.FP32, max_slots=4096)
+    ids = [s.submit(k, n, T, phase=ph, sample=sm, arrival=a) for (k, n, T, ph, sm, a) in reqs]
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clocks:
+        s.run(args.serve_chunk)
+    wall = time.perf_counter() - t0
+    res = [s.result(i) for i in ids]
+    launches = s.launches()
+    s.close()
+    lat = np.array([r["finish"] - r["arrival"] for r in res])
+    done = sum(1 for r in res if r["status"] == 2)
+    steps = [r["steps"] for r in res]
+
+    # plain FP64, one solve at a time: measured step time per (kind, n)
+    step_ms = {}
+    for (k, n) in sorted({(r[0], r[1]) for r in reqs}):
+        if k == lib.REQUEST_BURGERS:
+            sv = lib.Solver("burgers", "godunov", "weno2", "rungekutta2", "periodic", (n, 1, 1), (0, 0, 0),
+                            (1, 1, 1), cfl=0.475, precision=lib.FP64)
+            sv.set_primitive(lib.init_burgers_sine(n, 0.3))
+            T = 0.5
+        else:
+            sv = lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (n, n, 1), (0, 0, 0), (1, 1, 0),
+                            cfl=0.4, precision=lib.FP64)
+            sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=0))
+            T = 1.0
+        sv.advance(T, 1, 5)
+        st = torch.cuda.ExternalStream(sv.stream())
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        kk = 40 if k == lib.REQUEST_BURGERS else 10
+        a0.record(st)
+        sv.advance(T, 1, kk)
+        a1.record(st)
+        torch.cuda.synchronize()
+        step_ms[(k, n)] = a0.elapsed_time(a1) / kk
+        sv.close()
+    clock = 0.0
+    plain_lat = []
+    for (k, n, T, ph, sm, a), nsteps in zip(reqs, steps):
+        start = max(clock, a)
+        clock = start + nsteps * step_ms[(k, n)] * 1e-3
+        plain_lat.append(clock - a)
+    plain_lat = np.array(plain_lat)
+    plain_rate = R / (clock - arrivals[0])
+    line = {"metric": "serving samples/s", "value": done / wall, "unit": "samples/s", "n_gpus": 1,
+            "steps": int(sum(steps)), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state, f64 statistics",
+            "data": "synthetic (Poisson arrivals, seeded phases / perturbations)",
+            "config": {"workload": "serve_burgers1d_kh2d_mix", "requests": R, "rate_per_s": args.serve_rate,
+                       "budget_bytes": budget, "steps_per_chunk": args.serve_chunk},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "completed": done, "wall_s": wall,
+            "plain_fp64_one_at_a_time": {"samples_per_s": plain_rate,
+                                         "latency_p50_s": float(np.percentile(plain_lat, 50)),
+                                         "latency_p99_s": float(np.percentile(plain_lat, 99)),
+                                         "method": "measured FP64 step time per (kind, n) x each request's "
+                                                   "steps, served FIFO one at a time on the same arrivals"},
+            "speedup_vs_plain_fp64": (done / wall) / plain_rate,
+            "fp64_step_ms": {"%s_%d" % ("burgers" if k == 0 else "kh", n): v for (k, n), v in step_ms.items()},
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="kh1024", choices=["kh1024", "uq", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--uq-samples", type=int, default=4096)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -298,6 +487,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "uq":
+        run_uq(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

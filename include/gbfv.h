@@ -178,6 +178,124 @@ int gbfv_stats_merge(gbfv_stats* st, const gbfv_stats* other);
 /* Writes mean and variance to host arrays of `count` doubles. */
 int gbfv_stats_result(gbfv_stats* st, double* mean_host, double* var_host, long long* samples);
 
+/* --------------------------------------------------------- ensembles */
+
+/* Many grids (members) of one scheme advanced together: the UQ ensemble of
+ * alsuq's Runner (alsuq/src/run/Runner.cpp:39-90), which the reference runs
+ * one sample after another. Each RK stage of the whole ensemble is one
+ * persistent launch over the tiles of every member; each member has its own
+ * dt (from its own wave-speed maximum) and its own time; a time step of the
+ * ensemble is replayed as a CUDA graph. Members may have different grid sizes
+ * but share the equation, scheme, precision and dimension. Member memory comes
+ * from one pool allocated at creation (the HBM budget). The integrator must be
+ * rungekutta2 or rungekutta3. */
+typedef struct gbfv_batch gbfv_batch;
+
+/* scheme: names, gamma, cfl, precision (its grid fields are ignored). */
+int gbfv_batch_create(const gbfv_desc* scheme, long long pool_bytes, int max_members, gbfv_batch** out);
+int gbfv_batch_destroy(gbfv_batch* b);
+
+/* Pool bytes a member with this grid needs (three padded state arrays), or a
+ * negative status. */
+long long gbfv_batch_member_bytes(const gbfv_batch* b, const int n[3]);
+int gbfv_batch_free_bytes(const gbfv_batch* b, long long* free_total, long long* largest_block);
+
+/* Adds a member from interior primitive initial data (as gbfv_set_primitive).
+ * group >= 0 folds the member's state at end_time into that group's FP64
+ * Welford mean / variance (every member of a group shares its grid); < 0: no
+ * statistics. GBFV_ERR_MEMORY when the pool or the slots are full. */
+int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const double upper[3],
+                   const double* prim_host, int group, int* slot);
+int gbfv_batch_remove(gbfv_batch* b, int slot);
+
+/* Advances every member until it reaches end_time with its own dt (the
+ * number_of_saves > 0 clamp lands each member exactly on the save times), or
+ * until max_steps more steps (max_steps <= 0: no limit). Members that reach
+ * end_time stop; their states are folded into their statistics group. */
+int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int max_steps);
+
+int gbfv_batch_member_time(gbfv_batch* b, int slot, double* t, long long* steps);
+int gbfv_batch_member_state(gbfv_batch* b, int slot, double* state_host);
+
+/* Mean and (population) variance of a statistics group over the whole padded
+ * state (the reference's statistics volumes include the ghost cells), as
+ * nvar * total doubles each; *count = members folded in. */
+int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double* var_host, long long* count);
+int gbfv_batch_stats_reset(gbfv_batch* b);
+
+/* Slots whose member has reached the end time of the last advance (up to
+ * capacity written; *count = all of them), and the number of members. */
+int gbfv_batch_finished(gbfv_batch* b, int* slots, int capacity, int* count);
+int gbfv_batch_active(const gbfv_batch* b, int* count);
+
+/* Kernels launched by the ensemble since creation, and its CUDA stream. */
+int gbfv_batch_launches(gbfv_batch* b, long long* launches);
+int gbfv_batch_stream(gbfv_batch* b, void** stream);
+
+/* ----------------------------------------------------------- serving */
+
+/* A continuous-batching request loop over two ensembles (no counterpart in
+ * the reference, whose alsuq runs a fixed list of samples). Requests arrive
+ * at their `arrival` time (seconds after gbfv_server_run starts), are
+ * admitted once their grid fits the HBM budget (first fit in arrival order),
+ * run next to the requests already in flight with their own dt, fold their
+ * final state into the FP64 statistics of their (kind, grid) group and leave,
+ * freeing their memory. Burgers and Kelvin-Helmholtz requests run in two
+ * ensembles driven by two host threads on two streams. */
+typedef enum { GBFV_REQUEST_BURGERS = 0, GBFV_REQUEST_KELVIN_HELMHOLTZ = 1 } gbfv_request_kind;
+
+typedef struct {
+    int kind;         /* gbfv_request_kind */
+    int n;            /* cells per dimension (Burgers: nx; KH: nx = ny) */
+    double end_time;
+    double phase;     /* Burgers: u0 = sin(2 pi x) + 0.5 phase, phase in [-1, 1] */
+    int sample;       /* KH: generator sample of the interface perturbation */
+    double arrival;   /* seconds after the start of gbfv_server_run */
+    int keep;         /* 1: keep the final state for gbfv_server_final_state */
+} gbfv_request;
+
+typedef struct gbfv_server gbfv_server;
+
+/* budget_bytes: device memory for the two ensembles' member states;
+ * precision: gbfv_precision of the states; max_slots: members per ensemble. */
+int gbfv_server_create(long long budget_bytes, int precision, int max_slots, gbfv_server** out);
+int gbfv_server_destroy(gbfv_server* s);
+/* Queue requests before gbfv_server_run; their arrival times pace admission. */
+int gbfv_server_submit(gbfv_server* s, const gbfv_request* r, int* id);
+/* Serves every submitted request, advancing each ensemble in chunks of
+ * steps_per_chunk time steps between admissions. */
+int gbfv_server_run(gbfv_server* s, int steps_per_chunk);
+/* Times in seconds after the start of the run; status 2 done, 3 failed. */
+int gbfv_server_result(gbfv_server* s, int id, double* arrival_s, double* admit_s, double* finish_s,
+                       long long* steps, int* status);
+int gbfv_server_final_state(gbfv_server* s, int id, double* state_host, long long capacity);
+/* FP64 mean / variance of the final states of every request of a (kind, n). */
+int gbfv_server_stats(gbfv_server* s, int kind, int n, double* mean_host, double* var_host, long long* count);
+int gbfv_server_launches(gbfv_server* s, long long* launches);
+
+/* ---------------------------------------------------- initial data */
+
+/* Interior primitive variables of the benchmark workloads at the cell
+ * midpoints origin + dx*i + dx/2 (Grid::getCellMidpoints,
+ * alsfvm/src/grid/Grid.cpp:148-165), x fastest, one block per variable, ready
+ * for gbfv_set_primitive / gbfv_batch_add. They replace the reference's
+ * Python initial-data scripts for these workloads (PythonInitialData,
+ * alsfvm/src/init/PythonInitialData.cpp:84-281). */
+/* Sod: (rho,u,p) = (1,0,1) for x < 0, (0.125,0,0.1) otherwise. */
+int gbfv_init_sod(const int n[3], const double lower[3], const double upper[3], double* prim);
+/* Kelvin-Helmholtz: rho=2, u=-0.5 inside 0.25+d1(x) < y < 0.75+d2(x), else
+ * rho=1, u=0.5; v=0, p=2.5; d(x) = 0.01 sum_j a_j cos(b_j + 2 pi j x) with
+ * a = X[0:10] (d1), X[20:30] (d2) normalised to sum 1 and b = 2 pi X[10:20]
+ * (d1), 2 pi X[30:40] (d2); X are 40 draws of gbfv_uniform. */
+int gbfv_init_kelvin_helmholtz(const int n[3], const double lower[3], const double upper[3], const double X[40],
+                               double* prim);
+/* Taylor-Green: rho=1, u=sin x cos y cos z, v=-cos x sin y cos z, w=0,
+ * p = 100 + ((cos 2x + cos 2y)(cos 2z + 2) - 2)/16. */
+int gbfv_init_taylor_green(const int n[3], const double lower[3], const double upper[3], double* prim);
+/* Burgers: u = sin(2 pi x) + 0.5 * phase. */
+int gbfv_init_burgers_sine(const int n[3], const double lower[3], const double upper[3], double phase,
+                           double* prim);
+
 /* ------------------------------------------------------- generator */
 
 /* Uniform draws of the reference's sample generator: draw number

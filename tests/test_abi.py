@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     text = open(os.path.join(ROOT, "include", "gbfv.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gbfv_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char\*)\s+(gbfv_\w+)\s*\(", text, re.M)))
 
 
 def test_library_exports_every_declared_function():
@@ -65,3 +65,17 @@ def test_create_rejects_mismatched_combinations():
     with pytest.raises(lib.GbfvError) as e:
         lib.Solver("euler1", "hll3", "eno4", "rungekutta3", "periodic", (3, 1, 1), (0, 0, 0), (1, 1, 1))
     assert e.value.code == lib.ERR_UNSUPPORTED
+
+
+def test_initial_data_matches_the_workload_formulas():
+    """The library's initial data equal the formulas evaluated with Python's
+    math module (the same C library), bit for bit."""
+    import math
+
+    import workloads
+    assert np.array_equal(lib.init_sod(64), workloads.sod_prim(64))
+    for s in (0, 3):
+        assert np.array_equal(lib.init_kelvin_helmholtz(48, sample=s), workloads.kh_prim(48, lib.uniform(40, s)))
+    assert np.array_equal(lib.init_taylor_green(6), workloads.tg_prim(6))
+    assert np.array_equal(lib.init_burgers_sine(50, -0.37), workloads.burgers_prim(50, -0.37))
+    assert math.pi == 3.141592653589793

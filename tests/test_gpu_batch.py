@@ -1,0 +1,176 @@
+"""The ensemble engine (gbfv_batch_*): members of mixed grid sizes advanced
+together with their own dt must equal single-grid solves; their statistics
+must equal alsuq's MeanVariance over the same samples (the oracle); the FP32
+ensemble's mean must stay within 1e-4 of the FP64 oracle and its variance
+within 1e-2 (L1 errors scaled by the variable's or the density's L1 norm);
+admission follows the memory pool; a member's result is the same alone and in
+a mix."""
+import numpy as np
+import pytest
+
+import workloads
+from alsvinn_gb300 import lib
+from conftest import interior, rel_l1
+from oracle import fvoracle
+
+pytestmark = pytest.mark.gpu
+
+KH = dict(equation="euler2", flux="hll3", recon="weno2", integrator="rungekutta3", boundary="periodic",
+          lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4, cfl=0.4)
+
+
+def kh_member(n, sample):
+    return workloads.kh_prim(n, lib.uniform(40, sample))
+
+
+def solo(n, prim, end_time, nsaves, precision=lib.FP64, max_steps=0):
+    with lib.Solver(KH["equation"], KH["flux"], KH["recon"], KH["integrator"], KH["boundary"], (n, n, 1),
+                    KH["lower"], KH["upper"], gamma=KH["gamma"], cfl=KH["cfl"], precision=precision) as s:
+        s.set_primitive(prim)
+        s.advance(end_time, nsaves, max_steps)
+        t, steps, _ = s.time()
+        return s.get_state(), t, steps
+
+
+def kh_batch(pool_mb=256, members=64, precision=lib.FP64):
+    return lib.Batch(KH["equation"], KH["flux"], KH["recon"], KH["integrator"], KH["boundary"], pool_mb << 20,
+                     members, gamma=KH["gamma"], cfl=KH["cfl"], precision=precision)
+
+
+def test_members_equal_single_grid_solves(cuda_device):
+    sizes = [32, 48, 64, 32, 40]
+    T = 0.03
+    with kh_batch() as b:
+        slots = [b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, k)) for k, n in enumerate(sizes)]
+        b.advance(T, 1)
+        for k, (slot, n) in enumerate(zip(slots, sizes)):
+            total = (n + 4) ** 2
+            U = b.member_state(slot, total)
+            t, steps = b.member_time(slot)
+            ref, t_ref, steps_ref = solo(n, kh_member(n, k), T, 1)
+            assert (t, steps) == (t_ref, steps_ref)
+            assert t == T
+            assert np.array_equal(U, ref), n
+
+
+def test_members_have_their_own_dt(cuda_device):
+    with kh_batch() as b:
+        a = b.add((32, 32, 1), KH["lower"], KH["upper"], kh_member(32, 0))
+        c = b.add((64, 64, 1), KH["lower"], KH["upper"], kh_member(64, 1))
+        b.advance(0.02, 1)
+        (ta, sa), (tc, sc) = b.member_time(a), b.member_time(c)
+        assert ta == tc == 0.02
+        assert sc > sa  # the finer grid takes more, smaller steps
+
+
+def var_error(var, v_ref):
+    """Per-variable L1 error of a variance field over max(its own L1 norm, the
+    density variance's): variances that start at zero stay meaningful."""
+    d = np.abs(var - v_ref).reshape(var.shape[0], -1).sum(1)
+    den = np.maximum(np.abs(v_ref).reshape(v_ref.shape[0], -1).sum(1), np.abs(v_ref[0]).sum())
+    return d / den
+
+
+def test_statistics_match_meanvariance(cuda_device):
+    # at 96^2 the 0.01 interface perturbation moves cells across the interface,
+    # so the samples differ and the variance is far from zero
+    n, M, T = 96, 5, 0.02
+    g = 2
+    with kh_batch() as b:
+        for s in range(M):
+            b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, s), group=0)
+        b.advance(T, 1)
+        mean, var, count = b.stats(0, (n + 2 * g) ** 2)
+    assert count == M
+    states = []
+    for s in range(M):
+        rc, U, t, _ = fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (n, n, 1), KH["lower"],
+                                   KH["upper"], 1.4, 0.4, T, 1, 0, kh_member(n, s), g, 4)
+        assert rc == 0 and t == T
+        states.append(U)
+    m_ref, v_ref = fvoracle.meanvar(states)
+    assert np.abs(v_ref[0]).sum() > 1e-5 * np.abs(m_ref[0]).sum()
+    assert (var_error(mean, m_ref) <= 1e-12).all(), var_error(mean, m_ref)
+    assert (var_error(var, v_ref) <= 1e-9).all(), var_error(var, v_ref)
+
+
+def test_fp32_ensemble_statistics_within_1e4_of_fp64(cuda_device):
+    n, M, T = 128, 6, 0.05
+    g = 2
+    with kh_batch(precision=lib.FP32) as b:
+        for s in range(M):
+            b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, s), group=0)
+        b.advance(T, 1)
+        mean, var, count = b.stats(0, (n + 2 * g) ** 2)
+    assert count == M
+    states = []
+    for s in range(M):
+        rc, U, t, _ = fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (n, n, 1), KH["lower"],
+                                   KH["upper"], 1.4, 0.4, T, 1, 0, kh_member(n, s), g, 4)
+        states.append(U)
+    m_ref, v_ref = fvoracle.meanvar(states)
+    # both scaled like var_error: the mean of the y momentum is close to zero
+    em = var_error(interior(mean, (n, n, 1), g), interior(m_ref, (n, n, 1), g))
+    ev = var_error(interior(var, (n, n, 1), g), interior(v_ref, (n, n, 1), g))
+    assert (em <= 1e-4).all(), em
+    # The Kelvin-Helmholtz shear layer amplifies any perturbation of grid-scale
+    # modes by about exp(k du t): FP32 rounding (1e-7) grows to ~1e-3 at the
+    # interface cells by t = 0.05, which is where the variance lives. The mean
+    # stays within 1e-4; the variance within 1e-2 of the FP64 reference.
+    assert (ev <= 1e-2).all(), ev
+
+
+def test_rk2_members_alternate_buffers(cuda_device):
+    n, T = 256, 0.2
+    prim = workloads.burgers_prim(n, 0.3)
+    with lib.Batch("burgers", "godunov", "weno2", "rungekutta2", "periodic", 64 << 20, 8, cfl=0.475, dim=1) as b:
+        s1 = b.add((n, 1, 1), (0, 0, 0), (1, 1, 1), prim)
+        s2 = b.add((n // 2, 1, 1), (0, 0, 0), (1, 1, 1), workloads.burgers_prim(n // 2, -0.2))
+        b.advance(T, 1)
+        U = b.member_state(s1, n + 4)
+        t, steps = b.member_time(s1)
+        U2 = b.member_state(s2, n // 2 + 4)
+    with lib.Solver("burgers", "godunov", "weno2", "rungekutta2", "periodic", (n, 1, 1), (0, 0, 0), (1, 1, 1),
+                    cfl=0.475) as s:
+        s.set_primitive(prim)
+        s.advance(T, 1)
+        ref = s.get_state()
+        t_ref, steps_ref, _ = s.time()
+    assert (t, steps) == (t_ref, steps_ref)
+    assert np.array_equal(U, ref)
+    with lib.Solver("burgers", "godunov", "weno2", "rungekutta2", "periodic", (n // 2, 1, 1), (0, 0, 0),
+                    (1, 1, 1), cfl=0.475) as s:
+        s.set_primitive(workloads.burgers_prim(n // 2, -0.2))
+        s.advance(T, 1)
+        assert np.array_equal(U2, s.get_state())
+
+
+def test_admission_follows_the_pool(cuda_device):
+    with kh_batch(pool_mb=1, members=8) as b:
+        per = b.member_bytes((64, 64, 1))
+        assert per == 3 * ((4 * 68 * 68 * 8 + 255) // 256 * 256)
+        fits = (1 << 20) // per
+        slots = [b.add((64, 64, 1), KH["lower"], KH["upper"], kh_member(64, k)) for k in range(fits)]
+        with pytest.raises(lib.GbfvError) as e:
+            b.add((64, 64, 1), KH["lower"], KH["upper"], kh_member(64, 99))
+        assert e.value.code == lib.ERR_MEMORY
+        b.remove(slots[0])
+        b.add((64, 64, 1), KH["lower"], KH["upper"], kh_member(64, 99))
+        total, largest = b.free_bytes()
+        assert total == (1 << 20) - fits * per
+
+
+def test_member_result_is_the_same_alone_and_in_a_mix(cuda_device):
+    T = 0.04
+    with kh_batch() as b:
+        x = b.add((40, 40, 1), KH["lower"], KH["upper"], kh_member(40, 5))
+        b.advance(T, 1)
+        alone = b.member_state(x, 44 * 44)
+    with kh_batch() as b:
+        others = [b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, 10 + n)) for n in (32, 64, 24)]
+        b.advance(T / 2, 0, 3)  # the mix is already running when x arrives
+        x = b.add((40, 40, 1), KH["lower"], KH["upper"], kh_member(40, 5))
+        b.advance(T, 1)
+        mixed = b.member_state(x, 44 * 44)
+        assert all(b.member_time(s)[0] == T for s in others)
+    assert np.array_equal(alone, mixed)
