@@ -27,7 +27,7 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "libfvoracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + INCLUDE]
 
-VARIANTS = (0, 1, 2)   # fp64, fp64 exact, fp32
+VARIANTS = (0, 1, 2, 3)   # fp64, fp64 exact, fp32, fp64 state with double-float arithmetic
 EQUATIONS = (0, 1, 2, 3)  # burgers, euler1, euler2, euler3
 
 

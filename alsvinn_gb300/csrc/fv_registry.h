@@ -8,7 +8,7 @@
 namespace gbfv {
 
 // Arithmetic variants of the step.
-enum Variant { VAR_F64 = 0, VAR_F64_EXACT = 1, VAR_F32 = 2, NUM_VARIANTS = 3 };
+enum Variant { VAR_F64 = 0, VAR_F64_EXACT = 1, VAR_F32 = 2, VAR_F64_DF = 3, NUM_VARIANTS = 4 };
 enum Equation { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3, NUM_EQ = 4 };
 enum Flux { FL_HLL = 0, FL_HLL3 = 1, FL_GODUNOV = 2, NUM_FLUX = 3 };
 constexpr int NUM_RECON = 5;

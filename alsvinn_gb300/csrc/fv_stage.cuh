@@ -19,6 +19,9 @@
 // rebuilds U1 on the fly from U0 and L0, so U1 is never stored and an RK3 step
 // moves the algorithmic 8 * nvar state words per cell.
 #pragma once
+#include <type_traits>
+
+#include "fv_df.cuh"
 #include "fv_math.cuh"
 #include "fv_types.h"
 
@@ -191,18 +194,25 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 // One tile of one stage: shared by the single-grid kernel (one CTA per tile)
 // and the persistent ensemble kernel (each CTA loops over a list of tiles of
 // many grids). Every thread of the CTA calls it; it synchronises internally.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+// R is the storage type of the state in HBM, C the type the reconstruction and
+// flux arithmetic runs in (C = R, or the double-float type for an FP64 state).
+// With C != R the combination with the stage inputs re-reads the exact R
+// values of the thread's own cell (L1/L2 hits: the tile load just fetched them)
+// and runs in R.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
 __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
                                            double (*wred)[3]) {
-    using Ph = Physics<R, EQ, FLUX>;
+    using Ph = Physics<C, EQ, FLUX>;
+    using PhR = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     constexpr int G = ReconTraits<RC>::ghosts;
-    using SL = SmemLayout<R, NV, G, DIM, TX, TY, TZ>;
+    using SL = SmemLayout<C, NV, G, DIM, TX, TY, TZ>;
     constexpr int NT = TX * TY * TZ;
-    R* su = reinterpret_cast<R*>(smem_raw);
-    R* rl = su + NV * SL::HALO;
-    R* rr = rl + NV * SL::REC;
-    R* fc = rr + NV * SL::REC;
+    constexpr bool kSame = std::is_same<R, C>::value;
+    C* su = reinterpret_cast<C*>(smem_raw);
+    C* rl = su + NV * SL::HALO;
+    C* rr = rl + NV * SL::REC;
+    C* fc = rr + NV * SL::REC;
 
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;
@@ -229,26 +239,26 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
                 } else {
                     v = in[k * total + gi];
                 }
-                su[k * SL::HALO + w] = v;
+                su[k * SL::HALO + w] = C(v);
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = R(1);
+            for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = C(1);
         }
     }
     __syncthreads();
 
     // 2. flux difference per direction
-    R acc[NV];
+    C acc[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = R(0);
+    for (int k = 0; k < NV; ++k) acc[k] = C(0);
     double wsd[3] = {0.0, 0.0, 0.0};
-    const R gamma = (R)A.gamma;
-    tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
+    const C gamma = C(A.gamma);
+    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
     if constexpr (DIM > 1)
-        tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
     if constexpr (DIM > 2)
-        tile_direction<R, EQ, FLUX, RC, DIM, TX, TY, TZ, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
 
     // 3. wave speeds (stage 0 only): warp max, CTA max, one atomic per direction
     if (mode == MODE_L) {
@@ -276,12 +286,20 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     R res[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
+        const R acck = (R)acc[k];
         if (mode == MODE_L) {
-            res[k] = acc[k];
+            res[k] = acck;
         } else {
-            const R uin = su[k * SL::HALO + sidx];
+            R uin;
+            if constexpr (kSame) {
+                uin = su[k * SL::HALO + sidx];
+            } else if (mode == MODE_RK3_S1 || mode == MODE_RK2_S1) {
+                uin = add_rn(mul_rn(l0[k * total + own], scale), in[k * total + own]);
+            } else {
+                uin = in[k * total + own];
+            }
             const R base = u0[k * total + own];
-            R v = add_rn(mul_rn(acc[k], scale), uin);
+            R v = add_rn(mul_rn(acck, scale), uin);
             if (mode == MODE_RK3_S1) {
                 v = mul_rn(v, R(1. / 3.));
                 v = add_rn(v, base);
@@ -297,7 +315,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             res[k] = v;
         }
     }
-    if (A.check && !Ph::obeys(res, gamma)) {
+    if (A.check && !PhR::obeys(res, (R)A.gamma)) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     int px[3], py[3], pz[3];
@@ -314,13 +332,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             }
 }
 
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
 __global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double wred[(TX * TY * TZ) / 32][3];
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
-    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ>(A, org, smem_raw, wred);
+    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, C>(A, org, smem_raw, wred);
 }
 
 // Persistent ensemble stage: each CTA walks the tile list (tiles of every
@@ -328,7 +346,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
 // is done is skipped as a whole; the per-member wave-speed maxima land in
 // that member's step state (a segmented reduction), so every member gets its
 // own dt.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ>
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
 __global__ void __launch_bounds__(TX* TY* TZ) batch_stage_kernel(BatchArgs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double wred[(TX * TY * TZ) / 32][3];
@@ -359,7 +377,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) batch_stage_kernel(BatchArgs B) {
             A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
         }
         const int org[3] = {tile.y, tile.z, tile.w};
-        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ>(A, org, smem_raw, wred);
+        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, C>(A, org, smem_raw, wred);
         __syncthreads();
     }
 }

@@ -1,7 +1,8 @@
 // Kernel instantiations for one arithmetic variant and one equation. This file
 // is compiled once per (FV_VARIANT, FV_EQ) pair; the exact variant is built
 // with -fmad=false and FV_EXACT so that no multiply-add is contracted.
-//   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic
+//   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic,
+//               3 fp64 state with double-float arithmetic on the FP32 pipes
 //   FV_EQ:      0 burgers, 1 euler1, 2 euler2, 3 euler3
 #define FV_NS_CAT2(a, b) a##b
 #define FV_NS_CAT(a, b) FV_NS_CAT2(a, b)
@@ -21,6 +22,13 @@ typedef float Real;
 #else
 typedef double Real;
 #endif
+// arithmetic of reconstruction and fluxes: the storage type, or double-float
+// on the FP32 pipes for the FP64 state of variant 3
+#if FV_VARIANT == 3
+typedef gbfv::dfloat Compute;
+#else
+typedef Real Compute;
+#endif
 
 #define FV_CAT2(a, b, c, d) a##b##c##d
 #define FV_CAT(a, b, c, d) FV_CAT2(a, b, c, d)
@@ -37,9 +45,9 @@ template <> struct TileShape<3> { static constexpr int X = 8, Y = 8, Z = 4; };
 template <int EQ, int FLUX, int RC, int DIM>
 struct StageEntry {
     using TS = TileShape<DIM>;
-    using SL = SmemLayout<Real, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
     static int launch(const StageArgs& a, cudaStream_t s) {
-        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z>;
+        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, Compute>;
         static int configured = 0;
         if (!configured) {
             cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
@@ -55,9 +63,9 @@ struct StageEntry {
 template <int EQ, int FLUX, int RC, int DIM>
 struct BatchEntry {
     using TS = TileShape<DIM>;
-    using SL = SmemLayout<Real, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
     static int launch(const BatchArgs& a, int ctas, cudaStream_t s) {
-        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z>;
+        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, Compute>;
         static int resident = 0;
         if (!resident) {
             cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);

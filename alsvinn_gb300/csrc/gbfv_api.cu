@@ -18,6 +18,7 @@
 GBFV_REGISTER_DECL(0, 0) GBFV_REGISTER_DECL(0, 1) GBFV_REGISTER_DECL(0, 2) GBFV_REGISTER_DECL(0, 3)
 GBFV_REGISTER_DECL(1, 0) GBFV_REGISTER_DECL(1, 1) GBFV_REGISTER_DECL(1, 2) GBFV_REGISTER_DECL(1, 3)
 GBFV_REGISTER_DECL(2, 0) GBFV_REGISTER_DECL(2, 1) GBFV_REGISTER_DECL(2, 2) GBFV_REGISTER_DECL(2, 3)
+GBFV_REGISTER_DECL(3, 0) GBFV_REGISTER_DECL(3, 1) GBFV_REGISTER_DECL(3, 2) GBFV_REGISTER_DECL(3, 3)
 
 namespace gbfv {
 
@@ -28,6 +29,7 @@ Registry& registry() {
         gbfv_register_v0_e0(&r); gbfv_register_v0_e1(&r); gbfv_register_v0_e2(&r); gbfv_register_v0_e3(&r);
         gbfv_register_v1_e0(&r); gbfv_register_v1_e1(&r); gbfv_register_v1_e2(&r); gbfv_register_v1_e3(&r);
         gbfv_register_v2_e0(&r); gbfv_register_v2_e1(&r); gbfv_register_v2_e2(&r); gbfv_register_v2_e3(&r);
+        gbfv_register_v3_e0(&r); gbfv_register_v3_e1(&r); gbfv_register_v3_e2(&r); gbfv_register_v3_e3(&r);
         return r;
     }();
     return R;

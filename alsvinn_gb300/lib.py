@@ -12,7 +12,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libgbfv.so")
 
-FP64, FP64_EXACT, FP32 = 0, 1, 2
+FP64, FP64_EXACT, FP32, FP64_DF = 0, 1, 2, 3
 OK, ERR_ARGUMENT, ERR_CUDA, ERR_CONSTRAINT, ERR_MEMORY, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5
 
 _c_int3 = ctypes.c_int * 3

@@ -43,8 +43,11 @@ typedef enum {
     GBFV_FP64 = 0,        /* FP64 state, FP64 arithmetic: the drop-in path */
     GBFV_FP64_EXACT = 1,  /* FP64, reference operation order, no contraction:
                              bit-identical to the reference CPU path */
-    GBFV_FP32 = 2         /* FP32 state and arithmetic; dt, wave speeds and
+    GBFV_FP32 = 2,        /* FP32 state and arithmetic; dt, wave speeds and
                              statistics in FP64 */
+    GBFV_FP64_DF = 3      /* FP64 state and FP64 Runge-Kutta update;
+                             reconstruction and fluxes in double-float
+                             (two FP32 numbers, ~48 bits) on the FP32 pipes */
 } gbfv_precision;
 
 typedef struct {

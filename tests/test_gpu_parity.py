@@ -25,7 +25,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FLUX_GRIDS = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
-TOL = {lib.FP64_EXACT: 0.0, lib.FP64: 1e-10, lib.FP32: 1e-4}
+TOL = {lib.FP64_EXACT: 0.0, lib.FP64: 1e-10, lib.FP64_DF: 1e-10, lib.FP32: 1e-4}
 FP32_TOL = {"burgers96_eno4_rk3": 2e-2}
 
 
@@ -58,7 +58,7 @@ def flux_keys():
     return sorted({k.rsplit("_", 1)[0] for k in z.files})
 
 
-@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP32])
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP64_DF, lib.FP32])
 @pytest.mark.parametrize("key", flux_keys())
 def test_compute_flux_matches_reference(cuda_device, key, precision):
     z = np.load(os.path.join(GOLDEN, "flux.npz"))
@@ -81,9 +81,10 @@ def test_compute_flux_matches_reference(cuda_device, key, precision):
         # flux differences of a smooth field are small: compare against the
         # flux magnitude scale rather than the difference itself
         err = np.abs(a - b).reshape(a.shape[0], -1).sum(1) / np.maximum(np.abs(b).reshape(b.shape[0], -1).sum(1), 1e-30)
-        tol = 1e-10 if precision == lib.FP64 else 5e-3
+        tol = {lib.FP64: 1e-10, lib.FP64_DF: 1e-10}.get(precision, 5e-3)
         assert (err <= tol).all(), err
-        assert np.allclose(ws, ref_ws, rtol=1e-13 if precision == lib.FP64 else 1e-5, atol=0)
+        rtol = {lib.FP64: 1e-13, lib.FP64_DF: 1e-12}.get(precision, 1e-5)
+        assert np.allclose(ws, ref_ws, rtol=rtol, atol=0)
 
 
 @pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64])
@@ -136,7 +137,7 @@ def run_gpu(case, precision, prim=None):
         return s.get_state(), t, steps
 
 
-@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP32])
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP64_DF, lib.FP32])
 @pytest.mark.parametrize("name", sorted(workloads.GOLDEN_RUNS))
 def test_run_matches_reference(cuda_device, name, precision):
     z = np.load(os.path.join(GOLDEN, "runs.npz"))
@@ -150,7 +151,7 @@ def test_run_matches_reference(cuda_device, name, precision):
         assert steps == ref_steps and t == ref_t
         assert np.array_equal(U, ref)
         return
-    if precision == lib.FP64:
+    if precision in (lib.FP64, lib.FP64_DF):
         assert steps == ref_steps
         assert abs(t - ref_t) <= 1e-12 * max(1.0, abs(ref_t))
         err = rel_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
@@ -186,7 +187,7 @@ LARGE = {
 }
 
 
-@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64])
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP64_DF])
 @pytest.mark.parametrize("name", sorted(LARGE))
 def test_larger_runs_match_oracle(cuda_device, name, precision):
     case = LARGE[name]
@@ -205,7 +206,11 @@ def test_larger_runs_match_oracle(cuda_device, name, precision):
     else:
         assert steps == ref_steps
         err = rel_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
-        assert (err <= 1e-10).all(), err
+        # double-float arithmetic carries ~2^-47 relative error; Taylor-Green's
+        # z momentum starts at zero under a pressure of 100, so its flux
+        # differences sit on |F| ~ 100: measured 4.3e-10 there, <= 4e-11 elsewhere
+        tol = 1e-9 if (precision == lib.FP64_DF and name.startswith("tg")) else 1e-10
+        assert (err <= tol).all(), err
 
 
 def test_fp32_state_error_against_fp64_reference(cuda_device):
