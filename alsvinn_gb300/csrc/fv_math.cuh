@@ -38,6 +38,54 @@ template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return rsq
 
 template <class R> __device__ __forceinline__ R rcp_(R x) { return R(1) / x; }
 
+// FP64 reciprocal and reciprocal square root for the fast policy: a hardware
+// approximation (PTX rcp.approx / rsqrt.approx .f64) refined by two
+// Newton-Raphson steps, y <- y (2 - x y) and y <- y (3 - x y^2) / 2, each of
+// which doubles the number of correct bits; the result is within about an ulp
+// of the correctly rounded value, in fewer FP64 instructions than an IEEE
+// division or square root.
+template <> __device__ __forceinline__ double rcp_<double>(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double h = 0.5 * x;
+    double t = fma(-h * y, y, 0.5);
+    y = fma(y, t, y);
+    t = fma(-h * y, y, 0.5);
+    return fma(y, t, y);
+}
+
+// sqrt(x) = x / sqrt(x) for positive finite x; zero, negative and NaN
+// arguments take the IEEE square root
+template <class R> __device__ __forceinline__ R sqrt_(R x) { return sqrt(x); }
+template <> __device__ __forceinline__ double sqrt_<double>(double x) {
+    return (x > 0.0 && x < 1e300) ? x * rsqrt_nr(x) : sqrt(x);
+}
+
+// 1/rho and sqrt(rho) of a density: one reciprocal square root for FP64
+template <class R> __device__ __forceinline__ void inv_sqrt_pair(R rho, R& rinv, R& w) {
+    rinv = rcp_(rho);
+    w = sqrt(rho);
+}
+template <> __device__ __forceinline__ void inv_sqrt_pair<double>(double rho, double& rinv, double& w) {
+    if (rho > 0.0 && rho < 1e300) {
+        const double rs = rsqrt_nr(rho);
+        rinv = rs * rs;
+        w = rho * rs;
+    } else {
+        rinv = 1.0 / rho;
+        w = sqrt(rho);
+    }
+}
+
 // ---------------------------------------------------------------- Euler
 
 // Conserved variables of one cell side plus the derived pressure and velocity
@@ -45,6 +93,7 @@ template <class R> __device__ __forceinline__ R rcp_(R x) { return R(1) / x; }
 template <class R, int NSD> struct EulerState {
     R rho, m[NSD], E, p, u[NSD];
     R rinv;  // 1/rho (fast policy only)
+    R w;     // sqrt(rho) (fast policy only)
 };
 
 template <class R, int NSD>
@@ -58,7 +107,7 @@ __device__ __forceinline__ void euler_extra(EulerState<R, NSD>& a, R gamma) {
         for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] / a.rho;
         a.p = (gamma - R(1)) * ie;
     } else {
-        a.rinv = rcp_(a.rho);
+        inv_sqrt_pair(a.rho, a.rinv, a.w);
 #pragma unroll
         for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] * a.rinv;
         a.p = (gamma - R(1)) * (a.E - R(0.5) * dot * a.rinv);
@@ -105,15 +154,15 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
         speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
         speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
     } else {
-        const R waveLeft = sqrt(L.rho);
-        const R waveRight = sqrt(Rs.rho);
+        const R waveLeft = L.w;
+        const R waveRight = Rs.w;
         const R winv = rcp_(waveLeft + waveRight);
         const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
         const R p = (waveLeft * L.p + waveRight * Rs.p) * winv;
-        const R cfLeft = sqrt(gamma * L.p * L.rinv);
-        const R cfRight = sqrt(gamma * Rs.p * Rs.rinv);
+        const R cfLeft = sqrt_(gamma * L.p * L.rinv);
+        const R cfRight = sqrt_(gamma * Rs.p * Rs.rinv);
         const R correct = R(0.5) * fmax(R(0), L.u[D] - Rs.u[D]);
-        const R cs = sqrt(R(2) * gamma * p / (L.rho + Rs.rho));
+        const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
         speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
         speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
     }
@@ -123,7 +172,9 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
     const R udl = L.u[D] - speedLeft;
     const R udr = Rs.u[D] - speedRight;
     const R aa = udr * Rs.rho - udl * L.rho;
-    const R sm = (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) / aa;
+    const R ainv = kExact ? R(0) : rcp_(aa);
+    const R sm = kExact ? (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) / aa
+                        : (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) * ainv;
     if (speedLeft == R(0)) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = R(0);
@@ -153,7 +204,6 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
             const R pp = S.p + S.rho * (S.u[D] - sm) * ud;
             mid[1 + NSD] = (ud * S.E + S.p * S.u[D] - pp * sm) / (sm - s);
         } else {
-            const R ainv = rcp_(aa);
             const R sinv = rcp_(sm - s);
             mid[0] = S.rho * ud * sinv;
 #pragma unroll
@@ -179,8 +229,8 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
                                       R gamma, R* F) {
     constexpr int NV = NSD + 2;
     R speedLeft, speedRight;
-    const R waveLeft = sqrt(L.rho);
-    const R waveRight = sqrt(Rs.rho);
+    const R waveLeft = kExact ? sqrt(L.rho) : L.w;
+    const R waveRight = kExact ? sqrt(Rs.rho) : Rs.w;
     if (kExact) {
         const R rho = (L.rho + Rs.rho) / R(2);
         const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) / (waveLeft + waveRight);
@@ -192,9 +242,9 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
         const R winv = rcp_(waveLeft + waveRight);
         const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
         const R p = (L.p * waveLeft + Rs.p * waveRight) * winv;
-        const R cs = sqrt(R(2) * gamma * p / (L.rho + Rs.rho));
-        speedLeft = fmin(L.u[D] - sqrt(gamma * L.p * L.rinv), ud - cs);
-        speedRight = fmax(Rs.u[D] + sqrt(gamma * Rs.p * Rs.rinv), ud + cs);
+        const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
+        speedLeft = fmin(L.u[D] - sqrt_(gamma * L.p * L.rinv), ud - cs);
+        speedRight = fmax(Rs.u[D] + sqrt_(gamma * Rs.p * Rs.rinv), ud + cs);
     }
     if (speedLeft == R(0)) {
 #pragma unroll
