@@ -25,17 +25,59 @@ using ::fmin;
 using ::sqrt;
 using std::isfinite;
 
+// float -> double by bit construction for normal floats: GB300 executes the
+// F2F conversions on its FP64 pipe (1/64 of the FP32 rate), so the
+// conversions at the edges of the double-float arithmetic are built from
+// integer operations instead. Zero keeps its sign; subnormal, infinite and NaN
+// floats take the conversion instruction.
+__device__ __forceinline__ double df_widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u)
+        return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                                ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                                ((unsigned long long)(u & 0x7fffffu) << 29)));
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
+    return (double)f;
+}
+
 struct dfloat {
     float hi, lo;
     __device__ __forceinline__ dfloat() : hi(0.f), lo(0.f) {}
     __device__ __forceinline__ dfloat(float h, float l) : hi(h), lo(l) {}
     __device__ __forceinline__ dfloat(int v) : hi((float)v), lo(0.f) {}
     __device__ __forceinline__ dfloat(float v) : hi(v), lo(0.f) {}
+    // Split of a double from its bit pattern: hi takes the leading 24
+    // significant bits (truncated), lo the remaining 29 bits rounded to 24,
+    // then one renormalisation. The tail is assembled from two exact float
+    // subtractions: a float with a fixed exponent field and k in its mantissa
+    // field, minus the bare power of two, is k times that power's ulp. The
+    // pair carries the double to 2^-48 relative, like a rounding split.
+    // Doubles outside [2^-80, 2^128) take the conversion instructions.
     __device__ __forceinline__ explicit dfloat(double v) {
-        hi = __double2float_rn(v);
-        lo = __double2float_rn(v - (double)hi);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+        const int E = (int)((hw >> 20) & 0x7ffu) - 1023;
+        if (E >= -80 && E <= 127) {
+            const unsigned sign = hw & 0x80000000u;
+            const float h = __uint_as_float(sign | ((unsigned)(E + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+            const unsigned r = lw & 0x1fffffffu;
+            const unsigned xa = (unsigned)(E - 23 + 127) << 23, xb = (unsigned)(E - 46 + 127) << 23;
+            const float pa = __fsub_rn(__uint_as_float(xa | (r >> 6)), __uint_as_float(xa));
+            const float pb = __fsub_rn(__uint_as_float(xb | ((r & 63u) << 17)), __uint_as_float(xb));
+            const float l = __uint_as_float(__float_as_uint(__fadd_rn(pa, pb)) | sign);
+            hi = __fadd_rn(h, l);
+            lo = __fsub_rn(l, __fsub_rn(hi, h));
+        } else if ((b << 1) == 0ull) {
+            hi = __uint_as_float(hw);  // signed zero
+            lo = 0.f;
+        } else {
+            hi = __double2float_rn(v);
+            lo = __double2float_rn(v - (double)hi);
+        }
     }
-    __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+    // hi + lo is exact in double (48 significant bits at most)
+    __device__ __forceinline__ explicit operator double() const { return df_widen(hi) + df_widen(lo); }
     __device__ __forceinline__ dfloat& operator+=(const dfloat& b);
 };
 

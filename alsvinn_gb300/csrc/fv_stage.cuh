@@ -35,6 +35,22 @@ template <class R> __device__ __forceinline__ R add_rn(R a, R b);
 template <> __device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
 template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
 
+// a * b + c: two IEEE roundings in the exact policy (the reference's
+// `out *= c; out += u`), one fused rounding otherwise
+template <class R> __device__ __forceinline__ R madd(R a, R b, R c) {
+    if constexpr (kExact)
+        return add_rn(mul_rn(a, b), c);
+    else
+        return fma(a, b, c);
+}
+
+template <class C> __device__ __forceinline__ C shfl_xor_c(C v, int off) {
+    return __shfl_xor_sync(0xffffffffu, v, off);
+}
+template <> __device__ __forceinline__ dfloat shfl_xor_c<dfloat>(dfloat v, int off) {
+    return dfloat(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
@@ -114,7 +130,7 @@ struct SmemLayout {
 // One direction D of the tile: reconstruct, face fluxes, accumulate into acc.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int D>
 __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc, R* acc, int tid,
-                                               const int* org, const Grid& G, R gamma, double& wsmax) {
+                                               const int* org, const Grid& G, R gamma, R& wsmax) {
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
@@ -171,7 +187,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 #pragma unroll
         for (int d = 0; d < 3; ++d)
             if (d != D) valid = valid && (org[d] + c[d] < G.n[d]);
-        if (valid) wsmax = fmax(wsmax, (double)w);
+        if (valid) wsmax = fmax(wsmax, w);
     }
     __syncthreads();
     // this thread's cell: acc += (-F_{i+1/2}) + F_{i-1/2}
@@ -232,13 +248,11 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             const long long gi = gidx(Gd, px, py, pz);
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                R v;
-                if (mode == MODE_RK3_S1 || mode == MODE_RK2_S1) {
-                    // U1 = L0 * c + U0, rounded as the reference's *= then +=
-                    v = add_rn(mul_rn(l0[k * total + gi], scale), in[k * total + gi]);
-                } else {
-                    v = in[k * total + gi];
-                }
+                // U1 = L0 * c + U0 (the reference's *= then +=), formed in R:
+                // the ENO stencil choices compare differences of these values
+                const R v = (mode == MODE_RK3_S1 || mode == MODE_RK2_S1)
+                                ? madd(l0[k * total + gi], scale, in[k * total + gi])
+                                : in[k * total + gi];
                 su[k * SL::HALO + w] = C(v);
             }
         } else {
@@ -252,7 +266,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     C acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = C(0);
-    double wsd[3] = {0.0, 0.0, 0.0};
+    // wave-speed maxima in the arithmetic type (the max is exact, so one
+    // conversion per thread gives the same double as converting every face)
+    C wsd[3] = {C(0), C(0), C(0)};
     const C gamma = C(A.gamma);
     tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
     if constexpr (DIM > 1)
@@ -264,10 +280,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     if (mode == MODE_L) {
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-            double v = wsd[d];
+            C v = wsd[d];
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-            if ((tid & 31) == 0) wred[tid >> 5][d] = v;
+            for (int off = 16; off > 0; off >>= 1) v = fmax(v, shfl_xor_c(v, off));
+            if ((tid & 31) == 0) wred[tid >> 5][d] = (double)v;
         }
         __syncthreads();
         if (tid < DIM) {
@@ -294,19 +310,17 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             if constexpr (kSame) {
                 uin = su[k * SL::HALO + sidx];
             } else if (mode == MODE_RK3_S1 || mode == MODE_RK2_S1) {
-                uin = add_rn(mul_rn(l0[k * total + own], scale), in[k * total + own]);
+                uin = madd(l0[k * total + own], scale, in[k * total + own]);
             } else {
                 uin = in[k * total + own];
             }
             const R base = u0[k * total + own];
-            R v = add_rn(mul_rn(acck, scale), uin);
+            R v = madd(acck, scale, uin);
             if (mode == MODE_RK3_S1) {
-                v = mul_rn(v, R(1. / 3.));
-                v = add_rn(v, base);
+                v = madd(v, R(1. / 3.), base);
                 v = mul_rn(v, R(3. / 4.));
             } else if (mode == MODE_RK3_S2) {
-                v = mul_rn(v, R(2));
-                v = add_rn(v, base);
+                v = madd(v, R(2), base);
                 v = mul_rn(v, R(1. / 3.));
             } else {  // MODE_RK2_S1
                 v = add_rn(v, base);
@@ -403,7 +417,7 @@ __global__ void fe_apply_kernel(StageArgs A) {
     const R scale = (R)A.st->scale;
     R res[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) res[k] = add_rn(mul_rn(l0[k * total + own], scale), out[k * total + own]);
+    for (int k = 0; k < NV; ++k) res[k] = madd(l0[k * total + own], scale, out[k * total + own]);
     if (A.check && !Ph::obeys(res, (R)A.gamma)) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }

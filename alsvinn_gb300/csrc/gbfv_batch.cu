@@ -683,6 +683,18 @@ int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double*
     return GBFV_OK;
 }
 
+int gbfv_batch_stats_export(gbfv_batch* b, int group, double* mean_host, double* m2_host, long long* count) {
+    if (!b || group < 0 || group >= (int)b->groups.size() || !b->groups[group].mean)
+        return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group");
+    BCUDA(cudaStreamSynchronize(b->stream));
+    BCUDA(cudaMemcpy(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost));
+    const GroupAcc& g = b->groups[group];
+    if (count) *count = g.count;
+    if (mean_host) BCUDA(cudaMemcpy(mean_host, g.mean, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
+    if (m2_host) BCUDA(cudaMemcpy(m2_host, g.m2, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
+    return GBFV_OK;
+}
+
 int gbfv_batch_stats_reset(gbfv_batch* b) {
     if (!b) return bfail(GBFV_ERR_ARGUMENT, "null batch");
     BCUDA(cudaStreamSynchronize(b->stream));

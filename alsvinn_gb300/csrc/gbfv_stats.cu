@@ -157,4 +157,15 @@ int gbfv_stats_result(gbfv_stats* st, double* mean, double* var, long long* samp
     return e == cudaSuccess ? GBFV_OK : sfail(GBFV_ERR_CUDA, cudaGetErrorString(e));
 }
 
+int gbfv_stats_export(gbfv_stats* st, double* mean, double* m2, long long* samples) {
+    if (!st) return sfail(GBFV_ERR_ARGUMENT, "null stats");
+    if (samples) *samples = st->n;
+    cudaError_t e = cudaSuccess;
+    if (mean) e = cudaMemcpyAsync(mean, st->mean, st->count * sizeof(double), cudaMemcpyDeviceToHost, st->stream);
+    if (m2 && e == cudaSuccess)
+        e = cudaMemcpyAsync(m2, st->m2, st->count * sizeof(double), cudaMemcpyDeviceToHost, st->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st->stream);
+    return e == cudaSuccess ? GBFV_OK : sfail(GBFV_ERR_CUDA, cudaGetErrorString(e));
+}
+
 }  // extern "C"

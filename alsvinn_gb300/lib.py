@@ -79,6 +79,8 @@ _SIGNATURES = {
     "gbfv_stats_merge": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "gbfv_stats_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_stats_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_void_p]),
     "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
@@ -99,6 +101,8 @@ _SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_member_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "gbfv_batch_stats_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_stats_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_stats_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "gbfv_batch_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
@@ -368,6 +372,14 @@ class Stats:
         _check(load().gbfv_stats_result(self.h, _ptr(m), _ptr(v), ctypes.byref(n)))
         return m, v, n.value
 
+    def export(self):
+        """(count, mean, M2): the raw Welford triple for a cross-rank merge."""
+        m = np.zeros(self.count)
+        q = np.zeros(self.count)
+        n = ctypes.c_longlong()
+        _check(load().gbfv_stats_export(self.h, _ptr(m), _ptr(q), ctypes.byref(n)))
+        return n.value, m, q
+
 
 class Batch:
     """An ensemble of grids advanced together (gbfv_batch_*)."""
@@ -440,6 +452,15 @@ class Batch:
         c = ctypes.c_longlong()
         _check(load().gbfv_batch_stats_result(self.h, int(group), _ptr(m), _ptr(v), ctypes.byref(c)))
         return m, v, c.value
+
+    def stats_export(self, group, total):
+        """(count, mean, M2) of one group: the raw Welford triple for a
+        cross-rank merge (alsvinn_gb300.uq.combine_statistics)."""
+        m = np.zeros((self.nvar, total))
+        q = np.zeros((self.nvar, total))
+        c = ctypes.c_longlong()
+        _check(load().gbfv_batch_stats_export(self.h, int(group), _ptr(m), _ptr(q), ctypes.byref(c)))
+        return c.value, m, q
 
     def stats_reset(self):
         _check(load().gbfv_batch_stats_reset(self.h))

@@ -180,6 +180,11 @@ int gbfv_stats_add_host(gbfv_stats* st, const double* sample_host);
 int gbfv_stats_merge(gbfv_stats* st, const gbfv_stats* other);
 /* Writes mean and variance to host arrays of `count` doubles. */
 int gbfv_stats_result(gbfv_stats* st, double* mean_host, double* var_host, long long* samples);
+/* Writes the raw Welford triple (sample count, mean, M2 = sum of squared
+ * deviations) for a cross-rank merge; the rank-level counterpart of the
+ * per-rank sums that alsuq/src/stats/StatisticsHelper.cpp:65-68 reduces. An
+ * empty accumulator gives samples = 0 and zero arrays. */
+int gbfv_stats_export(gbfv_stats* st, double* mean_host, double* m2_host, long long* samples);
 
 /* --------------------------------------------------------- ensembles */
 
@@ -224,6 +229,8 @@ int gbfv_batch_member_state(gbfv_batch* b, int slot, double* state_host);
  * state (the reference's statistics volumes include the ghost cells), as
  * nvar * total doubles each; *count = members folded in. */
 int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double* var_host, long long* count);
+/* The raw Welford triple of one group (see gbfv_stats_export). */
+int gbfv_batch_stats_export(gbfv_batch* b, int group, double* mean_host, double* m2_host, long long* count);
 int gbfv_batch_stats_reset(gbfv_batch* b);
 
 /* Slots whose member has reached the end time of the last advance (up to
