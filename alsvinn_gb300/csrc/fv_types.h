@@ -25,14 +25,18 @@ struct StepState {
     long long step_limit;           // advance step limit (< 0: none)
     int just_done;                  // ensemble: reached end_time in the step just finished
     int group;                      // ensemble: statistics group (< 0: none)
+    long long number_saved2;        // second save clamp's counter (FixedIntervalStatistics, starts at 1)
+    int saved_mask;                 // bit k: save counter k advanced in the step just finished
 };
 
 struct StepParams {
     double cfl;
     double cell_lengths[3];
     double end_time;
-    double time_interval;  // 0: no save-time clamp
+    double time_interval;       // 0: no save-time clamp
     int dim;
+    double time_interval2 = 0;  // second clamp (statistics save times); 0: none
+    int stop_at_save = 0;       // end the advance after a step that reached a save time
 };
 
 struct Grid {

@@ -55,6 +55,12 @@ __global__ void dt_kernel(StepState* st, StepParams P) {
         const double lim = nextSaveTime - st->t;
         dt = lim < dt ? lim : dt;
     }
+    // FixedIntervalStatistics::adjustTimestep (alsuq/src/stats/FixedIntervalStatistics.cpp:33-41)
+    if (P.time_interval2 > 0) {
+        const double nextSaveTime = (double)st->number_saved2 * P.time_interval2;
+        const double lim = nextSaveTime - st->t;
+        dt = lim < dt ? lim : dt;
+    }
     st->dt = dt;
     st->scale = dt / P.cell_lengths[0];
 }
@@ -65,9 +71,21 @@ __global__ void finish_kernel(StepState* st, StepParams P) {
     if (st->done) return;
     st->t = st->t + st->dt;
     st->steps += 1;
-    if (P.time_interval > 0 && st->t >= (double)st->number_saved * P.time_interval + 0.0) st->number_saved += 1;
+    // the writers' save counters (FixedIntervalWriter::write, FixedIntervalWriter.cpp:32-42;
+    // FixedIntervalStatistics::computeStatistics, FixedIntervalStatistics.cpp:71-86)
+    int saved = 0;
+    if (P.time_interval > 0 && st->t >= (double)st->number_saved * P.time_interval + 0.0) {
+        st->number_saved += 1;
+        saved |= 1;
+    }
+    if (P.time_interval2 > 0 && st->t >= (double)st->number_saved2 * P.time_interval2) {
+        st->number_saved2 += 1;
+        saved |= 2;
+    }
+    st->saved_mask = saved;
     st->ws_bits[0] = st->ws_bits[1] = st->ws_bits[2] = 0ull;
-    if (!(st->t < st->end_time) || (st->step_limit >= 0 && st->steps >= st->step_limit) || st->status != 0)
+    if (!(st->t < st->end_time) || (st->step_limit >= 0 && st->steps >= st->step_limit) || st->status != 0 ||
+        (P.stop_at_save && saved))
         st->done = 1;
 }
 
@@ -306,6 +324,7 @@ int gbfv_create(const gbfv_desc* d, gbfv_solver** out) {
         StepState z;
         std::memset(&z, 0, sizeof z);
         z.number_saved = 1;
+        z.number_saved2 = 1;
         z.done = 1;
         *s->st_host = z;
         e = cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream);
@@ -339,6 +358,7 @@ static int reset_time(gbfv_solver* s) {
     StepState z;
     std::memset(&z, 0, sizeof z);
     z.number_saved = 1;
+    z.number_saved2 = 1;
     z.done = 1;
     *s->st_host = z;
     CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream));
@@ -521,19 +541,8 @@ static int enqueue_step(gbfv_solver* s, const StepParams& P) {
     return GBFV_OK;
 }
 
-int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps) {
-    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
-    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    const long long limit = max_steps > 0 ? s->st_host->steps + max_steps : -1;
-    if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
-    StepParams P;
-    P.cfl = s->cfl;
-    for (int k = 0; k < 3; ++k) P.cell_lengths[k] = s->cell_lengths[k];
-    P.end_time = end_time;
-    P.time_interval = number_of_saves > 0 ? s->time_interval : 0.0;
-    P.dim = s->G.dim;
-    begin_kernel<<<1, 1, 0, s->stream>>>(s->st, end_time, limit);
+static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
+    begin_kernel<<<1, 1, 0, s->stream>>>(s->st, P.end_time, limit);
     CUDA_TRY(cudaGetLastError());
     s->launches += 1;
     int chunk = 1;
@@ -545,7 +554,8 @@ int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_s
         CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         if (s->st_host->done) break;
-        if (chunk < 64) chunk *= 2;
+        // a run that stops at save times checks after every step
+        if (chunk < 64 && !P.stop_at_save) chunk *= 2;
     }
     if (s->st_host->status != 0) {
         char msg[256];
@@ -555,6 +565,45 @@ int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_s
         return fail(GBFV_ERR_CONSTRAINT, msg);
     }
     return GBFV_OK;
+}
+
+static StepParams step_params(const gbfv_solver* s, double end_time) {
+    StepParams P;
+    P.cfl = s->cfl;
+    for (int k = 0; k < 3; ++k) P.cell_lengths[k] = s->cell_lengths[k];
+    P.end_time = end_time;
+    P.time_interval = 0.0;
+    P.dim = s->G.dim;
+    return P;
+}
+
+int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const long long limit = max_steps > 0 ? s->st_host->steps + max_steps : -1;
+    if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
+    StepParams P = step_params(s, end_time);
+    P.time_interval = number_of_saves > 0 ? s->time_interval : 0.0;
+    return drive(s, P, limit);
+}
+
+int gbfv_advance_schedule(gbfv_solver* s, const gbfv_schedule* sch, int* saved_mask) {
+    if (!s || !sch) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    if (!(sch->save_interval[0] >= 0) || !(sch->save_interval[1] >= 0))
+        return fail(GBFV_ERR_ARGUMENT, "save intervals must be non-negative");
+    if (saved_mask) *saved_mask = 0;
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const long long steps0 = s->st_host->steps;
+    const long long limit = sch->max_steps > 0 ? steps0 + sch->max_steps : -1;
+    StepParams P = step_params(s, sch->end_time);
+    P.time_interval = sch->save_interval[0];
+    P.time_interval2 = sch->save_interval[1];
+    P.stop_at_save = sch->stop_at_save != 0;
+    const int r = drive(s, P, limit);
+    if (saved_mask && s->st_host->steps > steps0) *saved_mask = s->st_host->saved_mask;
+    return r;
 }
 
 int gbfv_stream(gbfv_solver* s, void** stream) {
@@ -668,12 +717,56 @@ int gbfv_obeys_constraints(gbfv_solver* s, const void* U, int* ok) {
 
 // ------------------------------------------------------- generator
 
+// The process-wide engine of STLMersenne as an object: one mt19937_64 with
+// the default seed and the count of numbers it has produced
+// (alsuq/src/generator/STLMersenne.cpp:24-29).
+struct gbfv_generator {
+    std::mt19937_64 engine;
+    long long drawn = 0;
+};
+
 int gbfv_uniform(int dimension, int sample, double lower, double upper, double* out) {
     if (dimension <= 0 || sample < 0 || !out) return fail(GBFV_ERR_ARGUMENT, "bad arguments");
     std::mt19937_64 gen;  // default seed, as the reference's process-wide engine
     gen.discard((unsigned long long)sample * (unsigned long long)dimension);
     std::uniform_real_distribution<double> dist{0.0, 1.0};
     for (int c = 0; c < dimension; ++c) out[c] = dist(gen) * (upper - lower) + lower;
+    return GBFV_OK;
+}
+
+int gbfv_generator_create(gbfv_generator** out) {
+    if (!out) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *out = new gbfv_generator();
+    return GBFV_OK;
+}
+
+int gbfv_generator_destroy(gbfv_generator* g) {
+    delete g;
+    return GBFV_OK;
+}
+
+int gbfv_generator_uniform(gbfv_generator* g, int dimension, int component, long long sample, double lower,
+                           double upper, double* out) {
+    if (!g || !out || dimension <= 0 || component < 0 || sample < 0)
+        return fail(GBFV_ERR_ARGUMENT, "bad arguments");
+    if (component >= dimension) return fail(GBFV_ERR_ARGUMENT, "Component given higher than dimension");
+    const long long dim = dimension;
+    // skip forward to the sample's block, then to the component within it;
+    // a generator never moves backwards (a repeated or earlier request draws
+    // the next number, as the reference's engine does)
+    if (g->drawn / dim < sample) {
+        const long long skip = sample * dim - g->drawn;
+        g->engine.discard((unsigned long long)skip);
+        g->drawn += skip;
+    }
+    if (g->drawn % dim < component) {
+        const long long skip = component - g->drawn % dim;
+        g->engine.discard((unsigned long long)skip);
+        g->drawn += skip;
+    }
+    g->drawn += 1;
+    std::uniform_real_distribution<double> dist{0.0, 1.0};
+    *out = dist(g->engine) * (upper - lower) + lower;
     return GBFV_OK;
 }
 

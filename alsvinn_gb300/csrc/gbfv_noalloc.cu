@@ -74,6 +74,7 @@ extern "C" int gbfv_advance_noalloc(const gbfv_desc* desc, void* state_dev, doub
     h.t = *t_inout;
     h.steps = *steps_inout;
     h.number_saved = 1;
+    h.number_saved2 = 1;
     const double interval = number_of_saves > 0 ? end_time / number_of_saves : 0.0;
     if (number_of_saves > 0)
         for (int k = 0; k < (1 << 20) && h.t >= (double)h.number_saved * interval + 0.0; ++k) h.number_saved += 1;

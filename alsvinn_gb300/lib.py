@@ -81,6 +81,11 @@ _SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_stats_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_generator_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_generator_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_generator_uniform": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                              ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "gbfv_advance_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_void_p]),
     "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
@@ -219,6 +224,37 @@ def init_burgers_sine(n, phase, lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0)):
     return prim
 
 
+class _Schedule(ctypes.Structure):
+    _fields_ = [("end_time", ctypes.c_double), ("save_interval", ctypes.c_double * 2),
+                ("max_steps", ctypes.c_int), ("stop_at_save", ctypes.c_int)]
+
+
+class Generator:
+    """The run-wide mt19937_64 of alsuq's STLMersenne (gbfv_generator_*)."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _check(load().gbfv_generator_create(ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_generator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def uniform(self, dimension, component, sample, lower=0.0, upper=1.0):
+        out = ctypes.c_double()
+        _check(load().gbfv_generator_uniform(self.h, int(dimension), int(component), int(sample), float(lower),
+                                             float(upper), ctypes.byref(out)))
+        return out.value
+
+
 class Solver:
     """One grid on the GPU: the handle of gbfv_create."""
 
@@ -286,6 +322,13 @@ class Solver:
 
     def advance(self, end_time, number_of_saves=0, max_steps=0):
         return _check(load().gbfv_advance(self.h, end_time, number_of_saves, max_steps))
+
+    def advance_schedule(self, end_time, save_interval=(0.0, 0.0), max_steps=0, stop_at_save=False):
+        """gbfv_advance_schedule: returns the saved mask of the last step."""
+        sch = _Schedule(float(end_time), (ctypes.c_double * 2)(*save_interval), int(max_steps), int(bool(stop_at_save)))
+        mask = ctypes.c_int()
+        _check(load().gbfv_advance_schedule(self.h, ctypes.byref(sch), ctypes.byref(mask)))
+        return mask.value
 
     def advance_host(self, U, end_time, number_of_saves=0, max_steps=0):
         assert U.dtype == np.float64 and U.flags.c_contiguous and U.size == self.nvar * self.total

@@ -114,6 +114,27 @@ int gbfv_state_device(gbfv_solver* s, void** state_dev);
  * constraint check (CPUCellComputer::obeysConstraints). */
 int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps);
 
+/* A run schedule with the reference's two kinds of save-time clamp: the fvm
+ * writer's FixedIntervalWriter (alsfvm/src/io/FixedIntervalWriter.cpp:32-53,
+ * save k at k * save_interval[0]) and alsuq's FixedIntervalStatistics
+ * (alsuq/src/stats/FixedIntervalStatistics.cpp:33-86, at k * save_interval[1]);
+ * dt is clamped to the nearer next save time of each nonzero interval
+ * (interval = endTime / numberOfSaves, as SimulatorSetup.cpp and Setup.cpp
+ * form it). Both save counters start at 1 (the t = 0 write, when wanted, is
+ * the caller's) and reset with the time. */
+typedef struct gbfv_schedule {
+    double end_time;
+    double save_interval[2];
+    int max_steps;    /* <= 0: no step limit */
+    int stop_at_save; /* nonzero: return after the step at which a save time was reached */
+} gbfv_schedule;
+
+/* Advances under a schedule. *saved_mask receives, for the last step taken,
+ * bit k set when save counter k advanced in it (the step after which the
+ * reference calls that writer's write), 0 when no step was taken. Returns
+ * GBFV_ERR_CONSTRAINT as gbfv_advance does. */
+int gbfv_advance_schedule(gbfv_solver* s, const gbfv_schedule* schedule, int* saved_mask);
+
 /* The CUDA stream (cudaStream_t) the solver issues its work on. */
 int gbfv_stream(gbfv_solver* s, void** stream);
 
@@ -314,6 +335,21 @@ int gbfv_init_burgers_sine(const int n[3], const double lower[3], const double u
  * (replaces STLMersenne + Uniform, alsuq/src/generator/STLMersenne.cpp:38-85,
  * alsuq/src/distribution/Uniform.cpp:27-34). */
 int gbfv_uniform(int dimension, int sample, double lower, double upper, double* out);
+
+/* The stateful generator behind alsuq's sample parameters: one default-seeded
+ * mt19937_64 shared by every parameter of a run (the reference keeps it
+ * process-wide). gbfv_generator_uniform is STLMersenne::generate(component,
+ * sample) for a parameter of `dimension` components -- discard forward to
+ * draw sample * dimension, then to the component, never backwards -- followed
+ * by Uniform's x * (upper - lower) + lower (alsuq/src/generator/
+ * STLMersenne.cpp:38-85, alsuq/src/distribution/Uniform.cpp:27-34). Requests
+ * in the reference's order (samples ascending; per sample the parameters in
+ * name order, components ascending) reproduce its parameter values. */
+typedef struct gbfv_generator gbfv_generator;
+int gbfv_generator_create(gbfv_generator** out);
+int gbfv_generator_destroy(gbfv_generator* g);
+int gbfv_generator_uniform(gbfv_generator* g, int dimension, int component, long long sample, double lower,
+                           double upper, double* out);
 
 /* ----------------------------------------------- allocation-free stepping */
 

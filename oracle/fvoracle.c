@@ -794,6 +794,44 @@ int fv_uniform(int dimension, int sample, double lower, double upper, double* ou
     return 0;
 }
 
+/* The Runner's parameter draws (alsuq/src/run/Runner.cpp:39-52) through the
+ * process-wide engine of STLMersenne (alsuq/src/generator/STLMersenne.cpp:
+ * 24-85): per sample (ascending from sample_start), per parameter in the
+ * given order, per component: skip forward to draw sample * dim of that
+ * parameter when the count of numbers produced is behind it, then to the
+ * component within the block, draw one canonical double, scale it by
+ * Uniform (alsuq/src/distribution/Uniform.cpp:27-34). One fresh engine per
+ * call. */
+int fv_generate_sequence(int nparams, const int* dims, const double* lowers, const double* uppers,
+                         long long sample_start, long long nsamples, double* out) {
+    if (nparams <= 0 || sample_start < 0 || nsamples < 0) return fail(-1, "bad arguments");
+    for (int p = 0; p < nparams; ++p)
+        if (dims[p] <= 0) return fail(-1, "bad dimension");
+    mt64 g;
+    mt64_seed(&g, 5489ULL);
+    long long drawn = 0, k = 0;
+    for (long long s = sample_start; s < sample_start + nsamples; ++s)
+        for (int p = 0; p < nparams; ++p)
+            for (int c = 0; c < dims[p]; ++c) {
+                const long long dim = dims[p];
+                if (drawn / dim < s) {
+                    const long long skip = s * dim - drawn;
+                    for (long long i = 0; i < skip; ++i) mt64_next(&g);
+                    drawn += skip;
+                }
+                if (drawn % dim < c) {
+                    const long long skip = c - drawn % dim;
+                    for (long long i = 0; i < skip; ++i) mt64_next(&g);
+                    drawn += skip;
+                }
+                drawn += 1;
+                double r = (double)mt64_next(&g) / 18446744073709551616.0;
+                if (r >= 1.0) r = nextafter(1.0, 0.0);
+                out[k++] = r * (uppers[p] - lowers[p]) + lowers[p];
+            }
+    return 0;
+}
+
 /* ---------------------------------------------------------- statistics */
 
 /* MeanVariance::computeStatistics adds u and pow(u,2) per sample

@@ -52,6 +52,8 @@ int fv_obeys_constraints(const char* equation, const int n[3], int ghosts, doubl
                          const double* U);
 
 int fv_uniform(int dimension, int sample, double lower, double upper, double* out);
+int fv_generate_sequence(int nparams, const int* dims, const double* lowers, const double* uppers,
+                         long long sample_start, long long nsamples, double* out);
 
 int fv_meanvar(long count, int nsamples, const double* const* samples, double* mean,
                double* var);

@@ -113,6 +113,19 @@ def uniform(dimension, sample, lower=0.0, upper=1.0):
     return out
 
 
+def generate_sequence(dims, sample_start, nsamples, lowers=None, uppers=None):
+    """Runner-order parameter draws: array (nsamples, sum(dims))."""
+    dims = [int(d) for d in dims]
+    lowers = np.zeros(len(dims)) if lowers is None else np.asarray(lowers, dtype=np.float64)
+    uppers = np.ones(len(dims)) if uppers is None else np.asarray(uppers, dtype=np.float64)
+    out = np.zeros((nsamples, sum(dims)))
+    di = (ctypes.c_int * len(dims))(*dims)
+    _check(load().fv_generate_sequence(len(dims), di, _p(np.ascontiguousarray(lowers)),
+                                       _p(np.ascontiguousarray(uppers)), ctypes.c_longlong(sample_start),
+                                       ctypes.c_longlong(nsamples), _p(out)))
+    return out
+
+
 def meanvar(samples):
     samples = [np.ascontiguousarray(s, dtype=np.float64) for s in samples]
     count = samples[0].size

@@ -385,6 +385,37 @@ int ref_uniform(int dimension, int sample, double lower, double upper, double* o
     }
 }
 
+// The Runner's parameter draws for samples sample_start .. sample_start +
+// nsamples - 1 (alsuq/src/run/Runner.cpp:39-52): per sample, each parameter
+// in the order given (the caller passes them in name order, as std::map
+// iterates), components ascending, through one STLMersenne per parameter on
+// the process-wide engine and Uniform(lower, upper). Valid once per process:
+// the engine is static.
+int ref_generate_sequence(int nparams, const int* dims, const double* lowers, const double* uppers,
+    long long sample_start, long long nsamples, double* out) {
+    try {
+        std::vector<std::unique_ptr<alsuq::generator::STLMersenne>> gens;
+        std::vector<std::unique_ptr<alsuq::distribution::Uniform>> dists;
+        for (int p = 0; p < nparams; ++p) {
+            gens.emplace_back(new alsuq::generator::STLMersenne(dims[p]));
+            char lo[64], hi[64];
+            std::snprintf(lo, sizeof lo, "%.17g", lowers[p]);
+            std::snprintf(hi, sizeof hi, "%.17g", uppers[p]);
+            std::map<std::string, std::string> values{{"lower", lo}, {"upper", hi}};
+            alsutils::parameters::Parameters pp(values);
+            dists.emplace_back(new alsuq::distribution::Uniform(pp));
+        }
+        long long k = 0;
+        for (long long s = sample_start; s < sample_start + nsamples; ++s)
+            for (int p = 0; p < nparams; ++p)
+                for (int c = 0; c < dims[p]; ++c) out[k++] = dists[p]->generate(*gens[p], c, (size_t)s);
+        return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
 // MeanVariance over nsamples padded states all taken at the same time
 // (alsuq/src/stats/MeanVariance.cpp:30-67 with StatisticsHelper::
 // combineStatistics on one rank). mean/var receive padded arrays.

@@ -93,6 +93,43 @@ def generator_cases():
     np.savez_compressed(os.path.join(HERE, "generator.npz"), **out)
 
 
+# (dims per parameter in name order, lowers, uppers, first sample, samples):
+# the Runner's draws on a fresh process-wide engine, as one rank sees them
+SEQUENCE_CASES = {
+    "kh40_from0": ([40], [0.0], [1.0], 0, 5),
+    "two_from0": ([3, 7], [0.0, 0.0], [1.0, 1.0], 0, 4),
+    "two_from5": ([3, 7], [0.0, 0.0], [1.0, 1.0], 5, 3),
+    "three_from2": ([10, 1, 4], [-1.0, 0.0, 2.0], [1.0, 5.0, 3.0], 2, 3),
+}
+
+
+def _sequence_case(name, path):
+    dims, lo, hi, start, n = SEQUENCE_CASES[name]
+    out = np.zeros((n, sum(dims)))
+    di = (ctypes.c_int * len(dims))(*dims)
+    check(R.ref_generate_sequence(len(dims), di, P(np.array(lo)), P(np.array(hi)), ctypes.c_longlong(start),
+                                  ctypes.c_longlong(n), P(out)))
+    np.save(path, out)
+
+
+def generator_sequence_cases():
+    import subprocess
+    import tempfile
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (dims, lo, hi, start, n) in SEQUENCE_CASES.items():
+            path = os.path.join(tmp, name + ".npy")
+            # a fresh process per case: the reference's engine is process-wide
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--sequence", name, path], check=True,
+                           timeout=300)
+            out[name] = np.load(path)
+            out[name + "_dims"] = np.array(dims)
+            out[name + "_lower"] = np.array(lo)
+            out[name + "_upper"] = np.array(hi)
+            out[name + "_start"] = np.array([start])
+    np.savez_compressed(os.path.join(HERE, "generator_sequence.npz"), **out)
+
+
 def meanvar_cases():
     rng = np.random.default_rng(7)
     n, g = (8, 6, 1), 2
@@ -127,9 +164,12 @@ def run_cases():
     np.savez_compressed(os.path.join(HERE, "runs.npz"), **out)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and len(sys.argv) == 4 and sys.argv[1] == "--sequence":
+    _sequence_case(sys.argv[2], sys.argv[3])
+elif __name__ == "__main__":
     R.ref_set_threads(4)
     generator_cases()
+    generator_sequence_cases()
     flux_cases()
     boundary_cases()
     meanvar_cases()

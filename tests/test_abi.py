@@ -38,6 +38,31 @@ def test_generator_matches_reference_fixture():
         assert np.array_equal(lib.uniform(40, s), z["uniform40_s%d" % s])
 
 
+@pytest.mark.parametrize("name", ("kh40_from0", "two_from0", "two_from5", "three_from2"))
+def test_stateful_generator_matches_reference_fixture(name):
+    """gbfv_generator driven in the Runner's order reproduces the reference's
+    parameter draws bit for bit (host code: no GPU needed)."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", "generator_sequence.npz"))
+    dims, lo, hi = z[name + "_dims"], z[name + "_lower"], z[name + "_upper"]
+    start, want = int(z[name + "_start"][0]), z[name]
+    g = lib.Generator()
+    got = []
+    for s in range(start, start + want.shape[0]):
+        row = []
+        for p, d in enumerate(dims):
+            row += [g.uniform(d, c, s, lo[p], hi[p]) for c in range(d)]
+        got.append(row)
+    g.close()
+    assert np.array_equal(np.array(got), want)
+
+
+def test_stateful_generator_rejects_bad_components():
+    g = lib.Generator()
+    with pytest.raises(lib.GbfvError):
+        g.uniform(3, 3, 0)
+    g.close()
+
+
 def test_generator_scaling():
     a = lib.uniform(10, 3, 0.0, 1.0)
     b = lib.uniform(10, 3, -2.0, 5.0)

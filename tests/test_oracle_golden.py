@@ -88,3 +88,16 @@ def test_constraint_violation_is_reported():
                                    1.4, 0.475, 1.0, 0, 5, prim, 2, 3)
     assert rc == -2
     assert steps == 1
+
+
+SEQUENCE_CASES = ("kh40_from0", "two_from0", "two_from5", "three_from2")
+
+
+@pytest.mark.parametrize("name", SEQUENCE_CASES)
+def test_generator_sequence_matches_reference(name):
+    """The Runner's stateful draws (several parameters on one engine, a rank
+    starting mid-way) from the oracle equal the reference's."""
+    z = load("generator_sequence.npz")
+    out = fvoracle.generate_sequence(z[name + "_dims"], int(z[name + "_start"][0]), z[name].shape[0],
+                                     z[name + "_lower"], z[name + "_upper"])
+    assert np.array_equal(out, z[name])
