@@ -554,8 +554,9 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
         CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         if (s->st_host->done) break;
-        // a run that stops at save times checks after every step
-        if (chunk < 64 && !P.stop_at_save) chunk *= 2;
+        // steps queued after the one that ended the advance return at once
+        // (done), leaving the state and the saved mask as that step left them
+        if (chunk < 64) chunk *= 2;
     }
     if (s->st_host->status != 0) {
         char msg[256];

@@ -1,0 +1,198 @@
+"""The UQ ensemble run of alsuqcli: sample parameters, one finite-volume run
+per sample, mean / variance statistics, written by rank 0.
+
+Follows alsuq's Setup::makeRunner and Runner::run
+(alsuq/src/config/Setup.cpp:69-126, alsuq/src/run/Runner.cpp:39-90):
+  * samples sampleStart .. sampleStart + samples - 1, split into contiguous
+    equal blocks over the ranks (SimpleLoadBalancer);
+  * per sample, ascending, the parameters in name order (std::map), each
+    component drawn through the run's one stateful generator
+    (lib.Generator: STLMersenne + Uniform, or Uniform1D's midpoints), then
+    the initial data program evaluated with them;
+  * statistics (meanvar) at the FixedIntervalStatistics save times over the
+    whole padded state, combined over ranks, written as <basename>_mean and
+    <basename>_variance.
+
+Two engines run the samples:
+  * "batch" - the ensemble engine (lib.Batch): every sample of a wave is a
+    member of one persistent launch per RK stage, each with its own dt; the
+    statistics are folded on the device as members reach the end time. Used
+    when statistics are taken once, at the end time, and no per-sample fvm
+    writer is configured.
+  * "serial" - one lib.Solver reused sample after sample with the writer and
+    statistics save clamps (any schedule).
+Both give each sample the reference's trajectory; the statistics are FP64
+Welford accumulators (population variance, as MeanVariance).
+"""
+import time
+
+import numpy as np
+
+from . import initdata, lib, uq
+from .config import ConfigError
+from .simulator import Simulator
+from .writers import NetCDFWriter, NumpyWriter
+
+
+def sample_parameters(uqc, samples, generator=None):
+    """{sample: {name: [values]}} for the given ascending samples, drawn in
+    the Runner's order on one generator."""
+    gen = generator or lib.Generator()
+    out = {}
+    for s in samples:
+        params = {}
+        for p in sorted(uqc.parameters, key=lambda q: q.name):
+            if p.type == "uniform":
+                params[p.name] = [gen.uniform(p.length, c, s, p.lower, p.upper) for c in range(p.length)]
+            elif p.type == "uniform1d":
+                if p.length != 1:
+                    raise ConfigError("With Uniform1D we only support 1 dimension")
+                params[p.name] = [p.a + (p.b - p.a) / uqc.samples * (s + 0.5)]
+            else:
+                raise ConfigError("Unknown distribution %s" % p.type)
+        out[s] = params
+    return out
+
+
+class Runner:
+    def __init__(self, config, precision=lib.FP64, rank=0, world_size=1, output_dir=".", engine="auto",
+                 hbm_budget_bytes=None):
+        if config.uq is None:
+            raise ConfigError("Missing configuration node: uq")
+        self.config = config
+        self.fvm = config.fvm
+        self.uqc = config.uq
+        self.precision = precision
+        self.rank = rank
+        self.world_size = world_size
+        self.output_dir = output_dir
+        self.hbm_budget = hbm_budget_bytes
+        s0, s1 = uq.sample_blocks(self.uqc.samples, world_size)[rank]
+        self.samples = list(range(self.uqc.sample_start + s0, self.uqc.sample_start + s1))
+        stats = self.uqc.stats
+        intervals = {st.save_interval(self.fvm.end_time) for st in stats}
+        if len(intervals) > 1:
+            raise ConfigError("statistics with different numberOfSaves in one run are not supported")
+        self.stats_interval = intervals.pop() if intervals else 0.0
+        self.stats_saves = stats[0].number_of_saves if stats else 0
+        self.stats_initial = bool(stats and stats[0].write_initial_timestep)
+        batch_ok = (self.fvm.writer is None and self.stats_saves <= 1 and not self.stats_initial
+                    and self.fvm.integrator in ("rungekutta2", "rungekutta3"))
+        if engine == "auto":
+            engine = "batch" if batch_ok else "serial"
+        if engine == "batch" and not batch_ok:
+            raise ConfigError("the batch engine needs rungekutta2/3, statistics at the end time only and no fvm "
+                              "writer; use the serial engine")
+        self.engine = engine
+        self.timesteps = 0
+        self.wall_s = 0.0
+
+    def _prim(self, params):
+        p = dict(self.fvm.init_parameters)
+        p.update(params)
+        return initdata.evaluate(self.fvm.python_program, self.fvm.equation, self.fvm.lower, self.fvm.upper,
+                                 self.fvm.dimension, p)
+
+    def run(self):
+        """Runs this rank's samples; returns (count, mean, variance) per
+        statistics save as padded states (nvar, total), identical on every
+        rank, and writes the statistics files on rank 0."""
+        t0 = time.perf_counter()
+        params = sample_parameters(self.uqc, self.samples)
+        if self.engine == "batch":
+            triples = self._run_batch(params)
+        else:
+            triples = self._run_serial(params)
+        results = [uq.combine_statistics(*t) for t in triples]
+        self.wall_s = time.perf_counter() - t0
+        if self.rank == 0:
+            self._write_statistics(results)
+        return results
+
+    # -- engines -----------------------------------------------------------
+
+    def _run_serial(self, params):
+        acc = None
+        sim = Simulator(self.fvm, self.precision, num_samples=self.uqc.samples, output_dir=self.output_dir,
+                        statistics_interval=self.stats_interval, statistics_initial=self.stats_initial)
+        nstat = self.stats_saves + (1 if self.stats_initial else 0)
+        count = sim.solver.nvar * sim.solver.total
+        acc = [lib.Stats(count) for _ in range(nstat)]
+
+        def on_statistics(s, k):
+            acc[k].add_device(s.solver.state_device(), self.precision if self.precision == lib.FP32 else lib.FP64)
+
+        sim.on_statistics = on_statistics
+        try:
+            for s in self.samples:
+                sim.sample = s
+                sim.set_initial_value(self._prim(params[s]))
+                sim.call_writers()
+                sim.run()
+                self.timesteps += sim.get_number_of_timesteps()
+            sim.finalize()
+            triples = [a.export() for a in acc]
+        finally:
+            for a in acc:
+                a.close()
+            sim.close()
+        return triples
+
+    def _run_batch(self, params):
+        f = self.fvm
+        b = lib.Batch(f.equation, f.flux, f.reconstruction, f.integrator, f.boundary, 1 << 20, 1, gamma=f.gamma,
+                      cfl=f.cfl, precision=self.precision)
+        per = b.member_bytes(f.dimension)
+        b.close()
+        budget = self.hbm_budget
+        if budget is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            budget = int(free * 0.8)
+        wave = max(1, min(len(self.samples), int(budget // per)))
+        pool = wave * per + (16 << 20)
+        b = lib.Batch(f.equation, f.flux, f.reconstruction, f.integrator, f.boundary, pool, wave, gamma=f.gamma,
+                      cfl=f.cfl, precision=self.precision)
+        total = None
+        try:
+            for i in range(0, len(self.samples), wave):
+                chunk = self.samples[i:i + wave]
+                slots = [b.add(f.dimension, f.lower, f.upper, self._prim(params[s]), group=0) for s in chunk]
+                b.advance(f.end_time, 1, 0)
+                for sl in slots:
+                    self.timesteps += b.member_time(sl)[1]
+                    b.remove(sl)
+            nv = lib.num_variables(f.equation)
+            g = lib.ghost_cells(f.reconstruction)
+            dim = f.dim
+            total = int(np.prod([f.dimension[d] + 2 * g if d < dim else f.dimension[d] for d in range(3)]))
+            if self.samples:
+                n, m, q = b.stats_export(0, total)
+            else:
+                n, m, q = 0, np.zeros((nv, total)), np.zeros((nv, total))
+        finally:
+            b.close()
+        return [(n, m.reshape(-1), q.reshape(-1))]
+
+    # -- output ------------------------------------------------------------
+
+    def _write_statistics(self, results):
+        if not self.uqc.stats:
+            return
+        f = self.fvm
+        nv = lib.num_variables(f.equation)
+        g = lib.ghost_cells(f.reconstruction)
+        from .simulator import interior
+        for st in self.uqc.stats:
+            w = st.writer
+            for kind, idx in (("mean", 1), ("variance", 2)):
+                base = "%s_%s" % (w.basename, kind)
+                if w.type == "netcdf":
+                    writer = NetCDFWriter("%s/%s" % (self.output_dir, base), f.equation, f.lower, f.upper,
+                                          f.dimension, 1, w.save_fractions())
+                else:
+                    writer = NumpyWriter("%s/%s" % (self.output_dir, base), f.equation)
+                for k, res in enumerate(results):
+                    U = np.asarray(res[idx]).reshape(nv, -1)
+                    writer.write(interior(U, f.dimension, g), 0, k)
+                writer.finalize()

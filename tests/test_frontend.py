@@ -1,0 +1,175 @@
+"""The XML / Python front end on the CPU: configuration reading with the
+reference's defaults and errors, initial data programs in both forms, the
+Runner's parameter draws against the oracle's restatement of the reference
+generator, the sample split, and the NetCDF writer read back by scipy."""
+import os
+
+import numpy as np
+import pytest
+
+from alsvinn_gb300 import config, initdata, lib, runner, writers
+from oracle import fvoracle
+
+INPUTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "inputs")
+
+
+def _xml(tmp_path, text, py="rho = 1.0\nux = 0.0\np = 1.0\n", pyname="init.py"):
+    (tmp_path / pyname).write_text(py)
+    p = tmp_path / "run.xml"
+    p.write_text(text)
+    return str(p)
+
+
+BASE = """<config><fvm>
+  <name> t </name><platform>{platform}</platform>
+  <grid><lowerCorner>0 0 0</lowerCorner><upperCorner>1 0 0</upperCorner><dimension>16 1 1</dimension></grid>
+  <boundary>{boundary}</boundary><flux>hll3</flux><endTime>0.1</endTime><equation>euler1</equation>
+  <reconstruction>{recon}</reconstruction><cfl>{cfl}</cfl><integrator>{integrator}</integrator>
+  <initialData><python>init.py</python></initialData>{extra}
+</fvm>{uq}</config>"""
+
+
+def base(**kw):
+    d = dict(platform="gb300", boundary="periodic", recon="weno2", cfl="auto", integrator="auto", extra="", uq="")
+    d.update(kw)
+    return BASE.format(**d)
+
+
+def test_reads_the_sod_input():
+    cfg = config.read_config(os.path.join(INPUTS, "sod.xml"))
+    f = cfg.fvm
+    assert (f.name, f.equation, f.flux, f.reconstruction, f.integrator, f.boundary) == \
+        ("sod", "euler1", "hll3", "weno2", "rungekutta3", "neumann")
+    assert f.cfl == 0.475 and f.gamma == 1.4 and f.end_time == 0.5
+    assert f.lower == (-5.0, 0.0, 0.0) and f.dimension == (128, 1, 1)
+    assert f.writer.type == "netcdf" and f.writer.number_of_saves == 3
+    assert f.save_interval() == 0.5 / 3
+    assert cfg.uq is None
+
+
+def test_auto_cfl_and_integrator_follow_the_reconstruction(tmp_path):
+    f = config.read_config(_xml(tmp_path, base(recon="none"))).fvm
+    assert (f.cfl, f.integrator) == (0.9, "forwardeuler")
+    f = config.read_config(_xml(tmp_path, base(recon="eno3"))).fvm
+    assert (f.cfl, f.integrator) == (0.475, "rungekutta2")
+    f = config.read_config(_xml(tmp_path, base(cfl="0.3", integrator="rungekutta3"))).fvm
+    assert (f.cfl, f.integrator) == (0.3, "rungekutta3")
+    assert f.name == "t"
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(extra="<bogus>1</bogus>"), "Unsupported configuration option bogus"),
+    (dict(boundary="reflective"), "Unknown boundary conditions"),
+    (dict(platform="rocm"), "Unknown platform"),
+    (dict(extra="<diffusion><name>tecno1</name><reconstruction>none</reconstruction></diffusion>"), "Diffusion"),
+])
+def test_rejects_what_the_reference_rejects(tmp_path, kw, msg):
+    with pytest.raises(config.ConfigError, match=msg):
+        config.read_config(_xml(tmp_path, base(**kw)))
+
+
+def test_uq_section_and_its_errors(tmp_path):
+    cfg = config.read_config(os.path.join(INPUTS, "kh_uq.xml"))
+    u = cfg.uq
+    assert (u.samples, u.sample_start, u.generator) == (4, 0, "stlmersenne")
+    assert [(p.name, p.length, p.type) for p in u.parameters] == [("a", 40, "uniform")]
+    assert u.stats[0].name == "meanvar" and u.stats[0].number_of_saves == 1
+    assert cfg.fvm.init_parameters["a"] == [0.0] * 40 and cfg.fvm.init_parameters["gamma"] == [1.4]
+    normal = "<uq><samples>2</samples><generator>auto</generator><parameters><parameter><name>a</name>" \
+             "<length>1</length><type>normal</type></parameter></parameters><stats/></uq>"
+    with pytest.raises(config.ConfigError, match="Normal variables are not supported"):
+        config.read_config(_xml(tmp_path, base(uq=normal)))
+
+
+def test_distribution_bounds_are_the_references_defaults(tmp_path):
+    # lower / upper in the XML are overwritten by Setup::makeSampleGenerator
+    uqx = "<uq><samples>2</samples><generator>auto</generator><parameters><parameter><name>a</name>" \
+          "<length>3</length><type>uniform</type><lower>5</lower><upper>6</upper></parameter></parameters>" \
+          "<stats/></uq>"
+    p = config.read_config(_xml(tmp_path, base(uq=uqx))).uq.parameters[0]
+    assert (p.lower, p.upper) == (0.0, 1.0)
+
+
+def test_snippet_and_global_initial_data_agree():
+    cfg = config.read_config(os.path.join(INPUTS, "sod.xml"))
+    f = cfg.fvm
+    snip = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, f.init_parameters)
+    glob = initdata.evaluate(open(os.path.join(INPUTS, "sod_global.py")).read(), f.equation, f.lower, f.upper,
+                             f.dimension, f.init_parameters)
+    assert snip.shape == (3, 1, 1, 128)
+    assert np.array_equal(snip, glob)
+    assert np.array_equal(snip.reshape(3, -1), lib.init_sod(128, lower=f.lower, upper=f.upper))
+
+
+def test_kelvin_helmholtz_program_matches_the_native_initial_data():
+    cfg = config.read_config(os.path.join(INPUTS, "kh_uq.xml"))
+    f = cfg.fvm
+    X = lib.uniform(40, 3)
+    prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, {"a": list(X)})
+    native = lib.init_kelvin_helmholtz(32, X=X)
+    # the interface test may flip only where cos rounds differently in the
+    # last bit right at a cell midpoint; none does here
+    assert np.array_equal(prim.reshape(4, -1), native.reshape(4, -1))
+
+
+def test_initial_data_errors_are_reported():
+    with pytest.raises(initdata.InitialDataError, match="NameError"):
+        initdata.evaluate("rho = undefined_name\n", "euler1", (0, 0, 0), (1, 0, 0), (4, 1, 1))
+
+
+def test_midpoints_follow_the_grid():
+    xs, ys, zs = initdata.cell_midpoints((-5.0, 0.0, 0.0), (5.0, 0.0, 0.0), (4, 1, 1))
+    assert xs == [-5.0 + 2.5 * i + 1.25 for i in range(4)]
+    assert ys == [0.5] and zs == [0.5]
+
+
+def test_runner_draws_follow_the_reference_generator():
+    """Two parameters in name order on one engine, a rank starting at sample 3."""
+    uqc = config.UQConfig(samples=8, sample_start=0, generator="stlmersenne",
+                          parameters=[config.UQParameter("zeta", 2, "uniform"), config.UQParameter("alpha", 5, "uniform")])
+    got = runner.sample_parameters(uqc, range(3, 7))
+    want = fvoracle.generate_sequence([5, 2], 3, 4)  # alpha (5) before zeta (2)
+    for i, s in enumerate(range(3, 7)):
+        assert np.array_equal(np.array(got[s]["alpha"] + got[s]["zeta"]), want[i])
+
+
+def test_uniform1d_uses_midpoints_without_draws():
+    uqc = config.UQConfig(samples=4, sample_start=0, generator="stlmersenne",
+                          parameters=[config.UQParameter("s", 1, "uniform1d")])
+    got = runner.sample_parameters(uqc, range(4))
+    assert [got[s]["s"][0] for s in range(4)] == [0.0 + 1.0 / 4 * (s + 0.5) for s in range(4)]
+
+
+def test_netcdf_writer_round_trip(tmp_path):
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    n = (6, 5, 1)
+    w = writers.NetCDFWriter(str(tmp_path / "out.nc"), "euler2", (0, 0, 0), (1, 1, 0), n, 3, [0.5, 1.0])
+    rng = np.random.default_rng(1)
+    states = {(m, k): rng.uniform(size=(4, 1, 5, 6)) for m in range(3) for k in range(2)}
+    for (m, k), U in states.items():
+        w.write(U, m, k)
+    with netcdf(str(tmp_path / "out.nc"), "r", mmap=False) as f:
+        assert f.dimensions == {"member": 3, "time": 2, "x": 6, "y": 5}
+        assert list(f.variables["member"][:]) == [0, 1, 2]
+        assert list(f.variables["time"][:]) == [0.5, 1.0]
+        np.testing.assert_array_equal(f.variables["x"][:], [(1 / 6) * i + (1 / 6) / 2.0 for i in range(6)])
+        for (m, k), U in states.items():
+            # the x-fastest buffer of each variable lands in the slab as is
+            for name, var in (("rho", 0), ("mx", 1), ("my", 2), ("E", 3)):
+                assert f.variables[name].shape == (3, 2, 6, 5)
+                np.testing.assert_array_equal(f.variables[name][m, k].reshape(-1), U[var].reshape(-1))
+
+
+def test_numpy_writer(tmp_path):
+    w = writers.NumpyWriter(str(tmp_path / "o"), "burgers")
+    U = np.arange(8.0).reshape(1, 1, 1, 8)
+    w.write(U, 2, 1, time=0.25)
+    z = np.load(str(tmp_path / "o_2_1.npz"))
+    assert np.array_equal(z["u"], U[0]) and z["time"][0] == 0.25
+
+
+def test_cli_reports_configuration_errors(tmp_path, capsys):
+    from alsvinn_gb300 import alsvinncli
+    rc = alsvinncli.main([_xml(tmp_path, base(boundary="reflective"))])
+    assert rc == 1
+    assert "Unknown boundary conditions" in capsys.readouterr().err

@@ -1,0 +1,140 @@
+"""The XML front end end to end on the GPU: alsvinncli and alsuqcli inputs run
+through config -> initial data -> Simulator / Runner -> writers, compared
+with the oracle run on the same initial data (bit for bit with the exact
+arithmetic variant; the statistics within the Welford-versus-sums rounding)."""
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import workloads
+from alsvinn_gb300 import alsuqcli, alsvinncli, config, initdata, lib, runner
+from alsvinn_gb300.simulator import interior
+from oracle import fvoracle
+
+pytestmark = pytest.mark.gpu
+
+INPUTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "inputs")
+
+
+def _copy_inputs(tmp_path, names):
+    for n in names:
+        shutil.copy(os.path.join(INPUTS, n), str(tmp_path / n))
+
+
+def _oracle_run(f, prim, end_time, saves):
+    g = lib.ghost_cells(f.reconstruction)
+    rc, U, t, steps = fvoracle.run(f.equation, f.flux, f.reconstruction, f.integrator, f.boundary, f.dimension,
+                                   f.lower, f.upper, f.gamma, f.cfl, end_time, saves, 0,
+                                   prim.reshape(prim.shape[0], -1), g, workloads.NVAR[f.equation])
+    assert rc == 0
+    return U, t, steps
+
+
+def test_alsvinncli_sod_matches_the_oracle_at_every_save(cuda_device, tmp_path):
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    _copy_inputs(tmp_path, ["sod.xml", "sod.py"])
+    xml = str(tmp_path / "sod.xml")
+    assert alsvinncli.main([xml, "--precision", "fp64-exact"]) == 0
+    f = config.read_config(xml).fvm
+    prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, f.init_parameters)
+    g = lib.ghost_cells(f.reconstruction)
+    interval = f.end_time / f.writer.number_of_saves
+    with netcdf(str(tmp_path / "sod_out.nc"), "r", mmap=False) as nc:
+        rho, mx, E = (np.array(nc.variables[v][0]) for v in ("rho", "mx", "E"))
+    for k in range(1, f.writer.number_of_saves + 1):
+        # the writer's trajectory up to save k is the oracle's with k saves to k * interval
+        end = f.end_time if k == f.writer.number_of_saves else k * interval
+        U, t, steps = _oracle_run(f, prim, end, k)
+        want = interior(U, f.dimension, g)
+        got = np.stack([rho[k - 1], mx[k - 1], E[k - 1]]).reshape(want.shape)
+        assert np.array_equal(got, want), k
+
+
+def test_simulator_steps_like_the_reference_loop(cuda_device, tmp_path):
+    """perform_step one step at a time and run() give the same state."""
+    from alsvinn_gb300.simulator import Simulator
+    _copy_inputs(tmp_path, ["sod.xml", "sod.py"])
+    f = config.read_config(str(tmp_path / "sod.xml")).fvm
+    f.writer = None
+    prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension)
+    a = Simulator(f, lib.FP64_EXACT)
+    b = Simulator(f, lib.FP64_EXACT)
+    a.set_initial_value(prim)
+    b.set_initial_value(prim)
+    n = 0
+    while not a.at_end():
+        a.perform_step()
+        n += 1
+    b.run()
+    assert n == a.get_number_of_timesteps() == b.get_number_of_timesteps()
+    assert a.get_current_time() == b.get_current_time() >= f.end_time
+    assert np.array_equal(a.solver.get_state(), b.solver.get_state())
+    a.close()
+    b.close()
+
+
+def _uq_expected(cfg, end_time, saves):
+    f, u = cfg.fvm, cfg.uq
+    draws = runner.sample_parameters(u, range(u.sample_start, u.sample_start + u.samples))
+    states = []
+    for s in sorted(draws):
+        p = dict(f.init_parameters)
+        p.update(draws[s])
+        prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, p)
+        states.append(_oracle_run(f, prim, end_time, saves)[0])
+    return fvoracle.meanvar(states)
+
+
+def _check_stats(res, m_ref, v_ref, count):
+    n, mean, var = res
+    assert n == count
+    mean = mean.reshape(m_ref.shape)
+    var = var.reshape(v_ref.shape)
+    np.testing.assert_allclose(mean, m_ref, rtol=1e-13, atol=1e-15)
+    # Welford M2 / n against the reference's sum(u^2)/n - mean^2
+    scale = np.abs(m_ref).max(axis=1, keepdims=True) ** 2
+    assert (np.abs(var - v_ref) / scale).max() < 1e-12
+
+
+@pytest.mark.parametrize("engine", ["serial", "batch"])
+def test_alsuq_statistics_match_the_oracle(cuda_device, tmp_path, engine):
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
+    xml = str(tmp_path / "kh_uq.xml")
+    cfg = config.read_config(xml)
+    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path), engine=engine)
+    results = r.run()
+    assert r.engine == engine and len(results) == 1
+    m_ref, v_ref = _uq_expected(cfg, cfg.fvm.end_time, 1)
+    _check_stats(results[0], m_ref, v_ref, cfg.uq.samples)
+    with netcdf(str(tmp_path / "kh_uq_stats_mean"), "r", mmap=False) as nc:
+        g = lib.ghost_cells(cfg.fvm.reconstruction)
+        want = interior(m_ref, cfg.fvm.dimension, g)
+        got = np.stack([np.array(nc.variables[v][0, 0]) for v in ("rho", "mx", "my", "E")]).reshape(want.shape)
+        np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-15)
+
+
+def test_alsuq_statistics_at_several_save_times(cuda_device, tmp_path):
+    _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
+    xml = str(tmp_path / "kh_uq.xml")
+    text = open(xml).read().replace("<numberOfSaves>1</numberOfSaves>", "<numberOfSaves>2</numberOfSaves>")
+    open(xml, "w").write(text)
+    cfg = config.read_config(xml)
+    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path))
+    assert r.engine == "serial"
+    results = r.run()
+    assert len(results) == 2
+    T = cfg.fvm.end_time
+    for k, (end, saves) in enumerate(((T / 2, 1), (T, 2))):
+        m_ref, v_ref = _uq_expected(cfg, end, saves)
+        _check_stats(results[k], m_ref, v_ref, cfg.uq.samples)
+
+
+def test_alsuqcli_runs_the_input(cuda_device, tmp_path, capsys):
+    _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
+    assert alsuqcli.main([str(tmp_path / "kh_uq.xml"), "--precision", "fp32"]) == 0
+    out = capsys.readouterr().out
+    assert '"engine": "batch"' in out
+    assert os.path.exists(str(tmp_path / "kh_uq_stats_variance"))
