@@ -20,6 +20,7 @@ namespace gbfv {
 
 // keep the float / double overloads visible next to the double-float ones
 using ::fabs;
+using ::fma;
 using ::fmax;
 using ::fmin;
 using ::sqrt;
@@ -180,5 +181,6 @@ __device__ __forceinline__ dfloat fmin(const dfloat& a, const dfloat& b) {
     return b < a ? b : a;
 }
 __device__ __forceinline__ bool isfinite(const dfloat& a) { return isfinite(a.hi); }
+__device__ __forceinline__ dfloat fma(const dfloat& a, const dfloat& b, const dfloat& c) { return a * b + c; }
 
 }  // namespace gbfv

@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "fv_types.h"
 
 // Kernel code is compiled once per arithmetic variant; each variant's
@@ -39,35 +41,92 @@ template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return rsq
 template <class R> __device__ __forceinline__ R rcp_(R x) { return R(1) / x; }
 
 // FP64 reciprocal and reciprocal square root for the fast policy: a hardware
-// approximation (PTX rcp.approx / rsqrt.approx .f64) refined by two
-// Newton-Raphson steps, y <- y (2 - x y) and y <- y (3 - x y^2) / 2, each of
-// which doubles the number of correct bits; the result is within about an ulp
-// of the correctly rounded value, in fewer FP64 instructions than an IEEE
-// division or square root.
+// approximation (PTX rcp.approx / rsqrt.approx .f64) refined by one step of a
+// third-order iteration, which triples the number of correct bits:
+//   reciprocal:  e = 1 - x y,    y' = y (1 + e + e^2)             (error e^3)
+//   rsqrt:       d = 1 - x y^2,  y' = y (1 + d/2 + 3 d^2 / 8)     (error ~5 d^3 / 16)
+// (truncated binomial series of (1 - e)^-1 and (1 - d)^-1/2, the
+// Householder-type corrections of the Newton-Raphson family). The results
+// are within about an ulp of the correctly rounded values
+// (tests/cpp/test_special_functions.cu measures the ulp error against CUDA's
+// IEEE division and sqrt), in fewer FP64 instructions than an IEEE division
+// or square root.
 template <> __device__ __forceinline__ double rcp_<double>(double x) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
 }
 
 __device__ __forceinline__ double rsqrt_nr(double x) {
     double y;
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    const double h = 0.5 * x;
-    double t = fma(-h * y, y, 0.5);
-    y = fma(y, t, y);
-    t = fma(-h * y, y, 0.5);
-    return fma(y, t, y);
+    const double d = fma(-x * y, y, 1.0);
+    return fma(y * d, fma(d, 0.375, 0.5), y);
+}
+
+// Tests on a double's bit pattern, evaluated on the integer pipes: GB300
+// executes FP64 compares and minima / maxima at the FP64 rate (1/64 of the
+// FP32 rate), which makes them as costly as an FMA in this FP64-bound kernel.
+// Each helper returns what the IEEE operation returns, NaN cases included.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+constexpr long long kInfBits = 0x7ff0000000000000LL;
+constexpr long long kAbsMask = 0x7fffffffffffffffLL;
+
+// 0 < x < 1e300 (a positive finite value whose reciprocal square root stays
+// normal): one unsigned compare of bits - 1 against the bits of 1e300 - 1
+__device__ __forceinline__ bool in_rsqrt_range(double x) {
+    return (unsigned long long)(dbits(x) - 1) < (unsigned long long)(0x7e37e43c8800759cLL - 1);
+}
+
+template <class R> __device__ __forceinline__ bool gt0(R x) { return x > R(0); }
+template <class R> __device__ __forceinline__ bool lt0(R x) { return x < R(0); }
+template <class R> __device__ __forceinline__ bool ge0(R x) { return x >= R(0); }
+template <class R> __device__ __forceinline__ bool is0(R x) { return x == R(0); }
+template <class R> __device__ __forceinline__ R fmin_(R a, R b) { return fmin(a, b); }
+template <class R> __device__ __forceinline__ R fmax_(R a, R b) { return fmax(a, b); }
+
+template <> __device__ __forceinline__ bool gt0<double>(double x) {
+    if (kExact) return x > 0.0;
+    const long long b = dbits(x);
+    return b > 0 && b <= kInfBits;
+}
+template <> __device__ __forceinline__ bool lt0<double>(double x) {
+    if (kExact) return x < 0.0;
+    const long long b = dbits(x), m = b & kAbsMask;
+    return b < 0 && m != 0 && m <= kInfBits;
+}
+template <> __device__ __forceinline__ bool ge0<double>(double x) {
+    if (kExact) return x >= 0.0;
+    const long long b = dbits(x);
+    return b >= 0 ? b <= kInfBits : (b & kAbsMask) == 0;
+}
+template <> __device__ __forceinline__ bool is0<double>(double x) {
+    if (kExact) return x == 0.0;
+    return (dbits(x) & kAbsMask) == 0;
+}
+// total order of the non-NaN doubles as signed integers (-0 just below +0)
+__device__ __forceinline__ long long order_key(long long b) { return b ^ ((b >> 63) & kAbsMask); }
+template <> __device__ __forceinline__ double fmin_<double>(double a, double b) {
+    if (kExact) return fmin(a, b);
+    const long long x = dbits(a), y = dbits(b);
+    if ((x & kAbsMask) > kInfBits) return b;
+    if ((y & kAbsMask) > kInfBits) return a;
+    return order_key(x) <= order_key(y) ? a : b;
+}
+template <> __device__ __forceinline__ double fmax_<double>(double a, double b) {
+    if (kExact) return fmax(a, b);
+    const long long x = dbits(a), y = dbits(b);
+    if ((x & kAbsMask) > kInfBits) return b;
+    if ((y & kAbsMask) > kInfBits) return a;
+    return order_key(x) >= order_key(y) ? a : b;
 }
 
 // sqrt(x) = x / sqrt(x) for positive finite x; zero, negative and NaN
 // arguments take the IEEE square root
 template <class R> __device__ __forceinline__ R sqrt_(R x) { return sqrt(x); }
 template <> __device__ __forceinline__ double sqrt_<double>(double x) {
-    return (x > 0.0 && x < 1e300) ? x * rsqrt_nr(x) : sqrt(x);
+    return in_rsqrt_range(x) ? x * rsqrt_nr(x) : sqrt(x);
 }
 
 // 1/rho and sqrt(rho) of a density: one reciprocal square root for FP64
@@ -76,7 +135,7 @@ template <class R> __device__ __forceinline__ void inv_sqrt_pair(R rho, R& rinv,
     w = sqrt(rho);
 }
 template <> __device__ __forceinline__ void inv_sqrt_pair<double>(double rho, double& rinv, double& w) {
-    if (rho > 0.0 && rho < 1e300) {
+    if (in_rsqrt_range(rho)) {
         const double rs = rsqrt_nr(rho);
         rinv = rs * rs;
         w = rho * rs;
@@ -98,19 +157,23 @@ template <class R, int NSD> struct EulerState {
 
 template <class R, int NSD>
 __device__ __forceinline__ void euler_extra(EulerState<R, NSD>& a, R gamma) {
-    R dot = a.m[0] * a.m[0];
-#pragma unroll
-    for (int k = 1; k < NSD; ++k) dot = dot + a.m[k] * a.m[k];
     if (kExact) {
+        R dot = a.m[0] * a.m[0];
+#pragma unroll
+        for (int k = 1; k < NSD; ++k) dot = dot + a.m[k] * a.m[k];
         const R ie = a.E - R(0.5) * dot / a.rho;
 #pragma unroll
         for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] / a.rho;
         a.p = (gamma - R(1)) * ie;
     } else {
+        // m.m / rho as m.u: the velocities are needed anyway
         inv_sqrt_pair(a.rho, a.rinv, a.w);
 #pragma unroll
         for (int k = 0; k < NSD; ++k) a.u[k] = a.m[k] * a.rinv;
-        a.p = (gamma - R(1)) * (a.E - R(0.5) * dot * a.rinv);
+        R mu = a.m[0] * a.u[0];
+#pragma unroll
+        for (int k = 1; k < NSD; ++k) mu = fma(a.m[k], a.u[k], mu);
+        a.p = (gamma - R(1)) * fma(R(-0.5), mu, a.E);
     }
 }
 
@@ -161,10 +224,10 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
         const R p = (waveLeft * L.p + waveRight * Rs.p) * winv;
         const R cfLeft = sqrt_(gamma * L.p * L.rinv);
         const R cfRight = sqrt_(gamma * Rs.p * Rs.rinv);
-        const R correct = R(0.5) * fmax(R(0), L.u[D] - Rs.u[D]);
+        const R correct = R(0.5) * fmax_(R(0), L.u[D] - Rs.u[D]);
         const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
-        speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
-        speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
+        speedLeft = fmin_(L.u[D] + correct - cfLeft, ud - cs);
+        speedRight = fmax_(Rs.u[D] - correct + cfRight, ud + cs);
     }
     R fluxLeft[NV], fluxRight[NV];
     euler_point_flux<R, NSD, D>(L, fluxLeft);
@@ -175,18 +238,18 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
     const R ainv = kExact ? R(0) : rcp_(aa);
     const R sm = kExact ? (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) / aa
                         : (Rs.m[D] * udr - L.m[D] * udl + Rs.p - L.p) * ainv;
-    if (speedLeft == R(0)) {
+    if (is0(speedLeft)) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = R(0);
-    } else if (speedLeft > R(0)) {
+    } else if (gt0(speedLeft)) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = fluxLeft[k];
-    } else if (speedRight < R(0)) {
+    } else if (lt0(speedRight)) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = fluxRight[k];
     } else {
         // Star state on the side of the contact speed sm.
-        const bool leftSide = sm >= R(0);
+        const bool leftSide = ge0(sm);
         const EulerState<R, NSD>& S = leftSide ? L : Rs;
         const R s = leftSide ? speedLeft : speedRight;
         const R ud = leftSide ? udl : udr;
@@ -220,7 +283,7 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = fS[k] + s * (mid[k] - c[k]);
     }
-    return fmax(fabs(speedLeft), fabs(speedRight));
+    return fmax_(fabs(speedLeft), fabs(speedRight));
 }
 
 // HLL flux (alsfvm/include/alsfvm/numflux/euler/HLL.hpp:51-115).
@@ -243,15 +306,15 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
         const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
         const R p = (L.p * waveLeft + Rs.p * waveRight) * winv;
         const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
-        speedLeft = fmin(L.u[D] - sqrt_(gamma * L.p * L.rinv), ud - cs);
-        speedRight = fmax(Rs.u[D] + sqrt_(gamma * Rs.p * Rs.rinv), ud + cs);
+        speedLeft = fmin_(L.u[D] - sqrt_(gamma * L.p * L.rinv), ud - cs);
+        speedRight = fmax_(Rs.u[D] + sqrt_(gamma * Rs.p * Rs.rinv), ud + cs);
     }
-    if (speedLeft == R(0)) {
+    if (is0(speedLeft)) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) F[k] = R(0);
-    } else if (speedLeft > R(0)) {
+    } else if (gt0(speedLeft)) {
         euler_point_flux<R, NSD, D>(L, F);
-    } else if (speedRight < R(0)) {
+    } else if (lt0(speedRight)) {
         euler_point_flux<R, NSD, D>(Rs, F);
     } else {
         R fl[NV], fr[NV], cl[NV], cr[NV];
@@ -272,17 +335,17 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
                 F[k] = (speedRight * fl[k] - speedLeft * fr[k] + srl * (cr[k] - cl[k])) * inv;
         }
     }
-    return fmax(fabs(speedLeft), fabs(speedRight));
+    return fmax_(fabs(speedLeft), fabs(speedRight));
 }
 
 // Godunov flux for Burgers: F = max(f(max(uL,0)), f(min(uR,0))), f = u^2/2,
 // wave speed max(|uL|,|uR|) (alsfvm/include/alsfvm/numflux/burgers/Godunov.hpp:40-60).
 template <class R>
 __device__ __forceinline__ R flux_godunov(R uL, R uR, R* F) {
-    const R a = fmax(uL, R(0));
-    const R b = fmin(uR, R(0));
-    F[0] = fmax(a * a / R(2), b * b / R(2));
-    return fmax(fabs(uL), fabs(uR));
+    const R a = fmax_(uL, R(0));
+    const R b = fmin_(uR, R(0));
+    F[0] = fmax_(a * a / R(2), b * b / R(2));
+    return fmax_(fabs(uL), fabs(uR));
 }
 
 // ------------------------------------------------------- reconstruction
@@ -325,6 +388,15 @@ template <> struct EnoC<4> {
     }
 };
 
+// |a| < |b| (false if either is NaN): on the magnitude bits for doubles in
+// the fast policy
+template <class R> __device__ __forceinline__ bool abs_less(R a, R b) { return fabs(a) < fabs(b); }
+template <> __device__ __forceinline__ bool abs_less<double>(double a, double b) {
+    if (kExact) return fabs(a) < fabs(b);
+    const long long x = dbits(a) & kAbsMask, y = dbits(b) & kAbsMask;
+    return x < y && y <= kInfBits;
+}
+
 #define FV_WENO_EPSILON 1e-8  // alsfvm/include/alsfvm/reconstruction/WENOCoefficients.hpp:21
 
 // Reconstructs the values of one cell at its left (i-1/2) and right (i+1/2)
@@ -364,6 +436,22 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
             const R s1 = (eps + b1) * (eps + b1);
             const R iL = rcp_(s1 + R(2) * s0);
             const R iR = rcp_(R(2) * s1 + s0);
+            if constexpr (std::is_same<R, double>::value || std::is_same<R, float>::value) {
+                // half weights and hardware FMAs: with w0 + w1 = 1,
+                // left = u_i - (w1/2)(u_i - u_{i-1}) - (w0/2)(u_{i+1} - u_i),
+                // right = u_i + (w0/2)(u_{i+1} - u_i) + (w1/2)(u_i - u_{i-1})
+                const R h0L = R(0.5) * s1 * iL, h1L = s0 * iL;
+                const R h0R = s1 * iR, h1R = R(0.5) * s0 * iR;
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const R* v = u + k * vs;
+                    const R uc = v[0];
+                    const R dp = v[ds] - uc, dm = uc - v[-ds];
+                    left[k] = fma(-h1L, dm, fma(-h0L, dp, uc));
+                    right[k] = fma(h0R, dp, fma(h1R, dm, uc));
+                }
+                return;
+            }
             w0Left = s1 * iL;
             w1Left = R(2) * s0 * iL;
             w0Right = R(2) * s1 * iR;
@@ -392,7 +480,7 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
         constexpr int c = ORDER - 1;
 #pragma unroll
         for (int l = 0; l < ORDER - 1; ++l) {
-            if (fabs(dd[c - 1]) < fabs(dd[c])) shift++;
+            if (abs_less(dd[c - 1], dd[c])) shift++;
             if (l + 1 < ORDER - 1) {
 #pragma unroll
                 for (int j = 0; j < W - 2 - l; ++j) dd[j] = dd[j + 1] - dd[j];

@@ -94,7 +94,7 @@ template <class R, int EQ, int FLUX> struct Physics {
             for (int k = 0; k < NSD; ++k) s.m[k] = c[1 + k];
             s.E = c[1 + NSD];
             euler_extra<R, NSD>(s, gamma);
-            bool ok = isfinite(s.rho) && isfinite(s.E) && isfinite(s.p) && s.rho > R(0) && s.p > R(0);
+            bool ok = isfinite(s.rho) && isfinite(s.E) && isfinite(s.p) && gt0(s.rho) && gt0(s.p);
 #pragma unroll
             for (int k = 0; k < NSD; ++k) ok = ok && isfinite(s.m[k]) && isfinite(s.u[k]);
             return ok;
@@ -128,13 +128,13 @@ struct SmemLayout {
 
 
 // One direction D of the tile: reconstruct, face fluxes, accumulate into acc.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int D>
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, int D>
 __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc, R* acc, int tid,
                                                const int* org, const Grid& G, R gamma, R& wsmax) {
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
-    constexpr int NT = TX * TY * TZ;
+    constexpr int NT = TX * TY * TZ;  // cells of the tile (NTH threads >= NT)
     constexpr int TD = D == 0 ? TX : (D == 1 ? TY : TZ);
     constexpr int O1 = D == 0 ? TY : TX;          // extent of the first other dimension
     constexpr int LEN = TD + 2;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     constexpr int VS = SL::HALO;
 
     // reconstruction of cells -1 .. TD along D
-    for (int w = tid; w < NREC; w += NT) {
+    for (int w = tid; w < NREC; w += NTH) {
         const int a = w % LEN;
         const int o = w / LEN;
         const int p = o % O1, q = o / O1;
@@ -164,7 +164,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     }
     __syncthreads();
     // face b is the left face of tile cell b along D (between cells b-1 and b)
-    for (int f = tid; f < NFACE; f += NT) {
+    for (int f = tid; f < NFACE; f += NTH) {
         const int b = f % (TD + 1);
         const int o = f / (TD + 1);
         const int p = o % O1, q = o / O1;
@@ -187,11 +187,11 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 #pragma unroll
         for (int d = 0; d < 3; ++d)
             if (d != D) valid = valid && (org[d] + c[d] < G.n[d]);
-        if (valid) wsmax = fmax(wsmax, w);
+        if (valid) wsmax = fmax_(wsmax, w);
     }
     __syncthreads();
     // this thread's cell: acc += (-F_{i+1/2}) + F_{i-1/2}
-    {
+    if (tid < NT) {
         const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
         const int cd = D == 0 ? cx : (D == 1 ? cy : cz);
         const int p = D == 0 ? cy : cx;
@@ -201,7 +201,10 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         for (int k = 0; k < NV; ++k) {
             const R fl = fc[k * NFACE + o * (TD + 1) + cd];
             const R fr = fc[k * NFACE + o * (TD + 1) + cd + 1];
-            acc[k] = acc[k] + ((-fr) + fl);
+            if constexpr (!kExact && D == 0)
+                acc[k] = fl - fr;  // the first direction starts the sum
+            else
+                acc[k] = acc[k] + ((-fr) + fl);
         }
     }
     __syncthreads();
@@ -215,7 +218,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 // With C != R the combination with the stage inputs re-reads the exact R
 // values of the thread's own cell (L1/L2 hits: the tile load just fetched them)
 // and runs in R.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
                                            double (*wred)[3]) {
     using Ph = Physics<C, EQ, FLUX>;
@@ -223,7 +226,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     constexpr int NV = Ph::NV;
     constexpr int G = ReconTraits<RC>::ghosts;
     using SL = SmemLayout<C, NV, G, DIM, TX, TY, TZ>;
-    constexpr int NT = TX * TY * TZ;
+    constexpr int NT = TX * TY * TZ;  // cells of the tile
+    static_assert(NT <= NTH && NTH % 32 == 0, "one thread per cell at least, whole warps");
     constexpr bool kSame = std::is_same<R, C>::value;
     C* su = reinterpret_cast<C*>(smem_raw);
     C* rl = su + NV * SL::HALO;
@@ -241,7 +245,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     const R scale = (R)A.st->scale;
 
     // 1. tile + halo: padded cells [org, org + T + 2g) per active dimension
-    for (int w = tid; w < SL::HALO; w += NT) {
+    for (int w = tid; w < SL::HALO; w += NTH) {
         const int hx = w % SL::HX, hy = (w / SL::HX) % SL::HY, hz = w / (SL::HX * SL::HY);
         const int px = org[0] + hx, py = org[1] + hy, pz = org[2] + hz;
         if (px < Gd.t[0] && py < Gd.t[1] && pz < Gd.t[2]) {
@@ -270,11 +274,11 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     // conversion per thread gives the same double as converting every face)
     C wsd[3] = {C(0), C(0), C(0)};
     const C gamma = C(A.gamma);
-    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
+    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
     if constexpr (DIM > 1)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
     if constexpr (DIM > 2)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
 
     // 3. wave speeds (stage 0 only): warp max, CTA max, one atomic per direction
     if (mode == MODE_L) {
@@ -282,18 +286,19 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
         for (int d = 0; d < DIM; ++d) {
             C v = wsd[d];
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v = fmax(v, shfl_xor_c(v, off));
+            for (int off = 16; off > 0; off >>= 1) v = fmax_(v, shfl_xor_c(v, off));
             if ((tid & 31) == 0) wred[tid >> 5][d] = (double)v;
         }
         __syncthreads();
         if (tid < DIM) {
             double v = 0.0;
-            for (int w = 0; w < NT / 32; ++w) v = fmax(v, wred[w][tid]);
+            for (int w = 0; w < NTH / 32; ++w) v = fmax_(v, wred[w][tid]);
             atomic_max_nonneg(&A.st->ws_bits[tid], v);
         }
     }
 
     // 4. this thread's cell: combine and write with its ghost images
+    if (tid >= NT) return;  // no barrier follows
     const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
     const int ix = org[0] + cx, iy = org[1] + cy, iz = org[2] + cz;
     if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) return;  // no barrier follows
@@ -346,13 +351,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             }
 }
 
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
-__global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+__global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double wred[(TX * TY * TZ) / 32][3];
+    __shared__ double wred[NTH / 32][3];
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
-    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, C>(A, org, smem_raw, wred);
+    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
 }
 
 // Persistent ensemble stage: each CTA walks the tile list (tiles of every
@@ -360,10 +365,10 @@ __global__ void __launch_bounds__(TX* TY* TZ) stage_kernel(StageArgs A) {
 // is done is skipped as a whole; the per-member wave-speed maxima land in
 // that member's step state (a segmented reduction), so every member gets its
 // own dt.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, class C = R>
-__global__ void __launch_bounds__(TX* TY* TZ) batch_stage_kernel(BatchArgs B) {
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+__global__ void __launch_bounds__(NTH) batch_stage_kernel(BatchArgs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double wred[(TX * TY * TZ) / 32][3];
+    __shared__ double wred[NTH / 32][3];
     const int ntiles = *B.ntiles;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 tile = B.tiles[t];
@@ -391,7 +396,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) batch_stage_kernel(BatchArgs B) {
             A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
         }
         const int org[3] = {tile.y, tile.z, tile.w};
-        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, C>(A, org, smem_raw, wred);
+        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
         __syncthreads();
     }
 }

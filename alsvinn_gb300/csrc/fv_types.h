@@ -39,6 +39,37 @@ struct StepParams {
     int stop_at_save = 0;       // end the advance after a step that reached a save time
 };
 
+// Tile of one CTA of the stage kernels and the CTA's thread count, per
+// dimension and arithmetic variant (0 fp64, 1 fp64 exact, 2 fp32, 3 fp64 state
+// with double-float arithmetic). A tile of T cells per direction needs
+// T_d + 2 reconstructions and T_d + 1 face fluxes along each direction d
+// (times the other extents). The FP64 and FP32 kernels use 32 x 8 tiles, one
+// thread per cell; the double-float kernel, bound by barrier waits, uses a
+// 16 x 12 tile on 256 threads, which keeps each reconstruction and flux phase
+// within one pass of the threads (a second, nearly empty pass leaves most
+// warps waiting at the next barrier). Threads past the tile's cells join the
+// reconstruction and flux phases only.
+template <int DIM, int VAR> struct TileShape;
+template <int VAR> struct TileShape<1, VAR> { static constexpr int X = 128, Y = 1, Z = 1, THREADS = 128; };
+template <int VAR> struct TileShape<2, VAR> { static constexpr int X = 32, Y = 8, Z = 1, THREADS = 256; };
+template <> struct TileShape<2, 3> { static constexpr int X = 16, Y = 12, Z = 1, THREADS = 256; };
+template <int VAR> struct TileShape<3, VAR> { static constexpr int X = 8, Y = 8, Z = 4, THREADS = 256; };
+
+template <int VAR> inline int tile_extent_v(int dim, int axis) {
+    const int shapes[3][3] = {{TileShape<1, VAR>::X, TileShape<1, VAR>::Y, TileShape<1, VAR>::Z},
+                              {TileShape<2, VAR>::X, TileShape<2, VAR>::Y, TileShape<2, VAR>::Z},
+                              {TileShape<3, VAR>::X, TileShape<3, VAR>::Y, TileShape<3, VAR>::Z}};
+    return shapes[dim - 1][axis];
+}
+inline int tile_extent(int variant, int dim, int axis) {
+    switch (variant) {
+        case 0: return tile_extent_v<0>(dim, axis);
+        case 1: return tile_extent_v<1>(dim, axis);
+        case 2: return tile_extent_v<2>(dim, axis);
+        default: return tile_extent_v<3>(dim, axis);
+    }
+}
+
 struct Grid {
     int n[3];   // interior cells
     int g[3];   // ghosts per dimension (0 in inactive dimensions)

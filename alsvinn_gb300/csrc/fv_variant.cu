@@ -37,17 +37,12 @@ typedef Real Compute;
 namespace gbfv {
 namespace GBFV_VARIANT_NS {
 
-template <int DIM> struct TileShape;
-template <> struct TileShape<1> { static constexpr int X = 128, Y = 1, Z = 1; };
-template <> struct TileShape<2> { static constexpr int X = 32, Y = 8, Z = 1; };
-template <> struct TileShape<3> { static constexpr int X = 8, Y = 8, Z = 4; };
-
 template <int EQ, int FLUX, int RC, int DIM>
 struct StageEntry {
-    using TS = TileShape<DIM>;
+    using TS = TileShape<DIM, FV_VARIANT>;
     using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
     static int launch(const StageArgs& a, cudaStream_t s) {
-        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, Compute>;
+        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, Compute>;
         static int configured = 0;
         if (!configured) {
             cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
@@ -55,29 +50,29 @@ struct StageEntry {
             configured = 1;
         }
         dim3 grid((a.G.n[0] + TS::X - 1) / TS::X, (a.G.n[1] + TS::Y - 1) / TS::Y, (a.G.n[2] + TS::Z - 1) / TS::Z);
-        k<<<grid, TS::X * TS::Y * TS::Z, SL::bytes, s>>>(a);
+        k<<<grid, TS::THREADS, SL::bytes, s>>>(a);
         return (int)cudaGetLastError();
     }
 };
 
 template <int EQ, int FLUX, int RC, int DIM>
 struct BatchEntry {
-    using TS = TileShape<DIM>;
+    using TS = TileShape<DIM, FV_VARIANT>;
     using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
     static int launch(const BatchArgs& a, int ctas, cudaStream_t s) {
-        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, Compute>;
+        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, Compute>;
         static int resident = 0;
         if (!resident) {
             cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
             if (e != cudaSuccess) return (int)e;
             int per_sm = 0, dev = 0, sms = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TS::X * TS::Y * TS::Z, SL::bytes);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TS::THREADS, SL::bytes);
             if (e == cudaSuccess) e = cudaGetDevice(&dev);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return (int)e;
             resident = (per_sm > 0 ? per_sm : 1) * sms;
         }
-        k<<<ctas > 0 ? ctas : resident, TS::X * TS::Y * TS::Z, SL::bytes, s>>>(a);
+        k<<<ctas > 0 ? ctas : resident, TS::THREADS, SL::bytes, s>>>(a);
         return (int)cudaGetLastError();
     }
 };

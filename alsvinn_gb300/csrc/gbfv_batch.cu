@@ -216,14 +216,11 @@ int bfail(int code, const std::string& m) { return gbfv_internal_fail(code, m.c_
         if (e_ != cudaSuccess) return bfail(GBFV_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-int tile_shape(int dim, int k) {
-    static const int shapes[3][3] = {{128, 1, 1}, {32, 8, 1}, {8, 8, 4}};
-    return shapes[dim - 1][k];
-}
+int tile_shape(const gbfv_batch* b, int k) { return tile_extent(b->scheme.var, b->dim, k); }
 
 int rebuild_tiles(gbfv_batch* b) {
     std::vector<int4> tiles;
-    const int tx = tile_shape(b->dim, 0), ty = tile_shape(b->dim, 1), tz = tile_shape(b->dim, 2);
+    const int tx = tile_shape(b, 0), ty = tile_shape(b, 1), tz = tile_shape(b, 2);
     for (size_t s = 0; s < b->members.size(); ++s) {
         const auto& h = b->members[s];
         if (!h.active) continue;

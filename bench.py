@@ -65,14 +65,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per stage launch from the committed ncu summary, if any."""
+def profile_summary():
+    """The committed ncu figures of the stage kernel (DRAM bytes per launch,
+    FP64 pipe use), if any."""
     p = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return d.get("dram_bytes_per_launch")
-    return None
+            return json.load(f)
+    return {}
+
+
+def profile_traffic():
+    """DRAM bytes per stage launch from the committed ncu summary, if any."""
+    return profile_summary().get("dram_bytes_per_launch")
 
 
 class ClockSampler:
@@ -296,7 +301,12 @@ def run_gpu(args):
                 "kernel": "stage_kernel<double,euler2,hll3,weno2,2D>", "launch_ms": per_launch_ms,
                 "alg_bytes_per_launch": alg_bytes_per_launch,
                 "note": "FP64 arithmetic on GB300 issues at ~1/64 of the FP32 rate; this step is FP64-compute "
-                        "bound, not HBM bound"}
+                        "bound, not HBM bound",
+                "fp64_pipe": {"active_frac": profile_summary().get("fp64_pipe_active_frac"),
+                              "issue_frac": profile_summary().get("fp64_issue_frac"),
+                              "source": "ncu sm__pipe_fp64_cycles_active and DADD+DFMA+DMUL thread "
+                                        "instructions per cycle over the 2 per SM per cycle peak "
+                                        "(profiles/stage_kernel_kh1024_fp64.md)"}}
     clk = clocks.summary()
     line = None
     if rank == 0:

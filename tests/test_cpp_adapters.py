@@ -1,6 +1,6 @@
-"""The C++ adapter header (include/gbfv_alsfvm.hpp): it compiles on the CPU;
-its test program, written like the reference's library tests, passes on the
-GPU."""
+"""The C++ adapter header (include/gbfv_alsfvm.hpp) and the fast special
+functions of the kernels: both test programs compile on the CPU and pass on
+the GPU (the adapters' one is written like the reference's library tests)."""
 import os
 import shutil
 import subprocess
@@ -31,6 +31,31 @@ def test_adapter_header_compiles():
 def test_adapters_pass_their_tests(cuda_device, tmp_path):
     exe = str(tmp_path / "test_alsfvm_adapters")
     p = subprocess.run(compile_cmd(exe), capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASSED" in r.stdout
+
+
+SPECIAL = os.path.join(ROOT, "tests", "cpp", "test_special_functions.cu")
+
+
+def _nvcc_cmd(out):
+    nvcc = os.path.join(CUDA, "bin", "nvcc")
+    return [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+            "-I" + os.path.join(ROOT, "alsvinn_gb300", "csrc"), SPECIAL, "-o", out]
+
+
+def test_special_function_test_compiles(tmp_path):
+    p = subprocess.run(_nvcc_cmd(str(tmp_path / "sf")), capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+
+
+@pytest.mark.gpu
+def test_special_functions_meet_their_error_bounds(cuda_device, tmp_path):
+    exe = str(tmp_path / "sf")
+    p = subprocess.run(_nvcc_cmd(exe), capture_output=True, text=True)
     assert p.returncode == 0, p.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(r.stdout)
