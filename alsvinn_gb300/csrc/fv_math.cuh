@@ -16,6 +16,7 @@
 
 #include <type_traits>
 
+#include "fv_df.cuh"
 #include "fv_types.h"
 
 // Kernel code is compiled once per arithmetic variant; each variant's
@@ -122,6 +123,36 @@ template <> __device__ __forceinline__ double fmax_<double>(double a, double b) 
     return order_key(x) >= order_key(y) ? a : b;
 }
 
+// Double-float evaluation of the nonlinear coefficients of the fast FP64
+// policy: the WENO2 weights and the HLL / HLL3 wave-speed estimates. They
+// enter the fluxes multiplied by differences of the state -- the weights by
+// the one-sided differences, the speeds through s (U* - U) and a star state
+// whose sensitivity to s vanishes with the jump -- so their 2^-48 relative
+// precision moves a flux by 2^-48 of those differences, well below the FP64
+// rounding of the fluxes themselves, while ~30 FP64 instructions per face and
+// ~20 per reconstructed cell move to the FP32 pipes (GB300 issues FP64 at 1/64
+// of the FP32 rate). Inputs whose squares or products could leave the FP32
+// exponent range take the FP64 formulas instead.
+__device__ __forceinline__ bool df_range(double x, int max_exp) {  // |x| < 2^max_exp, finite
+    return (dbits(x) & kAbsMask) < ((long long)(1023 + max_exp) << 52);
+}
+
+template <bool CORRECT>
+__device__ __forceinline__ void wave_speeds_df(double wl, double wr, double ul, double ur, double pl, double pr,
+                                               double il, double ir, double rl, double rr, double gamma,
+                                               double& sL, double& sR) {
+    const dfloat Wl(wl), Wr(wr), Ul(ul), Ur(ur), Pl(pl), Pr(pr), Il(il), Ir(ir), G(gamma);
+    const dfloat winv = dfloat(1) / (Wl + Wr);
+    const dfloat ud = (Wl * Ul + Wr * Ur) * winv;
+    const dfloat p = (Wl * Pl + Wr * Pr) * winv;
+    const dfloat cl = sqrt(G * Pl * Il), cr = sqrt(G * Pr * Ir);
+    const dfloat cs = sqrt((G + G) * p / (dfloat(rl) + dfloat(rr)));
+    dfloat corr(0.f);
+    if (CORRECT) corr = dfloat(0.5f) * fmax(dfloat(0), Ul - Ur);
+    sL = (double)fmin(Ul + corr - cl, ud - cs);
+    sR = (double)fmax(Ur - corr + cr, ud + cs);
+}
+
 // sqrt(x) = x / sqrt(x) for positive finite x; zero, negative and NaN
 // arguments take the IEEE square root
 template <class R> __device__ __forceinline__ R sqrt_(R x) { return sqrt(x); }
@@ -217,17 +248,28 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
         speedLeft = fmin(L.u[D] + correct - cfLeft, ud - cs);
         speedRight = fmax(Rs.u[D] - correct + cfRight, ud + cs);
     } else {
-        const R waveLeft = L.w;
-        const R waveRight = Rs.w;
-        const R winv = rcp_(waveLeft + waveRight);
-        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
-        const R p = (waveLeft * L.p + waveRight * Rs.p) * winv;
-        const R cfLeft = sqrt_(gamma * L.p * L.rinv);
-        const R cfRight = sqrt_(gamma * Rs.p * Rs.rinv);
-        const R correct = R(0.5) * fmax_(R(0), L.u[D] - Rs.u[D]);
-        const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
-        speedLeft = fmin_(L.u[D] + correct - cfLeft, ud - cs);
-        speedRight = fmax_(Rs.u[D] - correct + cfRight, ud + cs);
+        bool done = false;
+        if constexpr (std::is_same<R, double>::value) {
+            if (df_range(L.w, 60) && df_range(Rs.w, 60) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
+                df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
+                wave_speeds_df<true>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
+                                     speedLeft, speedRight);
+                done = true;
+            }
+        }
+        if (!done) {
+            const R waveLeft = L.w;
+            const R waveRight = Rs.w;
+            const R winv = rcp_(waveLeft + waveRight);
+            const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
+            const R p = (waveLeft * L.p + waveRight * Rs.p) * winv;
+            const R cfLeft = sqrt_(gamma * L.p * L.rinv);
+            const R cfRight = sqrt_(gamma * Rs.p * Rs.rinv);
+            const R correct = R(0.5) * fmax_(R(0), L.u[D] - Rs.u[D]);
+            const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
+            speedLeft = fmin_(L.u[D] + correct - cfLeft, ud - cs);
+            speedRight = fmax_(Rs.u[D] - correct + cfRight, ud + cs);
+        }
     }
     R fluxLeft[NV], fluxRight[NV];
     euler_point_flux<R, NSD, D>(L, fluxLeft);
@@ -302,12 +344,23 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
         speedLeft = fmin(L.u[D] - sqrt(gamma * L.p / L.rho), ud - cs);
         speedRight = fmax(Rs.u[D] + sqrt(gamma * Rs.p / Rs.rho), ud + cs);
     } else {
-        const R winv = rcp_(waveLeft + waveRight);
-        const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
-        const R p = (L.p * waveLeft + Rs.p * waveRight) * winv;
-        const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
-        speedLeft = fmin_(L.u[D] - sqrt_(gamma * L.p * L.rinv), ud - cs);
-        speedRight = fmax_(Rs.u[D] + sqrt_(gamma * Rs.p * Rs.rinv), ud + cs);
+        bool done = false;
+        if constexpr (std::is_same<R, double>::value) {
+            if (df_range(L.w, 60) && df_range(Rs.w, 60) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
+                df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
+                wave_speeds_df<false>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
+                                      speedLeft, speedRight);
+                done = true;
+            }
+        }
+        if (!done) {
+            const R winv = rcp_(waveLeft + waveRight);
+            const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) * winv;
+            const R p = (L.p * waveLeft + Rs.p * waveRight) * winv;
+            const R cs = sqrt_(R(2) * gamma * p * rcp_(L.rho + Rs.rho));
+            speedLeft = fmin_(L.u[D] - sqrt_(gamma * L.p * L.rinv), ud - cs);
+            speedRight = fmax_(Rs.u[D] + sqrt_(gamma * Rs.p * Rs.rinv), ud + cs);
+        }
     }
     if (is0(speedLeft)) {
 #pragma unroll
@@ -432,16 +485,35 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
             // mirrored pair on the right face; normalising gives weights in
             // terms of s_k = (eps+b_k)^2 with one reciprocal per face.
             const R eps = R(FV_WENO_EPSILON);
-            const R s0 = (eps + b0) * (eps + b0);
-            const R s1 = (eps + b1) * (eps + b1);
-            const R iL = rcp_(s1 + R(2) * s0);
-            const R iR = rcp_(R(2) * s1 + s0);
             if constexpr (std::is_same<R, double>::value || std::is_same<R, float>::value) {
                 // half weights and hardware FMAs: with w0 + w1 = 1,
                 // left = u_i - (w1/2)(u_i - u_{i-1}) - (w0/2)(u_{i+1} - u_i),
                 // right = u_i + (w0/2)(u_{i+1} - u_i) + (w1/2)(u_i - u_{i-1})
-                const R h0L = R(0.5) * s1 * iL, h1L = s0 * iL;
-                const R h0R = s1 * iR, h1R = R(0.5) * s0 * iR;
+                R h0L, h1L, h0R, h1R;
+                bool done = false;
+                if constexpr (std::is_same<R, double>::value) {
+                    if (df_range(d0, 30) && df_range(d1, 30)) {
+                        const dfloat D0(d0), D1(d1), E(FV_WENO_EPSILON);
+                        const dfloat e0 = E + D0 * D0, e1 = E + D1 * D1;
+                        const dfloat s0 = e0 * e0, s1 = e1 * e1;
+                        const dfloat iL = dfloat(1) / (s1 + s0 + s0), iR = dfloat(1) / (s1 + s1 + s0);
+                        h0L = (double)(dfloat(0.5f) * s1 * iL);
+                        h1L = (double)(s0 * iL);
+                        h0R = (double)(s1 * iR);
+                        h1R = (double)(dfloat(0.5f) * s0 * iR);
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    const R s0 = (eps + b0) * (eps + b0);
+                    const R s1 = (eps + b1) * (eps + b1);
+                    const R iL = rcp_(s1 + R(2) * s0);
+                    const R iR = rcp_(R(2) * s1 + s0);
+                    h0L = R(0.5) * s1 * iL;
+                    h1L = s0 * iL;
+                    h0R = s1 * iR;
+                    h1R = R(0.5) * s0 * iR;
+                }
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
                     const R* v = u + k * vs;
@@ -452,6 +524,10 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
                 }
                 return;
             }
+            const R s0 = (eps + b0) * (eps + b0);
+            const R s1 = (eps + b1) * (eps + b1);
+            const R iL = rcp_(s1 + R(2) * s0);
+            const R iR = rcp_(R(2) * s1 + s0);
             w0Left = s1 * iL;
             w1Left = R(2) * s0 * iL;
             w0Right = R(2) * s1 * iR;
