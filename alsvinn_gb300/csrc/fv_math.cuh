@@ -160,10 +160,36 @@ template <> __device__ __forceinline__ double sqrt_<double>(double x) {
     return in_rsqrt_range(x) ? x * rsqrt_nr(x) : sqrt(x);
 }
 
-// 1/rho and sqrt(rho) of a density: one reciprocal square root for FP64
+// FP32 state (its tolerance is set by FP32 rounding): the special-function
+// unit's approximations, within ~2 ulp, instead of the multi-instruction IEEE
+// division and square root
+template <> __device__ __forceinline__ float rcp_<float>(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+template <> __device__ __forceinline__ float sqrt_<float>(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// 1/rho and sqrt(rho) of a density: one reciprocal square root for FP64 and
+// FP32
 template <class R> __device__ __forceinline__ void inv_sqrt_pair(R rho, R& rinv, R& w) {
     rinv = rcp_(rho);
     w = sqrt(rho);
+}
+template <> __device__ __forceinline__ void inv_sqrt_pair<float>(float rho, float& rinv, float& w) {
+    if (rho > 0.f) {
+        float rs;
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rs) : "f"(rho));
+        rinv = rs * rs;
+        w = rho * rs;
+    } else {
+        rinv = 1.f / rho;
+        w = sqrtf(rho);
+    }
 }
 template <> __device__ __forceinline__ void inv_sqrt_pair<double>(double rho, double& rinv, double& w) {
     if (in_rsqrt_range(rho)) {

@@ -337,18 +337,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     if (A.check && !PhR::obeys(res, (R)A.gamma)) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
-    int px[3], py[3], pz[3];
-    const bool per = A.periodic != 0;
-    const int cxn = images(ix, Gd.n[0], Gd.g[0], per, px);
-    const int cyn = images(iy, Gd.n[1], Gd.g[1], per, py);
-    const int czn = images(iz, Gd.n[2], Gd.g[2], per, pz);
-    for (int a = 0; a < czn; ++a)
-        for (int b = 0; b < cyn; ++b)
-            for (int c = 0; c < cxn; ++c) {
-                const long long gi = gidx(Gd, px[c], py[b], pz[a]);
-#pragma unroll
-                for (int k = 0; k < NV; ++k) out[k * total + gi] = res[k];
-            }
+    store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
 }
 
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
@@ -366,7 +355,7 @@ __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
 // that member's step state (a segmented reduction), so every member gets its
 // own dt.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
-__global__ void __launch_bounds__(NTH) batch_stage_kernel(BatchArgs B) {
+__global__ void __launch_bounds__(NTH, (std::is_same<C, float>::value ? 5 : 1)) batch_stage_kernel(BatchArgs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double wred[NTH / 32][3];
     const int ntiles = *B.ntiles;
@@ -426,18 +415,7 @@ __global__ void fe_apply_kernel(StageArgs A) {
     if (A.check && !Ph::obeys(res, (R)A.gamma)) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
-    int px[3], py[3], pz[3];
-    const bool per = A.periodic != 0;
-    const int cxn = images(ix, Gd.n[0], Gd.g[0], per, px);
-    const int cyn = images(iy, Gd.n[1], Gd.g[1], per, py);
-    const int czn = images(iz, Gd.n[2], Gd.g[2], per, pz);
-    for (int a = 0; a < czn; ++a)
-        for (int b = 0; b < cyn; ++b)
-            for (int c = 0; c < cxn; ++c) {
-                const long long gi = gidx(Gd, px[c], py[b], pz[a]);
-#pragma unroll
-                for (int k = 0; k < NV; ++k) out[k * total + gi] = res[k];
-            }
+    store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
 }
 
 }  // namespace GBFV_VARIANT_NS

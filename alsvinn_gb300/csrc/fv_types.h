@@ -82,22 +82,52 @@ __device__ __forceinline__ long long gidx(const Grid& G, int x, int y, int z) {
     return ((long long)z * G.t[1] + y) * G.t[0] + x;
 }
 
-// Padded positions holding the value of interior cell i (interior coordinate)
-// along one dimension: the cell itself plus its ghost images
-// (Neumann mirror: alsfvm/include/alsfvm/boundary/Neumann.hpp:24-35;
-// periodic wrap: Periodic.hpp:24-42). Returns the count (1..3).
-__device__ __forceinline__ int images(int i, int n, int g, bool periodic, int* pos) {
-    int c = 0;
-    pos[c++] = i + g;
-    if (g == 0) return c;
-    if (periodic) {
-        if (i < g) pos[c++] = i + g + n;
-        if (i >= n - g) pos[c++] = i + g - n;
-    } else {
-        if (i < g) pos[c++] = g - 1 - i;
-        if (i >= n - g) pos[c++] = 2 * n + g - 1 - i;
+// Padded positions holding the value of interior cell i (interior
+// coordinate) along one dimension: slot 0 the cell itself, slots 1 and 2 its
+// ghost images (Neumann mirror: alsfvm/include/alsfvm/boundary/Neumann.hpp:
+// 24-35; periodic wrap: Periodic.hpp:24-42). Returns the mask of valid slots
+// (bit 0 always). Fixed slots keep the positions in registers.
+__device__ __forceinline__ int images(int i, int n, int g, bool periodic, int pos[3]) {
+    pos[0] = i + g;
+    pos[1] = 0;
+    pos[2] = 0;
+    int mask = 1;
+    if (g > 0) {
+        if (i < g) {
+            pos[1] = periodic ? i + g + n : g - 1 - i;
+            mask |= 2;
+        }
+        if (i >= n - g) {
+            pos[2] = periodic ? i + g - n : 2 * n + g - 1 - i;
+            mask |= 4;
+        }
     }
-    return c;
+    return mask;
+}
+
+// Stores one cell's values at its position and every ghost image of it.
+template <class R, int NV>
+__device__ __forceinline__ void store_with_images(R* out, long long total, const Grid& G, int ix, int iy, int iz,
+                                                  bool periodic, const R* v) {
+    int px[3], py[3], pz[3];
+    const int xm = images(ix, G.n[0], G.g[0], periodic, px);
+    const int ym = images(iy, G.n[1], G.g[1], periodic, py);
+    const int zm = images(iz, G.n[2], G.g[2], periodic, pz);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!((zm >> a) & 1)) continue;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (!((ym >> b) & 1)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (!((xm >> c) & 1)) continue;
+                const long long gi = gidx(G, px[c], py[b], pz[a]);
+#pragma unroll
+                for (int k = 0; k < NV; ++k) out[k * total + gi] = v[k];
+            }
+        }
+    }
 }
 
 
