@@ -427,7 +427,66 @@ __device__ __forceinline__ R flux_godunov(R uL, R uR, R* F) {
     return fmax_(fabs(uL), fabs(uR));
 }
 
+// Central flux F = (f(L) + f(R)) / 2 with the wave speed max over the two
+// states of |u_d| + sqrt(gamma p / rho) (alsfvm/include/alsfvm/numflux/
+// Central.hpp:31-55, Euler.hpp:251-258).
+template <class R, int NSD, int D>
+__device__ __forceinline__ R flux_central(const EulerState<R, NSD>& L, const EulerState<R, NSD>& Rs, R gamma,
+                                          R* F) {
+    constexpr int NV = NSD + 2;
+    R fl[NV], fr[NV];
+    euler_point_flux<R, NSD, D>(L, fl);
+    euler_point_flux<R, NSD, D>(Rs, fr);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) F[k] = R(0.5) * (fl[k] + fr[k]);
+    R wl, wr;
+    if (kExact) {
+        wl = fabs(L.u[D]) + sqrt(gamma * L.p / L.rho);
+        wr = fabs(Rs.u[D]) + sqrt(gamma * Rs.p / Rs.rho);
+    } else {
+        wl = fabs(L.u[D]) + sqrt_(gamma * L.p * L.rinv);
+        wr = fabs(Rs.u[D]) + sqrt_(gamma * Rs.p * Rs.rinv);
+    }
+    return fmax_(wl, wr);
+}
+
+// Burgers fluxes beyond Godunov, f(u) = u u / 2, wave speed max(|uL|, |uR|):
+// Central, Rusanov with the eigenvalue u (alsfvm/include/alsfvm/numflux/
+// Rusanov.hpp:31-59, Burgers.hpp:298-301) and Roe (alsfvm/include/alsfvm/
+// numflux/burgers/Roe.hpp:30-58).
+template <class R, int FLUX>
+__device__ __forceinline__ R flux_burgers(R uL, R uR, R* F) {
+    const R fL = uL * uL / R(2), fR = uR * uR / R(2);
+    if constexpr (FLUX == 3) {  // central
+        F[0] = R(0.5) * (fL + fR);
+    } else if constexpr (FLUX == 4) {  // rusanov
+        const R eigenMax = fmax_(fabs(uL), fabs(uR));
+        F[0] = R(0.5) * (fL + fR) - R(0.5) * eigenMax * (uR - uL);
+    } else {  // roe
+        if (uL >= -uR) {
+            const R a = fmax_(uL, R(0));
+            F[0] = a * a / R(2);
+        } else {
+            const R b = fmin_(uR, R(0));
+            F[0] = b * b / R(2);
+        }
+    }
+    return fmax_(fabs(uL), fabs(uR));
+}
+
 // ------------------------------------------------------- reconstruction
+
+// sign (1, 0, -1; -1 for NaN) and minmod of the limiter reconstructions
+// (alsfvm/include/alsfvm/reconstruction/sign.hpp, minmod.hpp)
+template <class R> __device__ __forceinline__ R sign_of(R a) { return gt0(a) ? R(1) : (is0(a) ? R(0) : R(-1)); }
+template <class R> __device__ __forceinline__ R minmod2(R a, R b) {
+    const R sa = sign_of(a);
+    return sa == sign_of(b) ? sa * fmin_(fabs(a), fabs(b)) : R(0);
+}
+template <class R> __device__ __forceinline__ R minmod3(R a, R b, R c) {
+    const R sa = sign_of(a), sb = sign_of(b);
+    return (sa == sb && sb == sign_of(c)) ? sa * fmin_(fabs(a), fmin_(fabs(b), fabs(c))) : R(0);
+}
 
 
 template <int RC> struct ReconTraits;
@@ -436,6 +495,8 @@ template <> struct ReconTraits<RC_WENO2> { static constexpr int ghosts = 2; stat
 template <> struct ReconTraits<RC_ENO2> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
 template <> struct ReconTraits<RC_ENO3> { static constexpr int ghosts = 3; static constexpr int reach = 2; };
 template <> struct ReconTraits<RC_ENO4> { static constexpr int ghosts = 4; static constexpr int reach = 3; };
+template <> struct ReconTraits<RC_MC> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
+template <> struct ReconTraits<RC_MM> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
 
 // ENO coefficient rows (alsfvm/src/reconstruction/ENOCoefficients.cpp:21-49):
 // row r weights the stencil starting r cells to the left for the value at the
@@ -488,6 +549,21 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
     if constexpr (RC == RC_NONE) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) left[k] = right[k] = u[k * vs];
+    } else if constexpr (RC == RC_MC || RC == RC_MM) {
+        // MC / MM slope limiters on every variable (alsfvm/include/alsfvm/
+        // reconstruction/MC.hpp:27-52, MM.hpp:25-47)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const R* v = u + k * vs;
+            const R l = v[-ds], m = v[0], r = v[ds];
+            R sigma;
+            if constexpr (RC == RC_MC)
+                sigma = minmod3(R(2) * (r - m), (r - l) / R(2), R(2) * (m - l));
+            else
+                sigma = minmod2(r - m, m - l);
+            left[k] = m - sigma / R(2);
+            right[k] = m + sigma / R(2);
+        }
     } else if constexpr (RC == RC_WENO2) {
         // WENO2::reconstruct (alsfvm/include/alsfvm/reconstruction/WENO2.hpp:31-91).
         const R i0 = u[0];

@@ -10,8 +10,16 @@ namespace gbfv {
 // Arithmetic variants of the step.
 enum Variant { VAR_F64 = 0, VAR_F64_EXACT = 1, VAR_F32 = 2, VAR_F64_DF = 3, NUM_VARIANTS = 4 };
 enum Equation { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3, NUM_EQ = 4 };
-enum Flux { FL_HLL = 0, FL_HLL3 = 1, FL_GODUNOV = 2, NUM_FLUX = 3 };
-constexpr int NUM_RECON = 5;
+enum Flux { FL_HLL = 0, FL_HLL3 = 1, FL_GODUNOV = 2, FL_CENTRAL = 3, FL_RUSANOV = 4, FL_ROE = 5, NUM_FLUX = 6 };
+constexpr int NUM_RECON = 7;
+
+// The fluxes each equation offers (alsfvm/include/alsfvm/numflux/
+// numerical_flux_list.hpp:41-113): Euler hll, hll3, central; Burgers
+// godunov, central, rusanov, roe.
+inline bool flux_applies(int eq, int fl) {
+    if (eq == EQ_BURGERS) return fl == FL_GODUNOV || fl == FL_CENTRAL || fl == FL_RUSANOV || fl == FL_ROE;
+    return fl == FL_HLL || fl == FL_HLL3 || fl == FL_CENTRAL;
+}
 
 typedef int (*StageLauncher)(const StageArgs& a, cudaStream_t s);
 typedef int (*ApplyLauncher)(const StageArgs& a, cudaStream_t s);

@@ -62,7 +62,10 @@ template <class R, int EQ, int FLUX> struct Physics {
     template <int D>
     static __device__ __forceinline__ R face_flux(const R* a, const R* b, R gamma, R* F) {
         if constexpr (EQ == 0) {
-            return flux_godunov<R>(a[0], b[0], F);
+            if constexpr (FLUX == 2)
+                return flux_godunov<R>(a[0], b[0], F);
+            else
+                return flux_burgers<R, FLUX>(a[0], b[0], F);
         } else {
             EulerState<R, NSD> L, Rr;
             L.rho = a[0];
@@ -78,6 +81,8 @@ template <class R, int EQ, int FLUX> struct Physics {
             euler_extra<R, NSD>(Rr, gamma);
             if constexpr (FLUX == 1)
                 return flux_hll3<R, NSD, D>(L, Rr, gamma, F);
+            else if constexpr (FLUX == 3)
+                return flux_central<R, NSD, D>(L, Rr, gamma, F);
             else
                 return flux_hll<R, NSD, D>(L, Rr, gamma, F);
         }

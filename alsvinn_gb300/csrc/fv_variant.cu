@@ -146,24 +146,28 @@ static int launch_check(const CheckArgs& a, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
+template <int FLUX, int RC, int DIM>
+static void reg_one(Registry& R) {
+    constexpr int V = FV_VARIANT, E = FV_EQ;
+    R.stage[V][E][FLUX][RC][DIM - 1] = &StageEntry<E, FLUX, RC, DIM>::launch;
+    R.batch[V][E][FLUX][RC][DIM - 1] = &BatchEntry<E, FLUX, RC, DIM>::launch;
+    R.stage_smem[V][E][FLUX][RC][DIM - 1] = StageEntry<E, FLUX, RC, DIM>::SL::bytes;
+}
+
+// Every reconstruction for one flux in one dimension. The double-float
+// variant covers the WENO / ENO reconstructions only (its stage kernels are
+// the slowest to compile).
 template <int FLUX, int DIM>
 static void reg_dim(Registry& R) {
-    constexpr int V = FV_VARIANT, E = FV_EQ;
-    R.stage[V][E][FLUX][RC_NONE][DIM - 1] = &StageEntry<E, FLUX, RC_NONE, DIM>::launch;
-    R.stage[V][E][FLUX][RC_WENO2][DIM - 1] = &StageEntry<E, FLUX, RC_WENO2, DIM>::launch;
-    R.stage[V][E][FLUX][RC_ENO2][DIM - 1] = &StageEntry<E, FLUX, RC_ENO2, DIM>::launch;
-    R.stage[V][E][FLUX][RC_ENO3][DIM - 1] = &StageEntry<E, FLUX, RC_ENO3, DIM>::launch;
-    R.stage[V][E][FLUX][RC_ENO4][DIM - 1] = &StageEntry<E, FLUX, RC_ENO4, DIM>::launch;
-    R.batch[V][E][FLUX][RC_NONE][DIM - 1] = &BatchEntry<E, FLUX, RC_NONE, DIM>::launch;
-    R.batch[V][E][FLUX][RC_WENO2][DIM - 1] = &BatchEntry<E, FLUX, RC_WENO2, DIM>::launch;
-    R.batch[V][E][FLUX][RC_ENO2][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO2, DIM>::launch;
-    R.batch[V][E][FLUX][RC_ENO3][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO3, DIM>::launch;
-    R.batch[V][E][FLUX][RC_ENO4][DIM - 1] = &BatchEntry<E, FLUX, RC_ENO4, DIM>::launch;
-    R.stage_smem[V][E][FLUX][RC_NONE][DIM - 1] = StageEntry<E, FLUX, RC_NONE, DIM>::SL::bytes;
-    R.stage_smem[V][E][FLUX][RC_WENO2][DIM - 1] = StageEntry<E, FLUX, RC_WENO2, DIM>::SL::bytes;
-    R.stage_smem[V][E][FLUX][RC_ENO2][DIM - 1] = StageEntry<E, FLUX, RC_ENO2, DIM>::SL::bytes;
-    R.stage_smem[V][E][FLUX][RC_ENO3][DIM - 1] = StageEntry<E, FLUX, RC_ENO3, DIM>::SL::bytes;
-    R.stage_smem[V][E][FLUX][RC_ENO4][DIM - 1] = StageEntry<E, FLUX, RC_ENO4, DIM>::SL::bytes;
+    reg_one<FLUX, RC_NONE, DIM>(R);
+    reg_one<FLUX, RC_WENO2, DIM>(R);
+    reg_one<FLUX, RC_ENO2, DIM>(R);
+    reg_one<FLUX, RC_ENO3, DIM>(R);
+    reg_one<FLUX, RC_ENO4, DIM>(R);
+#if FV_VARIANT != 3
+    reg_one<FLUX, RC_MC, DIM>(R);
+    reg_one<FLUX, RC_MM, DIM>(R);
+#endif
 }
 
 }  // namespace GBFV_VARIANT_NS
@@ -177,9 +181,23 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     reg_dim<FL_GODUNOV, 1>(*R);
     reg_dim<FL_GODUNOV, 2>(*R);
     reg_dim<FL_GODUNOV, 3>(*R);
+#if FV_VARIANT != 3
+    reg_dim<FL_CENTRAL, 1>(*R);
+    reg_dim<FL_CENTRAL, 2>(*R);
+    reg_dim<FL_CENTRAL, 3>(*R);
+    reg_dim<FL_RUSANOV, 1>(*R);
+    reg_dim<FL_RUSANOV, 2>(*R);
+    reg_dim<FL_RUSANOV, 3>(*R);
+    reg_dim<FL_ROE, 1>(*R);
+    reg_dim<FL_ROE, 2>(*R);
+    reg_dim<FL_ROE, 3>(*R);
+#endif
 #else
     reg_dim<FL_HLL, FV_EQ>(*R);
     reg_dim<FL_HLL3, FV_EQ>(*R);
+#if FV_VARIANT != 3
+    reg_dim<FL_CENTRAL, FV_EQ>(*R);
+#endif
 #endif
     R->apply[V][E] = &launch_apply<E>;
     R->check[V][E] = &launch_check<E>;
@@ -188,4 +206,6 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     R->recon[V][E][RC_ENO2] = &launch_recon<E, RC_ENO2>;
     R->recon[V][E][RC_ENO3] = &launch_recon<E, RC_ENO3>;
     R->recon[V][E][RC_ENO4] = &launch_recon<E, RC_ENO4>;
+    R->recon[V][E][RC_MC] = &launch_recon<E, RC_MC>;
+    R->recon[V][E][RC_MM] = &launch_recon<E, RC_MM>;
 }

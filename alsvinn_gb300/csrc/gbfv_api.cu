@@ -173,6 +173,9 @@ static int parse_flux(const char* s) {
     if (!strcmp(s, "hll")) return FL_HLL;
     if (!strcmp(s, "hll3")) return FL_HLL3;
     if (!strcmp(s, "godunov")) return FL_GODUNOV;
+    if (!strcmp(s, "central")) return FL_CENTRAL;
+    if (!strcmp(s, "rusanov")) return FL_RUSANOV;
+    if (!strcmp(s, "roe")) return FL_ROE;
     return -1;
 }
 static int parse_recon(const char* s) {
@@ -182,6 +185,8 @@ static int parse_recon(const char* s) {
     if (!strcmp(s, "eno2")) return RC_ENO2;
     if (!strcmp(s, "eno3")) return RC_ENO3;
     if (!strcmp(s, "eno4")) return RC_ENO4;
+    if (!strcmp(s, "mc")) return RC_MC;
+    if (!strcmp(s, "mm")) return RC_MM;
     return -1;
 }
 enum { IN_FE = 0, IN_RK2 = 1, IN_RK3 = 2 };
@@ -198,7 +203,7 @@ static int parse_bc(const char* s) {
     if (!strcmp(s, "periodic")) return 1;
     return -1;
 }
-static const int kReconGhosts[5] = {1, 2, 2, 3, 4};
+static const int kReconGhosts[7] = {1, 2, 2, 3, 4, 2, 2};
 
 // ---------------------------------------------------------------- solver
 
@@ -273,7 +278,7 @@ int gbfv_create(const gbfv_desc* d, gbfv_solver** out) {
     if (rc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown reconstruction");
     if (in < 0) return fail(GBFV_ERR_ARGUMENT, "unknown integrator");
     if (bc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown boundary");
-    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV))
+    if (!flux_applies(eq, fl))
         return fail(GBFV_ERR_UNSUPPORTED, "flux does not apply to this equation");
     if (d->precision < 0 || d->precision >= NUM_VARIANTS) return fail(GBFV_ERR_ARGUMENT, "bad precision");
     for (int k = 0; k < 3; ++k)
@@ -785,7 +790,7 @@ int gbfv_internal_plan(const gbfv_desc* d, GbfvPlan* p) {
     const int eq = parse_eq(d->equation), fl = parse_flux(d->flux), rc = parse_recon(d->reconstruction);
     const int in = parse_integrator(d->integrator), bc = parse_bc(d->boundary);
     if (eq < 0 || fl < 0 || rc < 0 || in < 0 || bc < 0) return fail(GBFV_ERR_ARGUMENT, "unknown name in descriptor");
-    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV)) return fail(GBFV_ERR_UNSUPPORTED, "flux does not apply to this equation");
+    if (!flux_applies(eq, fl)) return fail(GBFV_ERR_UNSUPPORTED, "flux does not apply to this equation");
     if (d->precision < 0 || d->precision >= NUM_VARIANTS) return fail(GBFV_ERR_ARGUMENT, "bad precision");
     for (int k = 0; k < 3; ++k)
         if (d->n[k] < 1) return fail(GBFV_ERR_ARGUMENT, "grid dimensions must be >= 1");

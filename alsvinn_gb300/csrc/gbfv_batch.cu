@@ -267,6 +267,7 @@ int enqueue_batch_step(gbfv_batch* b) {
     Registry& R = registry();
     const GbfvPlan& p = b->scheme;
     const BatchLauncher launch = R.batch[p.var][p.eq][p.fl][p.rc][b->dim - 1];
+    if (!launch) return bfail(GBFV_ERR_UNSUPPORTED, "no ensemble kernel for this scheme and precision");
     BatchArgs a;
     a.members = b->d_members;
     a.states = b->d_states;

@@ -53,8 +53,8 @@ int fv_get_threads(void) {
 /* ------------------------------------------------------------------ names */
 
 enum { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3 };
-enum { FL_HLL, FL_HLL3, FL_GODUNOV };
-enum { RC_NONE, RC_WENO2, RC_ENO2, RC_ENO3, RC_ENO4 };
+enum { FL_HLL, FL_HLL3, FL_GODUNOV, FL_CENTRAL, FL_RUSANOV, FL_ROE };
+enum { RC_NONE, RC_WENO2, RC_ENO2, RC_ENO3, RC_ENO4, RC_MC, RC_MM };
 enum { IN_FE, IN_RK2, IN_RK3 };
 enum { BC_NEUMANN, BC_PERIODIC };
 
@@ -69,6 +69,9 @@ static int parse_flux(const char* s) {
     if (!strcmp(s, "hll")) return FL_HLL;
     if (!strcmp(s, "hll3")) return FL_HLL3;
     if (!strcmp(s, "godunov")) return FL_GODUNOV;
+    if (!strcmp(s, "central")) return FL_CENTRAL;
+    if (!strcmp(s, "rusanov")) return FL_RUSANOV;
+    if (!strcmp(s, "roe")) return FL_ROE;
     return -1;
 }
 static int parse_recon(const char* s) {
@@ -77,6 +80,8 @@ static int parse_recon(const char* s) {
     if (!strcmp(s, "eno2")) return RC_ENO2;
     if (!strcmp(s, "eno3")) return RC_ENO3;
     if (!strcmp(s, "eno4")) return RC_ENO4;
+    if (!strcmp(s, "mc")) return RC_MC;
+    if (!strcmp(s, "mm")) return RC_MM;
     return -1;
 }
 static int parse_integrator(const char* s) {
@@ -94,6 +99,13 @@ static int parse_bc(const char* s) {
 /* Reconstruction ghost width: none 1, weno2 2, enoK K
  * (alsfvm/src/reconstruction/NoReconstruction.cpp:71-73, WENO2.hpp:93-95,
  * ENOCPU.cpp:180-183); the two-point flux stencil needs 1. */
+/* numerical_flux_list.hpp:41-113: Euler takes hll, hll3, central; Burgers
+ * takes godunov, central, rusanov, roe */
+static int flux_applies(int eq, int fl) {
+    if (eq == EQ_BURGERS) return fl == FL_GODUNOV || fl == FL_CENTRAL || fl == FL_RUSANOV || fl == FL_ROE;
+    return fl == FL_HLL || fl == FL_HLL3 || fl == FL_CENTRAL;
+}
+
 static int recon_ghosts(int rc) {
     switch (rc) {
         case RC_NONE: return 1;
@@ -101,6 +113,8 @@ static int recon_ghosts(int rc) {
         case RC_ENO2: return 2;
         case RC_ENO3: return 3;
         case RC_ENO4: return 4;
+        case RC_MC: return 2;
+        case RC_MM: return 2;
     }
     return -1;
 }
@@ -274,7 +288,54 @@ static double flux_godunov(double uL, double uR, double* F) {
     return fmax(fabs(uL), fabs(uR));
 }
 
+/* Central<Euler<nsd>>: F = 0.5 (f(L) + f(R)); wave speed max over the two
+ * states of |u_d| + sqrt(gamma p / rho) (alsfvm/include/alsfvm/numflux/
+ * Central.hpp:31-55, Euler.hpp:251-258). */
+static double flux_central_euler(const euler_all* L, const euler_all* R, int d, int nsd, double gamma,
+                                 double* F) {
+    double fl[5], fr[5];
+    euler_point_flux(L, d, nsd, fl);
+    euler_point_flux(R, d, nsd, fr);
+    for (int k = 0; k < nsd + 2; ++k) F[k] = 0.5 * (fl[k] + fr[k]);
+    const double wl = fabs(L->u[d]) + sqrt(gamma * L->p / L->rho);
+    const double wr = fabs(R->u[d]) + sqrt(gamma * R->p / R->rho);
+    return fmax(wl, wr);
+}
+
+/* Central<Burgers>, Rusanov<Burgers> (eigenvalue u: Burgers.hpp:298-301) and
+ * burgers::Roe (alsfvm/include/alsfvm/numflux/Rusanov.hpp:31-59,
+ * alsfvm/include/alsfvm/numflux/burgers/Roe.hpp:30-58); f(u) = u u / 2. */
+static double flux_burgers(int fl, double uL, double uR, double* F) {
+    const double fL = uL * uL / 2, fR = uR * uR / 2;
+    if (fl == FL_CENTRAL) {
+        F[0] = 0.5 * (fL + fR);
+    } else if (fl == FL_RUSANOV) {
+        const double eigenMax = fmax(fabs(uL), fabs(uR));
+        F[0] = 0.5 * (fL + fR) - 0.5 * eigenMax * (uR - uL);
+    } else {
+        if (uL >= -uR) {
+            const double a = fmax(uL, 0.0);
+            F[0] = a * a / 2;
+        } else {
+            const double b = fmin(uR, 0.0);
+            F[0] = b * b / 2;
+        }
+    }
+    return fmax(fabs(uL), fabs(uR));
+}
+
 /* -------------------------------------------------------- reconstruction */
+
+/* sign and minmod (alsfvm/include/alsfvm/reconstruction/sign.hpp,
+ * minmod.hpp): sign is 1, 0 or -1 (-1 for NaN). */
+static double sign_of(double a) { return a > 0 ? 1.0 : (a == 0 ? 0.0 : -1.0); }
+static double minmod2(double a, double b) {
+    return sign_of(a) == sign_of(b) ? sign_of(a) * fmin(fabs(a), fabs(b)) : 0.0;
+}
+static double minmod3(double a, double b, double c) {
+    return (sign_of(a) == sign_of(b) && sign_of(b) == sign_of(c)) ? sign_of(a) * fmin(fabs(a), fmin(fabs(b), fabs(c)))
+                                                                  : 0.0;
+}
 
 /* ENO reconstruction coefficients, row r gives the value at the cell's
  * left face for stencil shift r (row r+1 the right face); the standard
@@ -324,7 +385,18 @@ static void reconstruct(const grid_t* G, int rc, int dir, const double* U, doubl
         for (int y = lo[1]; y < hi[1]; ++y) {
             for (int x = lo[0]; x < hi[0]; ++x) {
                 const long i = IDX(G, x, y, z);
-                if (rc == RC_WENO2) {
+                if (rc == RC_MC || rc == RC_MM) {
+                    /* MC / MM slope limiters on every variable
+                     * (alsfvm/include/alsfvm/reconstruction/MC.hpp:27-52, MM.hpp:25-47) */
+                    for (int v = 0; v < nvar; ++v) {
+                        const double* u = U + v * total;
+                        const double l = u[i - stride], m = u[i], r = u[i + stride];
+                        const double sigma = rc == RC_MC ? minmod3(2 * (r - m), (r - l) / 2, 2 * (m - l))
+                                                         : minmod2(r - m, m - l);
+                        left[v * total + i] = m - sigma / 2;
+                        right[v * total + i] = m + sigma / 2;
+                    }
+                } else if (rc == RC_WENO2) {
                     /* WENO2::reconstruct (alsfvm/include/alsfvm/reconstruction/WENO2.hpp:31-91) */
                     const long il = i - stride, ir = i + stride;
                     const double i0 = U[i];
@@ -425,13 +497,15 @@ static double net_flux(const grid_t* G, int fl, int dir, const double* left, con
                 double F[5];
                 double wl;
                 if (G->eq == EQ_BURGERS) {
-                    wl = flux_godunov(right[i], left[i + stride], F);
+                    wl = fl == FL_GODUNOV ? flux_godunov(right[i], left[i + stride], F)
+                                          : flux_burgers(fl, right[i], left[i + stride], F);
                 } else {
                     euler_all A, B;
                     euler_fetch(&A, right, total, i, nsd, G->gamma);
                     euler_fetch(&B, left, total, i + stride, nsd, G->gamma);
                     wl = fl == FL_HLL3 ? flux_hll3(&A, &B, dir, nsd, G->gamma, F)
-                                       : flux_hll(&A, &B, dir, nsd, G->gamma, F);
+                         : fl == FL_HLL ? flux_hll(&A, &B, dir, nsd, G->gamma, F)
+                                        : flux_central_euler(&A, &B, dir, nsd, G->gamma, F);
                 }
                 for (int v = 0; v < nvar; ++v) temp[v * total + i] = (-1.0) * F[v];
                 wsz = (wsz < wl) ? wl : wsz; /* std::max */
@@ -504,7 +578,7 @@ int fv_compute_flux(const char* equation, const char* flux, const char* recon, c
                     double gamma, const double* U, double* out, double ws[3]) {
     const int eq = parse_eq(equation), fl = parse_flux(flux), rc = parse_recon(recon);
     if (eq < 0 || fl < 0 || rc < 0) return fail(-1, "bad equation/flux/reconstruction");
-    if ((eq == EQ_BURGERS) != (fl == FL_GODUNOV)) return fail(-1, "flux %s not for %s", flux, equation);
+    if (!flux_applies(eq, fl)) return fail(-1, "flux %s not for %s", flux, equation);
     flux_ctx c;
     int r = flux_ctx_init(&c, eq, fl, rc, n, gamma);
     if (r == 0) compute_flux(&c, U, out, ws);
@@ -639,6 +713,7 @@ int fv_run(const char* equation, const char* flux, const char* recon, const char
     const int eq = parse_eq(equation), fl = parse_flux(flux), rc = parse_recon(recon);
     const int in = parse_integrator(integrator), bc = parse_bc(boundary);
     if (eq < 0 || fl < 0 || rc < 0 || in < 0 || bc < 0) return fail(-1, "bad configuration name");
+    if (!flux_applies(eq, fl)) return fail(-1, "flux %s not for %s", flux, equation);
     flux_ctx c;
     int r = flux_ctx_init(&c, eq, fl, rc, n, gamma);
     if (r) { flux_ctx_free(&c); return r; }

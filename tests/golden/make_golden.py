@@ -69,6 +69,39 @@ def flux_cases():
     np.savez_compressed(os.path.join(HERE, "flux.npz"), **out)
 
 
+def extra_flux_combinations():
+    """(equation, flux, reconstruction) pairs beyond the base set: the extra
+    fluxes with every reconstruction, the limiters with every base flux."""
+    out = []
+    for eq in ("euler1", "euler2", "euler3", "burgers"):
+        for fl in workloads.EXTRA_FLUXES[eq]:
+            for rc in workloads.RECONSTRUCTIONS + workloads.LIMITER_RECONSTRUCTIONS:
+                out.append((eq, fl, rc))
+        for fl in workloads.BASE_FLUXES[eq]:
+            for rc in workloads.LIMITER_RECONSTRUCTIONS:
+                out.append((eq, fl, rc))
+    return out
+
+
+def flux_extra_cases():
+    rng = np.random.default_rng(20240602)
+    out = {}
+    grids = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
+    for eq, fl, rc in extra_flux_combinations():
+        n = grids[eq]
+        g = workloads.ghost_cells(rc)
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        o = np.zeros_like(U)
+        ws = (D * 3)()
+        check(R.ref_compute_flux(eq.encode(), fl.encode(), rc.encode(), i3(n), D(1.4), P(U), P(o), ws))
+        key = f"{eq}_{fl}_{rc}"
+        out[key + "_U"] = U
+        out[key + "_L"] = o
+        out[key + "_ws"] = np.array(list(ws))
+    np.savez_compressed(os.path.join(HERE, "flux_extra.npz"), **out)
+
+
 def boundary_cases():
     out = {}
     for bc in ("neumann", "periodic"):
@@ -171,6 +204,7 @@ elif __name__ == "__main__":
     generator_cases()
     generator_sequence_cases()
     flux_cases()
+    flux_extra_cases()
     boundary_cases()
     meanvar_cases()
     run_cases()

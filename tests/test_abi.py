@@ -26,7 +26,8 @@ def test_library_exports_every_declared_function():
 
 
 def test_ghost_cells_and_variables():
-    assert [lib.ghost_cells(r) for r in ("none", "weno2", "eno2", "eno3", "eno4")] == [1, 2, 2, 3, 4]
+    assert [lib.ghost_cells(r) for r in ("none", "weno2", "eno2", "eno3", "eno4", "mc", "mm")] == \
+        [1, 2, 2, 3, 4, 2, 2]
     assert [lib.num_variables(e) for e in ("burgers", "euler1", "euler2", "euler3")] == [1, 3, 4, 5]
     with pytest.raises(lib.GbfvError):
         lib.ghost_cells("weno9")
@@ -69,7 +70,7 @@ def test_generator_scaling():
     assert np.array_equal(b, a * 7.0 + -2.0)
 
 
-@pytest.mark.parametrize("field,value", [("equation", "euler4"), ("flux", "roe"), ("reconstruction", "weno9"),
+@pytest.mark.parametrize("field,value", [("equation", "euler4"), ("flux", "tecno1"), ("reconstruction", "weno9"),
                                          ("integrator", "rungekutta4"), ("boundary", "reflective")])
 def test_create_rejects_unknown_names(field, value):
     kw = dict(equation="euler2", flux="hll3", reconstruction="weno2", integrator="rungekutta3",
@@ -90,6 +91,11 @@ def test_create_rejects_mismatched_combinations():
     with pytest.raises(lib.GbfvError) as e:
         lib.Solver("euler1", "hll3", "eno4", "rungekutta3", "periodic", (3, 1, 1), (0, 0, 0), (1, 1, 1))
     assert e.value.code == lib.ERR_UNSUPPORTED
+    # rusanov and roe are Burgers fluxes (numerical_flux_list.hpp)
+    for flux in ("rusanov", "roe"):
+        with pytest.raises(lib.GbfvError) as e:
+            lib.Solver("euler1", flux, "mc", "rungekutta3", "periodic", (8, 1, 1), (0, 0, 0), (1, 1, 1))
+        assert e.value.code == lib.ERR_UNSUPPORTED
 
 
 def test_initial_data_matches_the_workload_formulas():

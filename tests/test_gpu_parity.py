@@ -54,14 +54,25 @@ def solver(eq, flux, recon, n, precision, integrator="rungekutta3", boundary="pe
 
 
 def flux_keys():
-    z = np.load(os.path.join(GOLDEN, "flux.npz"))
-    return sorted({k.rsplit("_", 1)[0] for k in z.files})
+    """(fixture file, key) pairs. The double-float variant covers the base
+    schemes only (flux.npz)."""
+    out = []
+    for name in ("flux.npz", "flux_extra.npz"):
+        z = np.load(os.path.join(GOLDEN, name))
+        out += [(name, k) for k in sorted({k.rsplit("_", 1)[0] for k in z.files})]
+    return out
 
 
 @pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP64_DF, lib.FP32])
-@pytest.mark.parametrize("key", flux_keys())
-def test_compute_flux_matches_reference(cuda_device, key, precision):
-    z = np.load(os.path.join(GOLDEN, "flux.npz"))
+@pytest.mark.parametrize("name,key", flux_keys())
+def test_compute_flux_matches_reference(cuda_device, name, key, precision):
+    if precision == lib.FP64_DF and name != "flux.npz":
+        with pytest.raises(lib.GbfvError) as e:
+            eq, fl, rc = key.split("_")
+            solver(eq, fl, rc, FLUX_GRIDS[eq], precision)
+        assert e.value.code == lib.ERR_UNSUPPORTED
+        return
+    z = np.load(os.path.join(GOLDEN, name))
     eq, fl, rc = key.split("_")
     n = FLUX_GRIDS[eq]
     g = workloads.ghost_cells(rc)
@@ -185,6 +196,66 @@ LARGE = {
                               cfl=0.4, end_time=0.2, number_of_saves=2, max_steps=0,
                               prim=lambda: np.sin(np.arange(40 * 33) * 0.05).reshape(1, -1)),
 }
+
+
+# runs with the extra fluxes and the limiter reconstructions
+EXTRA_RUNS = {
+    "burgers_rusanov_mc_rk2": dict(equation="burgers", flux="rusanov", recon="mc", integrator="rungekutta2",
+                                   boundary="periodic", n=(256, 1, 1), lower=(0, 0, 0), upper=(1, 1, 1), gamma=1.4,
+                                   cfl=0.45, end_time=0.4, number_of_saves=1, max_steps=0,
+                                   prim=lambda: workloads.burgers_prim(256, 0.1)),
+    "burgers2d_roe_mm_fe": dict(equation="burgers", flux="roe", recon="mm", integrator="forwardeuler",
+                                boundary="neumann", n=(40, 33, 1), lower=(0, 0, 0), upper=(1, 1, 1), gamma=1.4,
+                                cfl=0.4, end_time=0.2, number_of_saves=2, max_steps=0,
+                                prim=lambda: np.sin(np.arange(40 * 33) * 0.05).reshape(1, -1)),
+    "burgers_central_weno2_rk3": dict(equation="burgers", flux="central", recon="weno2", integrator="rungekutta3",
+                                      boundary="periodic", n=(128, 1, 1), lower=(0, 0, 0), upper=(1, 1, 1),
+                                      gamma=1.4, cfl=0.3, end_time=0.05, number_of_saves=0, max_steps=0,
+                                      prim=lambda: workloads.burgers_prim(128, 0.3)),
+    # the central flux has no upwinding: a smooth density wave (a shock
+    # would oscillate into negative pressure, as it does in the reference)
+    "wave_central_mc_rk3": dict(equation="euler1", flux="central", recon="mc", integrator="rungekutta3",
+                                boundary="periodic", n=(256, 1, 1), lower=(0, 0, 0), upper=(1, 1, 1), gamma=1.4,
+                                cfl=0.4, end_time=1.0, number_of_saves=0, max_steps=40,
+                                prim=lambda: np.stack([1 + 0.2 * np.sin(2 * np.pi * (np.arange(256) + 0.5) / 256),
+                                                       np.full(256, 0.5), np.ones(256)])),
+    "kh_hll3_mm_rk2": dict(equation="euler2", flux="hll3", recon="mm", integrator="rungekutta2",
+                           boundary="periodic", n=(64, 48, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4, cfl=0.4,
+                           end_time=2.0, number_of_saves=0, max_steps=30,
+                           prim=lambda: workloads.kh_prim(64, lib.uniform(40, 2))[:, :64 * 48]),
+    "kh_central_mc_rk3": dict(equation="euler2", flux="central", recon="mc", integrator="rungekutta3",
+                              boundary="periodic", n=(48, 48, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4,
+                              cfl=0.3, end_time=2.0, number_of_saves=0, max_steps=20,
+                              prim=lambda: workloads.kh_prim(48, lib.uniform(40, 4))),
+    "tg_hll_mc_rk3": dict(equation="euler3", flux="hll", recon="mc", integrator="rungekutta3", boundary="periodic",
+                          n=(12, 12, 12), lower=(0, 0, 0), upper=(2 * math.pi,) * 3, gamma=1.4, cfl=0.4,
+                          end_time=100.0, number_of_saves=0, max_steps=8, prim=lambda: workloads.tg_prim(12)),
+}
+
+
+@pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP32])
+@pytest.mark.parametrize("name", sorted(EXTRA_RUNS))
+def test_extra_scheme_runs_match_oracle(cuda_device, name, precision):
+    case = EXTRA_RUNS[name]
+    g = workloads.ghost_cells(case["recon"])
+    prim = case["prim"]()
+    rc, ref, ref_t, ref_steps = fvoracle.run(case["equation"], case["flux"], case["recon"], case["integrator"],
+                                             case["boundary"], case["n"], case["lower"], case["upper"],
+                                             case["gamma"], case["cfl"], case["end_time"],
+                                             case["number_of_saves"], case["max_steps"], prim, g,
+                                             workloads.NVAR[case["equation"]])
+    assert rc == 0
+    U, t, steps = run_gpu(case, precision, prim=prim)
+    if precision == lib.FP64_EXACT:
+        assert (steps, t) == (ref_steps, ref_t)
+        assert np.array_equal(U, ref)
+    elif precision == lib.FP64:
+        assert steps == ref_steps
+        err = rel_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+        assert (err <= 1e-10).all(), err
+    else:
+        err = scaled_l1(interior(U, case["n"], g), interior(ref, case["n"], g))
+        assert (err <= 1e-4).all(), err
 
 
 @pytest.mark.parametrize("precision", [lib.FP64_EXACT, lib.FP64, lib.FP64_DF])

@@ -19,13 +19,18 @@ FLUX_GRIDS = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "
 
 
 def flux_keys():
-    z = load("flux.npz")
-    return sorted({k.rsplit("_", 1)[0] for k in z.files})
+    """(fixture file, equation_flux_reconstruction) pairs: the base schemes
+    and the extra fluxes / limiter reconstructions."""
+    out = []
+    for name in ("flux.npz", "flux_extra.npz"):
+        z = load(name)
+        out += [(name, k) for k in sorted({k.rsplit("_", 1)[0] for k in z.files})]
+    return out
 
 
-@pytest.mark.parametrize("key", flux_keys())
-def test_flux_matches_reference(key):
-    z = load("flux.npz")
+@pytest.mark.parametrize("name,key", flux_keys())
+def test_flux_matches_reference(name, key):
+    z = load(name)
     eq, fl, rc = key.split("_")
     out, ws = fvoracle.compute_flux(eq, fl, rc, FLUX_GRIDS[eq], 1.4, z[key + "_U"])
     assert np.isfinite(out).all()
