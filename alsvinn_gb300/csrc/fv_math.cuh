@@ -497,6 +497,7 @@ template <> struct ReconTraits<RC_ENO3> { static constexpr int ghosts = 3; stati
 template <> struct ReconTraits<RC_ENO4> { static constexpr int ghosts = 4; static constexpr int reach = 3; };
 template <> struct ReconTraits<RC_MC> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
 template <> struct ReconTraits<RC_MM> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
+template <> struct ReconTraits<RC_WENOF2> { static constexpr int ghosts = 2; static constexpr int reach = 1; };
 
 // ENO coefficient rows (alsfvm/src/reconstruction/ENOCoefficients.cpp:21-49):
 // row r weights the stencil starting r cells to the left for the value at the
@@ -544,11 +545,85 @@ template <> __device__ __forceinline__ bool abs_less<double>(double a, double b)
 // store: variable k sits at u[k * vs], neighbour j along the direction at
 // u[j * ds]. Variable 0 is the WENO weight / ENO indicator (rho for Euler,
 // u for Burgers: Euler.hpp:286-288).
+// WENOF2<Euler<nsd>>::reconstruct (alsfvm/include/alsfvm/reconstruction/
+// WENOF2.hpp:31-112): the WENO2 weights of the density applied to the
+// primitive variables (rho, u, p) of the three cells, the density and
+// pressure increments bounded by 1.9 times the cell's values, the increment
+// scaled by aijk = sqrt(R / max(R, LL)) / 2 (R = p / (gamma - 1), LL a
+// kinetic-energy bound), then back to conserved variables
+// (Euler::computeConserved, Euler.hpp:236-245). The reference's operand
+// order throughout; vector dot products accumulate x, y, z in order.
+template <class R, int NSD>
+__device__ __forceinline__ void wenof2_prim(const R* c, int vs, R gamma, R* q) {
+    const R rho = c[0];
+    R dot = c[vs] * c[vs];
+#pragma unroll
+    for (int k = 0; k < NSD; ++k) q[1 + k] = c[(1 + k) * vs] / rho;
+#pragma unroll
+    for (int k = 1; k < NSD; ++k) dot = dot + c[(1 + k) * vs] * c[(1 + k) * vs];
+    const R ie = c[(1 + NSD) * vs] - R(0.5) * dot / rho;
+    q[0] = rho;
+    q[1 + NSD] = (gamma - R(1)) * ie;
+}
+
+template <class R, int NSD>
+__device__ __forceinline__ R dot_n(const R* a, const R* b) {
+    R d = a[0] * b[0];
+#pragma unroll
+    for (int k = 1; k < NSD; ++k) d = d + a[k] * b[k];
+    return d;
+}
+
+template <class R, int NSD, int SIDE>
+__device__ __forceinline__ void wenof2_side(const R* L, const R* M, const R* Rr, R w0, R w1, R gamma, R* out) {
+    constexpr int NV = NSD + 2;
+    const R BOUND = R(1.9);
+    R d[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) d[c] = w1 * (M[c] - L[c]) + w0 * (Rr[c] - M[c]);
+    d[0] = fmax(-BOUND * M[0], fmin(BOUND * M[0], d[0]));
+    d[NV - 1] = fmax(-BOUND * M[NV - 1], fmin(BOUND * M[NV - 1], d[NV - 1]));
+    const R dd = dot_n<R, NSD>(d + 1, d + 1);
+    const R LL = R(0.125) * M[0] * dd - R(0.5) * fmin(R(0), d[0] * dot_n<R, NSD>(M + 1, d + 1)) +
+                 R(0.5) * d[0] * d[0] * dd / M[0];
+    const R Rp = M[NV - 1] / (gamma - R(1));
+    const R a = R(0.5) * sqrt(Rp / fmax(Rp, LL));
+    R q[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) q[c] = SIDE < 0 ? M[c] - a * d[c] : M[c] + a * d[c];
+    out[0] = q[0];
+#pragma unroll
+    for (int k = 0; k < NSD; ++k) out[1 + k] = q[0] * q[1 + k];
+    out[1 + NSD] = q[NV - 1] / (gamma - R(1)) + R(0.5) * q[0] * dot_n<R, NSD>(q + 1, q + 1);
+}
+
 template <class R, int NV, int RC>
-__device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs, int ds, R* left, R* right) {
+__device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs, int ds, R* left, R* right,
+                                                 R gamma = R(1.4)) {
     if constexpr (RC == RC_NONE) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) left[k] = right[k] = u[k * vs];
+    } else if constexpr (RC == RC_WENOF2) {
+        constexpr int NSD = NV - 2;
+        static_assert(NSD >= 1, "WENOF2 reconstructs the Euler equations only");
+        const R i0 = u[0];
+        const R b0 = (u[ds] - i0) * (u[ds] - i0);
+        const R b1 = (i0 - u[-ds]) * (i0 - u[-ds]);
+        const R eps = R(FV_WENO_EPSILON);
+        const R a0Left = R(1) / (R(3) * (eps + b0) * (eps + b0));
+        const R a1Left = R(2) / (R(3) * (eps + b1) * (eps + b1));
+        const R w0Left = a0Left / (a0Left + a1Left);
+        const R w1Left = a1Left / (a0Left + a1Left);
+        const R a0Right = R(2) / (R(3) * (eps + b0) * (eps + b0));
+        const R a1Right = R(1) / (R(3) * (eps + b1) * (eps + b1));
+        const R w0Right = a0Right / (a0Right + a1Right);
+        const R w1Right = a1Right / (a0Right + a1Right);
+        R pl[NV], pm[NV], pr[NV];
+        wenof2_prim<R, NSD>(u - ds, vs, gamma, pl);
+        wenof2_prim<R, NSD>(u, vs, gamma, pm);
+        wenof2_prim<R, NSD>(u + ds, vs, gamma, pr);
+        wenof2_side<R, NSD, -1>(pl, pm, pr, w0Left, w1Left, gamma, left);
+        wenof2_side<R, NSD, 1>(pl, pm, pr, w0Right, w1Right, gamma, right);
     } else if constexpr (RC == RC_MC || RC == RC_MM) {
         // MC / MM slope limiters on every variable (alsfvm/include/alsfvm/
         // reconstruction/MC.hpp:27-52, MM.hpp:25-47)

@@ -11,7 +11,7 @@ namespace gbfv {
 enum Variant { VAR_F64 = 0, VAR_F64_EXACT = 1, VAR_F32 = 2, VAR_F64_DF = 3, NUM_VARIANTS = 4 };
 enum Equation { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3, NUM_EQ = 4 };
 enum Flux { FL_HLL = 0, FL_HLL3 = 1, FL_GODUNOV = 2, FL_CENTRAL = 3, FL_RUSANOV = 4, FL_ROE = 5, NUM_FLUX = 6 };
-constexpr int NUM_RECON = 7;
+constexpr int NUM_RECON = 8;
 
 // The fluxes each equation offers (alsfvm/include/alsfvm/numflux/
 // numerical_flux_list.hpp:41-113): Euler hll, hll3, central; Burgers

@@ -160,7 +160,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         else { c[0] = p; c[1] = q; }
         const int s = ((c[2] + SL::GZ) * SL::HY + (c[1] + SL::GY)) * SL::HX + (c[0] + SL::GX);
         R l[NV], r[NV];
-        reconstruct_cell<R, NV, RC>(su + s, VS, DS, l, r);
+        reconstruct_cell<R, NV, RC>(su + s, VS, DS, l, r, gamma);
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             rl[k * NREC + w] = l[k];

@@ -5,7 +5,7 @@
 
 namespace gbfv {
 
-enum Recon { RC_NONE = 0, RC_WENO2 = 1, RC_ENO2 = 2, RC_ENO3 = 3, RC_ENO4 = 4, RC_MC = 5, RC_MM = 6 };
+enum Recon { RC_NONE = 0, RC_WENO2 = 1, RC_ENO2 = 2, RC_ENO3 = 3, RC_ENO4 = 4, RC_MC = 5, RC_MM = 6, RC_WENOF2 = 7 };
 
 enum Mode { MODE_L = 0, MODE_RK3_S1 = 1, MODE_RK3_S2 = 2, MODE_RK2_S1 = 3 };
 
@@ -153,6 +153,7 @@ struct ReconArgs {
     void* right;
     Grid G;
     int dir;
+    double gamma;  // for reconstructions in primitive variables
 };
 
 // Constraint check over every padded cell (ghosts included, as the reference

@@ -108,7 +108,7 @@ __global__ void recon_kernel(ReconArgs A) {
     const int ds = d == 0 ? 1 : (d == 1 ? G.t[0] : G.t[0] * G.t[1]);
     const Real* in = reinterpret_cast<const Real*>(A.in);
     Real l[NV], r[NV];
-    reconstruct_cell<Real, NV, RC>(in + gi, (int)G.total, ds, l, r);
+    reconstruct_cell<Real, NV, RC>(in + gi, (int)G.total, ds, l, r, (Real)A.gamma);
     Real* L = reinterpret_cast<Real*>(A.left);
     Real* Rr = reinterpret_cast<Real*>(A.right);
     for (int k = 0; k < NV; ++k) {
@@ -167,6 +167,9 @@ static void reg_dim(Registry& R) {
 #if FV_VARIANT != 3
     reg_one<FLUX, RC_MC, DIM>(R);
     reg_one<FLUX, RC_MM, DIM>(R);
+#if FV_EQ != 0
+    reg_one<FLUX, RC_WENOF2, DIM>(R);
+#endif
 #endif
 }
 
@@ -208,4 +211,7 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     R->recon[V][E][RC_ENO4] = &launch_recon<E, RC_ENO4>;
     R->recon[V][E][RC_MC] = &launch_recon<E, RC_MC>;
     R->recon[V][E][RC_MM] = &launch_recon<E, RC_MM>;
+#if FV_EQ != 0
+    R->recon[V][E][RC_WENOF2] = &launch_recon<E, RC_WENOF2>;
+#endif
 }

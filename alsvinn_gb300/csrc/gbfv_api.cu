@@ -187,6 +187,7 @@ static int parse_recon(const char* s) {
     if (!strcmp(s, "eno4")) return RC_ENO4;
     if (!strcmp(s, "mc")) return RC_MC;
     if (!strcmp(s, "mm")) return RC_MM;
+    if (!strcmp(s, "wenof2")) return RC_WENOF2;
     return -1;
 }
 enum { IN_FE = 0, IN_RK2 = 1, IN_RK3 = 2 };
@@ -203,7 +204,7 @@ static int parse_bc(const char* s) {
     if (!strcmp(s, "periodic")) return 1;
     return -1;
 }
-static const int kReconGhosts[7] = {1, 2, 2, 3, 4, 2, 2};
+static const int kReconGhosts[8] = {1, 2, 2, 3, 4, 2, 2, 2};
 
 // ---------------------------------------------------------------- solver
 
@@ -692,6 +693,7 @@ int gbfv_reconstruct(gbfv_solver* s, int direction, const void* U, void* left, v
     a.right = right;
     a.G = s->G;
     a.dir = direction;
+    a.gamma = s->gamma;
     LAUNCH_TRY(registry().recon[s->var][s->eq][s->rc](a, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return GBFV_OK;

@@ -54,7 +54,7 @@ int fv_get_threads(void) {
 
 enum { EQ_BURGERS = 0, EQ_EULER1 = 1, EQ_EULER2 = 2, EQ_EULER3 = 3 };
 enum { FL_HLL, FL_HLL3, FL_GODUNOV, FL_CENTRAL, FL_RUSANOV, FL_ROE };
-enum { RC_NONE, RC_WENO2, RC_ENO2, RC_ENO3, RC_ENO4, RC_MC, RC_MM };
+enum { RC_NONE, RC_WENO2, RC_ENO2, RC_ENO3, RC_ENO4, RC_MC, RC_MM, RC_WENOF2 };
 enum { IN_FE, IN_RK2, IN_RK3 };
 enum { BC_NEUMANN, BC_PERIODIC };
 
@@ -82,6 +82,7 @@ static int parse_recon(const char* s) {
     if (!strcmp(s, "eno4")) return RC_ENO4;
     if (!strcmp(s, "mc")) return RC_MC;
     if (!strcmp(s, "mm")) return RC_MM;
+    if (!strcmp(s, "wenof2")) return RC_WENOF2;
     return -1;
 }
 static int parse_integrator(const char* s) {
@@ -115,6 +116,7 @@ static int recon_ghosts(int rc) {
         case RC_ENO4: return 4;
         case RC_MC: return 2;
         case RC_MM: return 2;
+        case RC_WENOF2: return 2;
     }
     return -1;
 }
@@ -357,6 +359,91 @@ static const double ENO4C[5][4] = {{25.0 / 12.0, -23.0 / 12.0, 13.0 / 12.0, -1.0
  * the other directions (ReconstructionCPU.cpp:37-97, ENOCPU.cpp:41-171). The
  * weight / stencil-indicator variable is variable 0 (rho for Euler, u for
  * Burgers: Euler.hpp:286-288, Burgers.hpp:225-227). */
+/* WENOF2<Euler<nsd>>::reconstruct (alsfvm/include/alsfvm/reconstruction/
+ * WENOF2.hpp:31-112): WENO2 weights from rho, applied to the primitive
+ * variables (rho, u, p); the rho and p increments bounded by 1.9 times the
+ * cell's value; the increment scaled by aijk = sqrt(R / max(R, LL)) / 2 with
+ * R = p / (gamma - 1) and LL a kinetic-energy bound; back to conserved
+ * variables with Euler::computeConserved (Euler.hpp:236-245). Vector dot
+ * products accumulate x, y, z in order. */
+typedef struct { double rho, u[3], p; } prim_t;
+
+static prim_t to_prim(const double* U, long total, long i, int nsd, double gamma) {
+    prim_t q;
+    const double rho = U[i];
+    double m[3], dot = 0;
+    for (int k = 0; k < nsd; ++k) m[k] = U[(1 + k) * total + i];
+    for (int k = 0; k < nsd; ++k) q.u[k] = m[k] / rho;
+    dot = m[0] * m[0];
+    for (int k = 1; k < nsd; ++k) dot = dot + m[k] * m[k];
+    const double ie = U[(1 + nsd) * total + i] - 0.5 * dot / rho;
+    q.rho = rho;
+    q.p = (gamma - 1) * ie;
+    return q;
+}
+
+static double dot_n(const double* a, const double* b, int nsd) {
+    double d = a[0] * b[0];
+    for (int k = 1; k < nsd; ++k) d = d + a[k] * b[k];
+    return d;
+}
+
+static void wenof2_side(const prim_t* L, const prim_t* M, const prim_t* R, double w0, double w1, int sgn, int nsd,
+                        double gamma, double* out) {
+    const double BOUND = 1.9;
+    prim_t d;
+    d.rho = w1 * (M->rho - L->rho) + w0 * (R->rho - M->rho);
+    for (int k = 0; k < nsd; ++k) d.u[k] = w1 * (M->u[k] - L->u[k]) + w0 * (R->u[k] - M->u[k]);
+    d.p = w1 * (M->p - L->p) + w0 * (R->p - M->p);
+    d.rho = fmax(-BOUND * M->rho, fmin(BOUND * M->rho, d.rho));
+    d.p = fmax(-BOUND * M->p, fmin(BOUND * M->p, d.p));
+    const double dd = dot_n(d.u, d.u, nsd);
+    const double LL = 0.125 * M->rho * dd - 0.5 * fmin(0.0, d.rho * dot_n(M->u, d.u, nsd)) +
+                      0.5 * d.rho * d.rho * dd / M->rho;
+    const double Rr = M->p / (gamma - 1);
+    const double a = 0.5 * sqrt(Rr / fmax(Rr, LL));
+    prim_t q;
+    if (sgn < 0) {
+        q.rho = M->rho - a * d.rho;
+        for (int k = 0; k < nsd; ++k) q.u[k] = M->u[k] - a * d.u[k];
+        q.p = M->p - a * d.p;
+    } else {
+        q.rho = M->rho + a * d.rho;
+        for (int k = 0; k < nsd; ++k) q.u[k] = M->u[k] + a * d.u[k];
+        q.p = M->p + a * d.p;
+    }
+    out[0] = q.rho;
+    for (int k = 0; k < nsd; ++k) out[1 + k] = q.rho * q.u[k];
+    out[1 + nsd] = q.p / (gamma - 1) + 0.5 * q.rho * dot_n(q.u, q.u, nsd);
+}
+
+static void wenof2_cell(const grid_t* G, const double* U, long i, long stride, double* left, double* right) {
+    const long total = G->total;
+    const int nsd = G->nsd;
+    const long il = i - stride, ir = i + stride;
+    const double i0 = U[i];
+    const double b0 = (U[ir] - i0) * (U[ir] - i0);
+    const double b1 = (i0 - U[il]) * (i0 - U[il]);
+    const double a0Left = 1 / (3 * (WENO_EPSILON + b0) * (WENO_EPSILON + b0));
+    const double a1Left = 2 / (3 * (WENO_EPSILON + b1) * (WENO_EPSILON + b1));
+    const double w0Left = a0Left / (a0Left + a1Left);
+    const double w1Left = a1Left / (a0Left + a1Left);
+    const double a0Right = 2 / (3 * (WENO_EPSILON + b0) * (WENO_EPSILON + b0));
+    const double a1Right = 1 / (3 * (WENO_EPSILON + b1) * (WENO_EPSILON + b1));
+    const double w0Right = a0Right / (a0Right + a1Right);
+    const double w1Right = a1Right / (a0Right + a1Right);
+    const prim_t L = to_prim(U, total, il, nsd, G->gamma);
+    const prim_t M = to_prim(U, total, i, nsd, G->gamma);
+    const prim_t R = to_prim(U, total, ir, nsd, G->gamma);
+    double l[5], r[5];
+    wenof2_side(&L, &M, &R, w0Left, w1Left, -1, nsd, G->gamma, l);
+    wenof2_side(&L, &M, &R, w0Right, w1Right, +1, nsd, G->gamma, r);
+    for (int v = 0; v < nsd + 2; ++v) {
+        left[v * total + i] = l[v];
+        right[v * total + i] = r[v];
+    }
+}
+
 static void reconstruct(const grid_t* G, int rc, int dir, const double* U, double* left,
                         double* right) {
     const long total = G->total;
@@ -385,7 +472,9 @@ static void reconstruct(const grid_t* G, int rc, int dir, const double* U, doubl
         for (int y = lo[1]; y < hi[1]; ++y) {
             for (int x = lo[0]; x < hi[0]; ++x) {
                 const long i = IDX(G, x, y, z);
-                if (rc == RC_MC || rc == RC_MM) {
+                if (rc == RC_WENOF2) {
+                    wenof2_cell(G, U, i, stride, left, right);
+                } else if (rc == RC_MC || rc == RC_MM) {
                     /* MC / MM slope limiters on every variable
                      * (alsfvm/include/alsfvm/reconstruction/MC.hpp:27-52, MM.hpp:25-47) */
                     for (int v = 0; v < nvar; ++v) {

@@ -74,11 +74,12 @@ def extra_flux_combinations():
     fluxes with every reconstruction, the limiters with every base flux."""
     out = []
     for eq in ("euler1", "euler2", "euler3", "burgers"):
+        extra_rc = workloads.LIMITER_RECONSTRUCTIONS + (workloads.EULER_RECONSTRUCTIONS if eq != "burgers" else [])
         for fl in workloads.EXTRA_FLUXES[eq]:
-            for rc in workloads.RECONSTRUCTIONS + workloads.LIMITER_RECONSTRUCTIONS:
+            for rc in workloads.RECONSTRUCTIONS + extra_rc:
                 out.append((eq, fl, rc))
         for fl in workloads.BASE_FLUXES[eq]:
-            for rc in workloads.LIMITER_RECONSTRUCTIONS:
+            for rc in extra_rc:
                 out.append((eq, fl, rc))
     return out
 

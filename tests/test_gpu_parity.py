@@ -227,6 +227,14 @@ EXTRA_RUNS = {
                               boundary="periodic", n=(48, 48, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4,
                               cfl=0.3, end_time=2.0, number_of_saves=0, max_steps=20,
                               prim=lambda: workloads.kh_prim(48, lib.uniform(40, 4))),
+    "sod_hll3_wenof2_rk3": dict(equation="euler1", flux="hll3", recon="wenof2", integrator="rungekutta3",
+                                boundary="neumann", n=(512, 1, 1), lower=(-5, 0, 0), upper=(5, 1, 1), gamma=1.4,
+                                cfl=0.475, end_time=0.5, number_of_saves=1, max_steps=0,
+                                prim=lambda: workloads.sod_prim(512)),
+    "kh_hll_wenof2_rk3": dict(equation="euler2", flux="hll", recon="wenof2", integrator="rungekutta3",
+                              boundary="periodic", n=(48, 40, 1), lower=(0, 0, 0), upper=(1, 1, 0), gamma=1.4,
+                              cfl=0.4, end_time=2.0, number_of_saves=0, max_steps=15,
+                              prim=lambda: workloads.kh_prim(48, lib.uniform(40, 5))[:, :48 * 40]),
     "tg_hll_mc_rk3": dict(equation="euler3", flux="hll", recon="mc", integrator="rungekutta3", boundary="periodic",
                           n=(12, 12, 12), lower=(0, 0, 0), upper=(2 * math.pi,) * 3, gamma=1.4, cfl=0.4,
                           end_time=100.0, number_of_saves=0, max_steps=8, prim=lambda: workloads.tg_prim(12)),

@@ -16,11 +16,12 @@ RECONSTRUCTIONS = ["none", "weno2", "eno2", "eno3", "eno4"]
 # HLL3 / Godunov (numerical_flux_list.hpp): their fixtures live in
 # golden/flux_extra.npz
 LIMITER_RECONSTRUCTIONS = ["mc", "mm"]
+EULER_RECONSTRUCTIONS = ["wenof2"]  # WENOF2.hpp: primitive-variable WENO2, Euler only
 EXTRA_FLUXES = {"euler1": ["central"], "euler2": ["central"], "euler3": ["central"],
                 "burgers": ["central", "rusanov", "roe"]}
 BASE_FLUXES = {"euler1": ["hll", "hll3"], "euler2": ["hll", "hll3"], "euler3": ["hll", "hll3"],
                "burgers": ["godunov"]}
-_GHOSTS = {"none": 1, "weno2": 2, "eno2": 2, "eno3": 3, "eno4": 4, "mc": 2, "mm": 2}
+_GHOSTS = {"none": 1, "weno2": 2, "eno2": 2, "eno3": 3, "eno4": 4, "mc": 2, "mm": 2, "wenof2": 2}
 
 
 def ghost_cells(recon):
