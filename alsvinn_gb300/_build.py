@@ -48,6 +48,7 @@ def _units():
             units.append(("fv_variant.cu", "fv_v%d_e%d.o" % (v, e), flags))
     units.append(("gbfv_api.cu", "gbfv_api.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_stats.cu", "gbfv_stats.o", []))
+    units.append(("gbfv_structure.cu", "gbfv_structure.o", []))
     units.append(("gbfv_noalloc.cu", "gbfv_noalloc.o", []))
     units.append(("gbfv_batch.cu", "gbfv_batch.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_init.cpp", "gbfv_init.o", ["-Xcompiler", "-ffp-contract=off"]))

@@ -22,8 +22,9 @@ alsuq/src/config/Setup.cpp:69-347:
     (SimulatorSetup.cpp:347-380);
   * <uq>: samples, optional sampleStart, generator ("auto" is stlmersenne),
     parameters (name, length, type, optional lower / upper / a / b), stats
-    (name, numberOfSaves, optional writeInitialTimestep, writer type and
-    basename) (Setup.cpp:69-347).
+    (meanvar, or structure_cube with p and numberOfH; numberOfSaves, optional
+    writeInitialTimestep, writer type and basename) (Setup.cpp:69-347,
+    alsuq/src/stats/StructureCube.cpp:23-31).
 Platform strings cpu, cuda and gb300 all run on the GB300 path.
 """
 import os
@@ -119,6 +120,16 @@ class StatConfig:
     number_of_saves: int
     write_initial_timestep: bool
     writer: WriterConfig
+    p: float = 2.0          # structure_cube: the exponent
+    number_of_h: int = 1    # structure_cube: distances 0 .. numberOfH - 1
+
+    def output_names(self):
+        """The statistic's output names (getStatisticsNames): MeanVariance
+        gives mean and variance, StructureCube "structure_cube_" plus p as
+        std::to_string prints it."""
+        if self.name == "meanvar":
+            return ["mean", "variance"]
+        return ["structure_cube_%.6f" % self.p]
 
     def save_interval(self, end_time):
         return end_time / self.number_of_saves if self.number_of_saves > 0 else 0.0
@@ -286,16 +297,19 @@ def read_uq(root):
     snode = uq.find("stats")
     for s in (snode if snode is not None else []):
         name = _text(s, "name")
-        if name != "meanvar":
-            raise ConfigError("Unknown statistics %s (supported: meanvar)" % name)
+        if name not in ("meanvar", "structure_cube"):
+            raise ConfigError("Unknown statistics %s (supported: meanvar, structure_cube)" % name)
         saves = _text(s, "numberOfSaves", required=False)
         if saves is None:
             raise ConfigError("Statistics %s needs numberOfSaves (time-integrated statistics are not supported)"
                               % name)
         wit = _text(s, "writeInitialTimestep", required=False)
+        extra = {}
+        if name == "structure_cube":
+            extra = dict(p=float(_text(s, "p")), number_of_h=int(_text(s, "numberOfH")))
         stats.append(StatConfig(name=name, number_of_saves=int(saves),
                                 write_initial_timestep=_bool(wit) if wit is not None else False,
-                                writer=_writer(s.find("writer"), default_saves=saves)))
+                                writer=_writer(s.find("writer"), default_saves=saves), **extra))
     return UQConfig(samples=int(float(_text(uq, "samples"))),
                     sample_start=int(_text(uq, "sampleStart", default="0", required=False)),
                     generator=generator, parameters=params, stats=stats)

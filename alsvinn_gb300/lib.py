@@ -86,6 +86,12 @@ _SIGNATURES = {
     "gbfv_generator_uniform": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
                                               ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     "gbfv_advance_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_structure_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_structure_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_structure_add_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_structure_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_structure_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_void_p]),
     "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
@@ -422,6 +428,45 @@ class Stats:
         n = ctypes.c_longlong()
         _check(load().gbfv_stats_export(self.h, _ptr(m), _ptr(q), ctypes.byref(n)))
         return n.value, m, q
+
+
+class Structure:
+    """Cube structure function statistic (gbfv_structure_*)."""
+
+    def __init__(self, boundary, n, ghosts, nvar, number_of_h, p):
+        h = ctypes.c_void_p()
+        _check(load().gbfv_structure_create(boundary.encode(), _c_int3(*n), int(ghosts), int(nvar),
+                                            int(number_of_h), float(p), ctypes.byref(h)))
+        self.h = h
+        self.nvar = int(nvar)
+        self.number_of_h = int(number_of_h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_structure_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_device(self, ptr, precision=FP64):
+        _check(load().gbfv_structure_add_device(self.h, ctypes.c_void_p(ptr), precision))
+
+    def result(self):
+        out = np.zeros((self.nvar, self.number_of_h))
+        n = ctypes.c_longlong()
+        _check(load().gbfv_structure_result(self.h, _ptr(out), ctypes.byref(n)))
+        return out, n.value
+
+    def export(self):
+        """(count, sums): the raw sums for a cross-rank merge."""
+        out = np.zeros((self.nvar, self.number_of_h))
+        n = ctypes.c_longlong()
+        _check(load().gbfv_structure_export(self.h, _ptr(out), ctypes.byref(n)))
+        return n.value, out
 
 
 class Batch:

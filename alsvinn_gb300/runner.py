@@ -9,16 +9,18 @@ Follows alsuq's Setup::makeRunner and Runner::run
     component drawn through the run's one stateful generator
     (lib.Generator: STLMersenne + Uniform, or Uniform1D's midpoints), then
     the initial data program evaluated with them;
-  * statistics (meanvar) at the FixedIntervalStatistics save times over the
-    whole padded state, combined over ranks, written as <basename>_mean and
-    <basename>_variance.
+  * statistics at the FixedIntervalStatistics save times, combined over
+    ranks and written by rank 0: meanvar over the whole padded state
+    (<basename>_mean, <basename>_variance) and structure_cube
+    (<basename>_structure_cube_<p>, one value per distance h;
+    alsuq/src/stats/StructureCube.cpp).
 
 Two engines run the samples:
   * "batch" - the ensemble engine (lib.Batch): every sample of a wave is a
     member of one persistent launch per RK stage, each with its own dt; the
     statistics are folded on the device as members reach the end time. Used
-    when statistics are taken once, at the end time, and no per-sample fvm
-    writer is configured.
+    when mean / variance statistics are taken once, at the end time, and no
+    per-sample fvm writer is configured.
   * "serial" - one lib.Solver reused sample after sample with the writer and
     statistics save clamps (any schedule).
 Both give each sample the reference's trajectory; the statistics are FP64
@@ -77,12 +79,13 @@ class Runner:
         self.stats_saves = stats[0].number_of_saves if stats else 0
         self.stats_initial = bool(stats and stats[0].write_initial_timestep)
         batch_ok = (self.fvm.writer is None and self.stats_saves <= 1 and not self.stats_initial
+                    and all(st.name == "meanvar" for st in stats)
                     and self.fvm.integrator in ("rungekutta2", "rungekutta3"))
         if engine == "auto":
             engine = "batch" if batch_ok else "serial"
         if engine == "batch" and not batch_ok:
-            raise ConfigError("the batch engine needs rungekutta2/3, statistics at the end time only and no fvm "
-                              "writer; use the serial engine")
+            raise ConfigError("the batch engine needs rungekutta2/3, mean/variance statistics at the end time only "
+                              "and no fvm writer; use the serial engine")
         self.engine = engine
         self.timesteps = 0
         self.wall_s = 0.0
@@ -94,33 +97,53 @@ class Runner:
                                  self.fvm.dimension, p)
 
     def run(self):
-        """Runs this rank's samples; returns (count, mean, variance) per
-        statistics save as padded states (nvar, total), identical on every
-        rank, and writes the statistics files on rank 0."""
+        """Runs this rank's samples and combines the statistics over the
+        ranks (identical on every rank); rank 0 writes them. self.statistics
+        holds, per configured statistic, one entry per save: (count, mean,
+        variance) for meanvar (padded states (nvar, total) flattened), (count,
+        structure function (nvar, numberOfH)) for structure_cube. Returns the
+        first meanvar statistic's entries."""
         t0 = time.perf_counter()
         params = sample_parameters(self.uqc, self.samples)
         if self.engine == "batch":
-            triples = self._run_batch(params)
+            raw = self._run_batch(params)
         else:
-            triples = self._run_serial(params)
-        results = [uq.combine_statistics(*t) for t in triples]
+            raw = self._run_serial(params)
+        self.statistics = []
+        for st, saves in zip(self.uqc.stats, raw):
+            if st.name == "meanvar":
+                self.statistics.append([uq.combine_statistics(*t) for t in saves])
+            else:
+                self.statistics.append([uq.combine_sums(*t) for t in saves])
         self.wall_s = time.perf_counter() - t0
         if self.rank == 0:
-            self._write_statistics(results)
-        return results
+            self._write_statistics()
+        for st, res in zip(self.uqc.stats, self.statistics):
+            if st.name == "meanvar":
+                return res
+        return []
 
     # -- engines -----------------------------------------------------------
 
     def _run_serial(self, params):
-        acc = None
         sim = Simulator(self.fvm, self.precision, num_samples=self.uqc.samples, output_dir=self.output_dir,
                         statistics_interval=self.stats_interval, statistics_initial=self.stats_initial)
-        nstat = self.stats_saves + (1 if self.stats_initial else 0)
+        nsave = self.stats_saves + (1 if self.stats_initial else 0)
         count = sim.solver.nvar * sim.solver.total
-        acc = [lib.Stats(count) for _ in range(nstat)]
+        g = lib.ghost_cells(self.fvm.reconstruction)
+        acc = []  # per statistic, per save
+        for st in self.uqc.stats:
+            if st.name == "meanvar":
+                acc.append([lib.Stats(count) for _ in range(nsave)])
+            else:
+                acc.append([lib.Structure(self.fvm.boundary, self.fvm.dimension, g, sim.solver.nvar,
+                                          st.number_of_h, st.p) for _ in range(nsave)])
+        prec = self.precision if self.precision == lib.FP32 else lib.FP64
 
         def on_statistics(s, k):
-            acc[k].add_device(s.solver.state_device(), self.precision if self.precision == lib.FP32 else lib.FP64)
+            ptr = s.solver.state_device()
+            for per_save in acc:
+                per_save[k].add_device(ptr, prec)
 
         sim.on_statistics = on_statistics
         try:
@@ -131,12 +154,13 @@ class Runner:
                 sim.run()
                 self.timesteps += sim.get_number_of_timesteps()
             sim.finalize()
-            triples = [a.export() for a in acc]
+            raw = [[a.export() for a in per_save] for per_save in acc]
         finally:
-            for a in acc:
-                a.close()
+            for per_save in acc:
+                for a in per_save:
+                    a.close()
             sim.close()
-        return triples
+        return raw
 
     def _run_batch(self, params):
         f = self.fvm
@@ -172,27 +196,32 @@ class Runner:
                 n, m, q = 0, np.zeros((nv, total)), np.zeros((nv, total))
         finally:
             b.close()
-        return [(n, m.reshape(-1), q.reshape(-1))]
+        return [[(n, m.reshape(-1), q.reshape(-1))] for _ in self.uqc.stats]
 
     # -- output ------------------------------------------------------------
 
-    def _write_statistics(self, results):
-        if not self.uqc.stats:
-            return
+    def _write_statistics(self):
         f = self.fvm
         nv = lib.num_variables(f.equation)
         g = lib.ghost_cells(f.reconstruction)
         from .simulator import interior
-        for st in self.uqc.stats:
+        for st, results in zip(self.uqc.stats, self.statistics):
             w = st.writer
-            for kind, idx in (("mean", 1), ("variance", 2)):
-                base = "%s_%s" % (w.basename, kind)
+            if st.name == "meanvar":
+                outputs = [(name, [interior(np.asarray(r[idx]).reshape(nv, -1), f.dimension, g) for r in results],
+                            (f.lower, f.upper, f.dimension))
+                           for name, idx in (("mean", 1), ("variance", 2))]
+            else:
+                # one value per distance h: x runs over h = 0 .. numberOfH - 1
+                H = st.number_of_h
+                outputs = [(st.output_names()[0], [np.asarray(r[1]).reshape(nv, 1, 1, H) for r in results],
+                            ((-0.5, 0.0, 0.0), (H - 0.5, 1.0, 1.0), (H, 1, 1)))]
+            for name, arrays, (lo, hi, dims) in outputs:
+                base = "%s/%s_%s" % (self.output_dir, w.basename, name)
                 if w.type == "netcdf":
-                    writer = NetCDFWriter("%s/%s" % (self.output_dir, base), f.equation, f.lower, f.upper,
-                                          f.dimension, 1, w.save_fractions())
+                    writer = NetCDFWriter(base, f.equation, lo, hi, dims, 1, w.save_fractions())
                 else:
-                    writer = NumpyWriter("%s/%s" % (self.output_dir, base), f.equation)
-                for k, res in enumerate(results):
-                    U = np.asarray(res[idx]).reshape(nv, -1)
-                    writer.write(interior(U, f.dimension, g), 0, k)
+                    writer = NumpyWriter(base, f.equation)
+                for k, a in enumerate(arrays):
+                    writer.write(a, 0, k)
                 writer.finalize()

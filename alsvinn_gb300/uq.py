@@ -112,3 +112,30 @@ def combine_statistics(count, mean, m2, group=None):
             n, m, q = chan_merge((n, m, q), (int(c.item()), p[0].reshape(mean.shape), p[1].reshape(m2.shape)))
     var = q / n if n else np.zeros_like(q)
     return n, m, var
+
+
+def combine_sums(count, sums, group=None):
+    """All-gather every rank's (count, sums) and add them in rank order;
+    returns (total count, total sums / total count): the rank reduction of
+    sum-type statistics such as the structure functions
+    (StatisticsHelper::combineStatistics, MPI_Reduce(SUM) then division by the
+    sample count)."""
+    import torch
+    import torch.distributed as dist
+
+    sums = np.ascontiguousarray(sums, dtype=np.float64)
+    if not (dist.is_available() and dist.is_initialized()):
+        n, total = count, sums
+    else:
+        world = dist.get_world_size(group)
+        backend = dist.get_backend(group)
+        dev = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" else torch.device("cpu")
+        packed = torch.from_numpy(np.concatenate(([float(count)], sums.ravel()))).to(dev)
+        parts = [torch.empty_like(packed) for _ in range(world)]
+        dist.all_gather(parts, packed, group=group)
+        n, total = 0, np.zeros_like(sums)
+        for part in parts:
+            a = part.cpu().numpy()
+            n += int(a[0])
+            total = total + a[1:].reshape(sums.shape)
+    return n, (total / n if n else np.zeros_like(total))

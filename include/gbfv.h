@@ -207,6 +207,25 @@ int gbfv_stats_result(gbfv_stats* st, double* mean_host, double* var_host, long 
  * empty accumulator gives samples = 0 and zero arrays. */
 int gbfv_stats_export(gbfv_stats* st, double* mean_host, double* m2_host, long long* samples);
 
+/* Cube structure functions (alsuq's "structure_cube" statistic,
+ * alsuq/src/stats/StructureCube.cpp:36-76, kernel
+ * alsfvm/include/alsfvm/functional/structure_common.hpp:37-154). Each sample
+ * adds, per variable and h = 1 .. number_of_h - 1, the sum over cells and
+ * over the points of the cube surface at distance h of |u(x) - u(y)|^p /
+ * (nx ny nz), points outside the grid wrapped ("periodic") or clamped
+ * ("neumann"); entry 0 stays 0. The result is the mean over the samples;
+ * gbfv_structure_export gives the raw sums for a cross-rank merge (sums and
+ * sample counts add). Arrays are nvar x number_of_h doubles. */
+typedef struct gbfv_structure gbfv_structure;
+int gbfv_structure_create(const char* boundary, const int n[3], int ghosts, int nvar, int number_of_h, double p,
+                          gbfv_structure** out);
+int gbfv_structure_destroy(gbfv_structure* s);
+/* Adds one sample: a padded device state of nvar variables (precision 0 or 1:
+ * double, 2: float). */
+int gbfv_structure_add_device(gbfv_structure* s, const void* state_dev, int precision);
+int gbfv_structure_result(gbfv_structure* s, double* mean_host, long long* samples);
+int gbfv_structure_export(gbfv_structure* s, double* sums_host, long long* samples);
+
 /* --------------------------------------------------------- ensembles */
 
 /* Many grids (members) of one scheme advanced together: the UQ ensemble of

@@ -996,6 +996,89 @@ int fv_generate_sequence(int nparams, const int* dims, const double* lowers, con
     return 0;
 }
 
+/* ------------------------------------------------- structure functions */
+
+/* |x|^p as the reference evaluates it: FastPower<p> (x * FastPower<p-1>(x))
+ * for p = 1..5, pow otherwise (alsutils/include/alsutils/math/FastPower.hpp,
+ * PowPower.hpp, dispatched in structure_common.hpp:156-180). */
+static double structure_power(double x, double p, int ip) {
+    switch (ip) {
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return x * (x * x);
+        case 4: return x * (x * (x * x));
+        case 5: return x * (x * (x * (x * x)));
+        default: return pow(x, p);
+    }
+}
+
+/* ValueAtBoundary<PERIODIC / NEUMANN> (alsfvm/include/alsfvm/boundary/
+ * ValueAtBoundary.hpp): periodic wraps the interior position, Neumann clamps
+ * it to the interior. */
+static long structure_index(const grid_t* G, int periodic, int x, int y, int z) {
+    const int n[3] = {G->n[0], G->n[1], G->n[2]};
+    int q[3] = {x, y, z};
+    for (int d = 0; d < 3; ++d) {
+        if (periodic) {
+            while (q[d] < 0) q[d] += n[d];
+            q[d] = q[d] % n[d];
+        } else {
+            q[d] = q[d] < n[d] - 1 ? q[d] : n[d] - 1;
+            q[d] = q[d] > 0 ? q[d] : 0;
+        }
+    }
+    return IDX(G, q[0] + G->g[0], q[1] + G->g[1], q[2] + G->g[2]);
+}
+
+/* computeStructureCubeCPU (alsfvm/include/alsfvm/functional/
+ * structure_common.hpp:37-154): for every variable, cell (k, j, i) and h in
+ * 1 .. number_of_h - 1, out[h] += |u - u_h|^p / (nx ny nz) over the points
+ * of the cube surface at distance h, visited per direction d and side in
+ * the reference's loop bounds. */
+int fv_structure_cube(const char* equation, const char* boundary, const int n[3], int ghosts, int number_of_h,
+                      double p, const double* U, double* out) {
+    const int eq = parse_eq(equation), bc = parse_bc(boundary);
+    if (eq < 0 || bc < 0 || number_of_h < 1) return fail(-1, "bad arguments");
+    grid_t G;
+    make_grid(&G, eq, n, ghosts, 1.4);
+    const int ip = (p == 1.0) ? 1 : (p == 2.0) ? 2 : (p == 3.0) ? 3 : (p == 4.0) ? 4 : (p == 5.0) ? 5 : 0;
+    const int dims = G.dim, nx = n[0], ny = n[1], nz = n[2];
+    const int periodic = bc == BC_PERIODIC;
+    for (int v = 0; v < G.nvar; ++v) {
+        const double* u = U + (long)v * G.total;
+        double* o = out + (long)v * number_of_h;
+        for (int h = 0; h < number_of_h; ++h) o[h] = 0.0;
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    for (int h = 1; h < number_of_h; ++h) {
+                        const double uc = u[IDX(&G, i + G.g[0], j + G.g[1], k + G.g[2])];
+                        for (int d = 0; d < dims; d++)
+                            for (int side = 0; side < 2; side++) {
+                                const int zDir = d == 2, yDir = d == 1, xDir = d == 0;
+                                const int zStart = zDir ? (side == 0 ? k - h : k + h) : (dims > 2 ? k - h : 0);
+                                const int zEnd = zDir ? (zStart + 1) : (dims > 2 ? k + h + 1 : 1);
+                                const int yStart = yDir ? (side == 0 ? j - h : j + h)
+                                                        : (dims == 2 ? j - h + 1 : (dims == 3 ? j - h + 1 : 0));
+                                const int yEnd = yDir ? (yStart + 1) : (dims == 2 ? j + h : (dims == 3 ? j + h : 1));
+                                int xStart = xDir ? (side == 0 ? i - h : i + h) : i - h;
+                                int xEnd = xDir ? (xStart + 1) : i + h + 1;
+                                if (zDir) {
+                                    xStart += 1;
+                                    xEnd -= 1;
+                                }
+                                for (int z = zStart; z < zEnd; z++)
+                                    for (int y = yStart; y < yEnd; y++)
+                                        for (int x = xStart; x < xEnd; x++) {
+                                            const double uh = u[structure_index(&G, periodic, x, y, z)];
+                                            o[h] += structure_power(fabs(uc - uh), p, ip) / (nx * ny * nz);
+                                        }
+                            }
+                    }
+    }
+    return 0;
+}
+
 /* ---------------------------------------------------------- statistics */
 
 /* MeanVariance::computeStatistics adds u and pow(u,2) per sample

@@ -55,6 +55,8 @@ int fv_uniform(int dimension, int sample, double lower, double upper, double* ou
 int fv_generate_sequence(int nparams, const int* dims, const double* lowers, const double* uppers,
                          long long sample_start, long long nsamples, double* out);
 
+int fv_structure_cube(const char* equation, const char* boundary, const int n[3], int ghosts, int number_of_h,
+                      double p, const double* U, double* out);
 int fv_meanvar(long count, int nsamples, const double* const* samples, double* mean,
                double* var);
 

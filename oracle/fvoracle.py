@@ -126,6 +126,15 @@ def generate_sequence(dims, sample_start, nsamples, lowers=None, uppers=None):
     return out
 
 
+def structure_cube(equation, boundary, n, ghosts, number_of_h, p, U):
+    """One sample's cube structure function: (nvar, number_of_h)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    out = np.zeros((U.shape[0], number_of_h))
+    _check(load().fv_structure_cube(equation.encode(), boundary.encode(), _i3(n), int(ghosts), int(number_of_h),
+                                    D(p), _p(U), _p(out)))
+    return out
+
+
 def meanvar(samples):
     samples = [np.ascontiguousarray(s, dtype=np.float64) for s in samples]
     count = samples[0].size

@@ -15,6 +15,7 @@
 #include "alsfvm/diffusion/NoDiffusion.hpp"
 #include "alsfvm/equation/CellComputerFactory.hpp"
 #include "alsfvm/equation/euler/EulerParameters.hpp"
+#include "alsfvm/functional/structure_common.hpp"
 #include "alsfvm/grid/Grid.hpp"
 #include "alsfvm/init/InitialData.hpp"
 #include "alsfvm/integrator/IntegratorFactory.hpp"
@@ -448,6 +449,34 @@ int ref_meanvar(const char* equation, const int dims[3], int ghosts, int nsample
         mv.combineStatistics();
         mv.finalizeStatistics();
         mv.writeStatistics(*s.grid);
+        return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
+// One sample's cube structure function (StructureCube::computeStatistics,
+// alsuq/src/stats/StructureCube.cpp:36-76, through the reference's own
+// alsfvm/include/alsfvm/functional/structure_common.hpp): out receives nvar
+// arrays of number_of_h values, entry h the sum over cells and over the
+// cube surface at distance h of |u - u_h|^p / (nx ny nz).
+int ref_structure_cube(const char* equation, const char* boundary, const int dims[3], int ghosts, int number_of_h,
+    double p, const double* U, double* out) {
+    try {
+        double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+        Setup s(equation, "godunov", "none", boundary, "forwardeuler", dims, lo, hi, 1.4, 0.5);
+        const int nvar = nvar_of(equation);
+        volume::VolumeFactory vf(equation, s.memory);
+        auto in = vf.createConservedVolume(dims[0], dims[1], dims[2], ghosts);
+        copy_in(*in, U, nvar);
+        auto o = vf.createConservedVolume(number_of_h, 1, 1, 0);
+        o->makeZero();
+        if (std::string(boundary) == "periodic")
+            functional::dispatchComputeStructureCubeCPU<boundary::PERIODIC>(*o, *in, number_of_h, p);
+        else
+            functional::dispatchComputeStructureCubeCPU<boundary::NEUMANN>(*o, *in, number_of_h, p);
+        copy_out(*o, out, nvar);
         return 0;
     } catch (std::exception& e) {
         g_error = e.what();

@@ -103,6 +103,31 @@ def flux_extra_cases():
     np.savez_compressed(os.path.join(HERE, "flux_extra.npz"), **out)
 
 
+STRUCTURE_CASES = {
+    # name: (equation, boundary, n, ghosts, number_of_h, p)
+    "burgers_periodic_p2": ("burgers", "periodic", (20, 1, 1), 2, 6, 2.0),
+    "euler1_neumann_p1": ("euler1", "neumann", (16, 1, 1), 3, 5, 1.0),
+    "euler2_periodic_p3": ("euler2", "periodic", (12, 10, 1), 2, 5, 3.0),
+    "euler2_neumann_p2_5": ("euler2", "neumann", (9, 11, 1), 1, 4, 2.5),
+    "euler3_periodic_p2": ("euler3", "periodic", (6, 5, 4), 2, 4, 2.0),
+    "burgers2d_neumann_p4": ("burgers", "neumann", (8, 7, 1), 2, 5, 4.0),
+}
+
+
+def structure_cases():
+    rng = np.random.default_rng(20240603)
+    out = {}
+    for name, (eq, bc, n, g, H, p) in STRUCTURE_CASES.items():
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        nv = workloads.NVAR[eq]
+        o = np.zeros((nv, H))
+        check(R.ref_structure_cube(eq.encode(), bc.encode(), i3(n), g, H, D(p), P(U), P(o)))
+        out[name + "_U"] = U
+        out[name + "_S"] = o
+    np.savez_compressed(os.path.join(HERE, "structure.npz"), **out)
+
+
 def boundary_cases():
     out = {}
     for bc in ("neumann", "periodic"):
@@ -206,6 +231,7 @@ elif __name__ == "__main__":
     generator_sequence_cases()
     flux_cases()
     flux_extra_cases()
+    structure_cases()
     boundary_cases()
     meanvar_cases()
     run_cases()

@@ -173,3 +173,12 @@ def test_cli_reports_configuration_errors(tmp_path, capsys):
     rc = alsvinncli.main([_xml(tmp_path, base(boundary="reflective"))])
     assert rc == 1
     assert "Unknown boundary conditions" in capsys.readouterr().err
+
+
+def test_structure_cube_statistics_are_read(tmp_path):
+    uqx = ("<uq><samples>2</samples><generator>auto</generator><parameters/><stats><stat>"
+           "<name>structure_cube</name><p>3</p><numberOfH>7</numberOfH><numberOfSaves>2</numberOfSaves>"
+           "<writer><type>netcdf</type><basename>kh</basename></writer></stat></stats></uq>")
+    st = config.read_config(_xml(tmp_path, base(uq=uqx))).uq.stats[0]
+    assert (st.name, st.p, st.number_of_h, st.number_of_saves) == ("structure_cube", 3.0, 7, 2)
+    assert st.output_names() == ["structure_cube_3.000000"]

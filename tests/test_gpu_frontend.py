@@ -138,3 +138,35 @@ def test_alsuqcli_runs_the_input(cuda_device, tmp_path, capsys):
     out = capsys.readouterr().out
     assert '"engine": "batch"' in out
     assert os.path.exists(str(tmp_path / "kh_uq_stats_variance"))
+
+
+def test_alsuq_structure_functions_match_the_oracle(cuda_device, tmp_path):
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
+    xml = str(tmp_path / "kh_uq.xml")
+    text = open(xml).read().replace(
+        "<stats>",
+        "<stats><stat><name>structure_cube</name><p>2</p><numberOfH>5</numberOfH><numberOfSaves>1</numberOfSaves>"
+        "<writer><type>netcdf</type><basename>kh_uq_sf</basename></writer></stat>")
+    open(xml, "w").write(text)
+    cfg = config.read_config(xml)
+    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path))
+    assert r.engine == "serial"
+    r.run()
+    f, u = cfg.fvm, cfg.uq
+    draws = runner.sample_parameters(u, range(u.samples))
+    g = lib.ghost_cells(f.reconstruction)
+    want = 0
+    for s in range(u.samples):
+        p = dict(f.init_parameters)
+        p.update(draws[s])
+        prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, p)
+        U = _oracle_run(f, prim, f.end_time, 1)[0]
+        want = want + fvoracle.structure_cube(f.equation, f.boundary, f.dimension, g, 5, 2.0, U)
+    want = want / u.samples
+    n, got = r.statistics[0][0]
+    assert n == u.samples
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-15)
+    with netcdf(str(tmp_path / "kh_uq_sf_structure_cube_2.000000"), "r", mmap=False) as nc:
+        assert nc.dimensions["x"] == 5
+        np.testing.assert_allclose(np.array(nc.variables["rho"][0, 0]).reshape(-1), want[0], rtol=1e-12)

@@ -106,3 +106,22 @@ def test_generator_sequence_matches_reference(name):
     out = fvoracle.generate_sequence(z[name + "_dims"], int(z[name + "_start"][0]), z[name].shape[0],
                                      z[name + "_lower"], z[name + "_upper"])
     assert np.array_equal(out, z[name])
+
+
+STRUCTURE_CASES = {
+    # name: (equation, boundary, n, ghosts, number_of_h, p), as tests/golden/make_golden.py
+    "burgers_periodic_p2": ("burgers", "periodic", (20, 1, 1), 2, 6, 2.0),
+    "euler1_neumann_p1": ("euler1", "neumann", (16, 1, 1), 3, 5, 1.0),
+    "euler2_periodic_p3": ("euler2", "periodic", (12, 10, 1), 2, 5, 3.0),
+    "euler2_neumann_p2_5": ("euler2", "neumann", (9, 11, 1), 1, 4, 2.5),
+    "euler3_periodic_p2": ("euler3", "periodic", (6, 5, 4), 2, 4, 2.0),
+    "burgers2d_neumann_p4": ("burgers", "neumann", (8, 7, 1), 2, 5, 4.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(STRUCTURE_CASES))
+def test_structure_cube_matches_reference(name):
+    z = load("structure.npz")
+    eq, bc, n, g, H, p = STRUCTURE_CASES[name]
+    out = fvoracle.structure_cube(eq, bc, n, g, H, p, z[name + "_U"])
+    assert np.array_equal(out, z[name + "_S"])
