@@ -51,6 +51,14 @@ template <> __device__ __forceinline__ dfloat shfl_xor_c<dfloat>(dfloat v, int o
     return dfloat(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
 }
 
+// A kernel-uniform double in the arithmetic type: the float copy the host or
+// the dt kernel rounded once (no per-thread conversion on the FP64 pipe), the
+// double itself, or its double-float split.
+template <class T> __device__ __forceinline__ T uniform_value(double d, float f);
+template <> __device__ __forceinline__ double uniform_value<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float uniform_value<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ dfloat uniform_value<dfloat>(double d, float) { return dfloat(d); }
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
@@ -225,7 +233,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 // and runs in R.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
-                                           double (*wred)[3]) {
+                                           C* wred) {
     using Ph = Physics<C, EQ, FLUX>;
     using PhR = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
@@ -247,7 +255,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     R* out = reinterpret_cast<R*>(A.out);
     const long long total = Gd.total;
     const int mode = A.mode;
-    const R scale = (R)A.st->scale;
+    const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
 
     // 1. tile + halo: padded cells [org, org + T + 2g) per active dimension
     for (int w = tid; w < SL::HALO; w += NTH) {
@@ -278,7 +286,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     // wave-speed maxima in the arithmetic type (the max is exact, so one
     // conversion per thread gives the same double as converting every face)
     C wsd[3] = {C(0), C(0), C(0)};
-    const C gamma = C(A.gamma);
+    const C gamma = uniform_value<C>(A.gamma, A.gamma_f);
     tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
     if constexpr (DIM > 1)
         tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
@@ -292,13 +300,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             C v = wsd[d];
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) v = fmax_(v, shfl_xor_c(v, off));
-            if ((tid & 31) == 0) wred[tid >> 5][d] = (double)v;
+            if ((tid & 31) == 0) wred[(tid >> 5) * 3 + d] = v;
         }
         __syncthreads();
+        // one conversion to double per CTA and direction: per-warp FP64
+        // instructions occupy GB300's narrow FP64 pipe even on one lane
         if (tid < DIM) {
-            double v = 0.0;
-            for (int w = 0; w < NTH / 32; ++w) v = fmax_(v, wred[w][tid]);
-            atomic_max_nonneg(&A.st->ws_bits[tid], v);
+            C v = wred[tid];
+            for (int w = 1; w < NTH / 32; ++w) v = fmax_(v, wred[w * 3 + tid]);
+            atomic_max_nonneg(&A.st->ws_bits[tid], (double)v);
         }
     }
 
@@ -339,7 +349,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             res[k] = v;
         }
     }
-    if (A.check && !PhR::obeys(res, (R)A.gamma)) {
+    if (A.check && !PhR::obeys(res, uniform_value<R>(A.gamma, A.gamma_f))) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
@@ -348,7 +358,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double wred[NTH / 32][3];
+    __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
+    C* wred = reinterpret_cast<C*>(wred_raw);
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
     stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
@@ -362,7 +373,8 @@ __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __global__ void __launch_bounds__(NTH, (std::is_same<C, float>::value ? 5 : 1)) batch_stage_kernel(BatchArgs B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double wred[NTH / 32][3];
+    __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
+    C* wred = reinterpret_cast<C*>(wred_raw);
     const int ntiles = *B.ntiles;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 tile = B.tiles[t];
@@ -376,6 +388,7 @@ __global__ void __launch_bounds__(NTH, (std::is_same<C, float>::value ? 5 : 1)) 
         A.G = m.G;
         A.st = st;
         A.gamma = B.gamma;
+        A.gamma_f = B.gamma_f;
         A.mode = B.mode;
         A.periodic = B.periodic;
         A.check = 0;
@@ -413,11 +426,11 @@ __global__ void fe_apply_kernel(StageArgs A) {
     R* out = reinterpret_cast<R*>(A.out);
     const long long total = Gd.total;
     const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
-    const R scale = (R)A.st->scale;
+    const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
     R res[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) res[k] = madd(l0[k * total + own], scale, out[k * total + own]);
-    if (A.check && !Ph::obeys(res, (R)A.gamma)) {
+    if (A.check && !Ph::obeys(res, uniform_value<R>(A.gamma, A.gamma_f))) {
         if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);

@@ -27,6 +27,7 @@ struct StepState {
     int group;                      // ensemble: statistics group (< 0: none)
     long long number_saved2;        // second save clamp's counter (FixedIntervalStatistics, starts at 1)
     int saved_mask;                 // bit k: save counter k advanced in the step just finished
+    float scale_f;                  // scale rounded to float once, for the FP32 kernels
 };
 
 struct StepParams {
@@ -78,7 +79,12 @@ struct Grid {
     int dim;
 };
 
+// Padded index of (x, y, z). Arrays below 2^31 cells per variable (every
+// grid up to ~1290^3) take 32-bit products: GB300 runs 64-bit integer
+// multiplies on its narrow FP64 pipe, which the stage kernels otherwise keep
+// free for FP64 arithmetic.
 __device__ __forceinline__ long long gidx(const Grid& G, int x, int y, int z) {
+    if (G.total < (1LL << 31)) return (long long)((z * G.t[1] + y) * G.t[0] + x);
     return ((long long)z * G.t[1] + y) * G.t[0] + x;
 }
 
@@ -139,6 +145,7 @@ struct StageArgs {
     StepState* st;
     Grid G;
     double gamma;
+    float gamma_f;    // gamma rounded to float once, for the FP32 kernels
     int mode;
     int periodic;
     int check;        // run the constraint check on the output
@@ -182,6 +189,7 @@ struct BatchArgs {
     const int4* tiles;
     const int* ntiles;
     double gamma;
+    float gamma_f;
     int mode;
     int periodic;
 };

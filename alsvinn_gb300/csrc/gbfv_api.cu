@@ -63,6 +63,7 @@ __global__ void dt_kernel(StepState* st, StepParams P) {
     }
     st->dt = dt;
     st->scale = dt / P.cell_lengths[0];
+    st->scale_f = (float)st->scale;
 }
 
 // t += dt (TimestepInformation::incrementTime), the writer's save counter, and
@@ -477,6 +478,7 @@ static StageArgs stage_args(gbfv_solver* s, StepState* st, const void* in, const
     a.st = st;
     a.G = s->G;
     a.gamma = s->gamma;
+    a.gamma_f = (float)s->gamma;
     a.mode = mode;
     a.periodic = s->periodic;
     a.check = check;
@@ -834,6 +836,7 @@ int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* 
     auto args = [&](const void* in, const void* u0, const void* l0, void* out, int mode, int check) {
         StageArgs a;
         a.in = in; a.u0 = u0; a.l0 = l0; a.out = out; a.st = st; a.G = p.G; a.gamma = p.gamma;
+        a.gamma_f = (float)p.gamma;
         a.mode = mode; a.periodic = p.periodic; a.check = check;
         return a;
     };

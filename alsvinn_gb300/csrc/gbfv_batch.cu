@@ -66,6 +66,7 @@ __global__ void batch_dt_kernel(StepState* st, const MemberParam* mp, int M, dou
     }
     S.dt = dt;
     S.scale = dt / P.cell_lengths[0];
+    S.scale_f = (float)S.scale;
 }
 
 __global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M, int alternate) {
@@ -274,6 +275,7 @@ int enqueue_batch_step(gbfv_batch* b) {
     a.tiles = b->d_tiles;
     a.ntiles = b->d_ntiles;
     a.gamma = p.gamma;
+    a.gamma_f = (float)p.gamma;
     a.periodic = p.periodic;
     const int M = b->max_members;
     const unsigned mb = (unsigned)((M + 127) / 128);
