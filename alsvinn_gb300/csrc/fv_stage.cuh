@@ -156,11 +156,26 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     constexpr int DS = D == 0 ? 1 : (D == 1 ? SL::HX : SL::HX * SL::HY);
     constexpr int VS = SL::HALO;
 
+    // Work items: along x (D = 0) the cells of a line are consecutive; for
+    // D >= 1 consecutive items step along x (p, the first other dimension),
+    // so a warp's shared-memory accesses stay unit-stride in every phase.
+    // Line buffers hold item w at index w in both layouts:
+    //   D = 0:  w = (o * LEN + a),            o = p + O1 q
+    //   D >= 1: w = ((q * LEN + a) * O1 + p)  (faces: LEN -> TD + 1)
     // reconstruction of cells -1 .. TD along D
     for (int w = tid; w < NREC; w += NTH) {
-        const int a = w % LEN;
-        const int o = w / LEN;
-        const int p = o % O1, q = o / O1;
+        int a, p, q;
+        if constexpr (D == 0) {
+            a = w % LEN;
+            const int o = w / LEN;
+            p = o % O1;
+            q = o / O1;
+        } else {
+            p = w % O1;
+            const int r = w / O1;
+            a = r % LEN;
+            q = r / LEN;
+        }
         int c[3];
         c[D] = a - 1;
         if (D == 0) { c[1] = p; c[2] = q; }
@@ -178,14 +193,27 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     __syncthreads();
     // face b is the left face of tile cell b along D (between cells b-1 and b)
     for (int f = tid; f < NFACE; f += NTH) {
-        const int b = f % (TD + 1);
-        const int o = f / (TD + 1);
-        const int p = o % O1, q = o / O1;
+        int b, p, q, il, ir;  // il: item of cell b-1, ir: item of cell b
+        if constexpr (D == 0) {
+            b = f % (TD + 1);
+            const int o = f / (TD + 1);
+            p = o % O1;
+            q = o / O1;
+            il = o * LEN + b;
+            ir = il + 1;
+        } else {
+            p = f % O1;
+            const int r = f / O1;
+            b = r % (TD + 1);
+            q = r / (TD + 1);
+            il = (q * LEN + b) * O1 + p;
+            ir = il + O1;
+        }
         R a[NV], bb[NV], F[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            a[k] = rr[k * NREC + o * LEN + b];       // cell b-1 at its right face
-            bb[k] = rl[k * NREC + o * LEN + b + 1];  // cell b at its left face
+            a[k] = rr[k * NREC + il];   // cell b-1 at its right face
+            bb[k] = rl[k * NREC + ir];  // cell b at its left face
         }
         const R w = Ph::template face_flux<D>(a, bb, gamma, F);
 #pragma unroll
@@ -209,11 +237,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         const int cd = D == 0 ? cx : (D == 1 ? cy : cz);
         const int p = D == 0 ? cy : cx;
         const int q = D == 2 ? cy : cz;
-        const int o = p + O1 * q;
+        // faces cd (left) and cd + 1 (right) of this cell's line
+        const int fli = D == 0 ? (p + O1 * q) * (TD + 1) + cd : (q * (TD + 1) + cd) * O1 + p;
+        const int fri = D == 0 ? fli + 1 : fli + O1;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R fl = fc[k * NFACE + o * (TD + 1) + cd];
-            const R fr = fc[k * NFACE + o * (TD + 1) + cd + 1];
+            const R fl = fc[k * NFACE + fli];
+            const R fr = fc[k * NFACE + fri];
             if constexpr (!kExact && D == 0)
                 acc[k] = fl - fr;  // the first direction starts the sum
             else
