@@ -137,6 +137,8 @@ struct SmemLayout {
     static constexpr int FAC2 = DIM > 2 ? TX * TY * (TZ + 1) : 0;
     static constexpr int FAC = FAC0 > FAC1 ? (FAC0 > FAC2 ? FAC0 : FAC2) : (FAC1 > FAC2 ? FAC1 : FAC2);
     static constexpr size_t bytes = sizeof(R) * ((size_t)NV * HALO + 2 * (size_t)NV * REC + (size_t)NV * FAC);
+    // the ensemble kernel's second halo buffer and L0 halo
+    static constexpr size_t prefetch_bytes = sizeof(R) * 2 * (size_t)NV * HALO;
 };
 
 
@@ -261,33 +263,20 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
 // With C != R the combination with the stage inputs re-reads the exact R
 // values of the thread's own cell (L1/L2 hits: the tile load just fetched them)
 // and runs in R.
+// Phase 1 of a tile: the tile plus its halo of g cells per active dimension
+// into su, the stage-1 modes forming U1 = L0 c + U0 on the way.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
-__device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
-                                           C* wred) {
-    using Ph = Physics<C, EQ, FLUX>;
-    using PhR = Physics<R, EQ, FLUX>;
-    constexpr int NV = Ph::NV;
-    constexpr int G = ReconTraits<RC>::ghosts;
-    using SL = SmemLayout<C, NV, G, DIM, TX, TY, TZ>;
-    constexpr int NT = TX * TY * TZ;  // cells of the tile
-    static_assert(NT <= NTH && NTH % 32 == 0, "one thread per cell at least, whole warps");
+__device__ __forceinline__ void stage_tile_load(const StageArgs& A, const int* org, C* su) {
+    constexpr int NV = Physics<C, EQ, FLUX>::NV;
+    using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
     constexpr bool kSame = std::is_same<R, C>::value;
-    C* su = reinterpret_cast<C*>(smem_raw);
-    C* rl = su + NV * SL::HALO;
-    C* rr = rl + NV * SL::REC;
-    C* fc = rr + NV * SL::REC;
-
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;
     const R* in = reinterpret_cast<const R*>(A.in);
-    const R* u0 = reinterpret_cast<const R*>(A.u0);
     const R* l0 = reinterpret_cast<const R*>(A.l0);
-    R* out = reinterpret_cast<R*>(A.out);
     const long long total = Gd.total;
     const int mode = A.mode;
     const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
-
-    // 1. tile + halo: padded cells [org, org + T + 2g) per active dimension
     for (int w = tid; w < SL::HALO; w += NTH) {
         const int hx = w % SL::HX, hy = (w / SL::HX) % SL::HY, hz = w / (SL::HX * SL::HY);
         const int px = org[0] + hx, py = org[1] + hy, pz = org[2] + hz;
@@ -307,7 +296,99 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
             for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = C(1);
         }
     }
+    (void)kSame;
     __syncthreads();
+}
+
+// Asynchronous copy of one element global -> shared (cp.async, sm_80+): the
+// ensemble kernel stages the next tile's halo while the current one computes.
+template <class T> __device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Issues the copies of a tile's halo into su (and of L0 into l0s for the
+// stage-1 modes); cells past the padded array get the values the
+// synchronous load gives them. Storage and arithmetic type must agree.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH>
+__device__ __forceinline__ void stage_tile_prefetch(const StageArgs& A, const int* org, R* su, R* l0s) {
+    constexpr int NV = Physics<R, EQ, FLUX>::NV;
+    using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    const Grid& Gd = A.G;
+    const int tid = threadIdx.x;
+    const R* in = reinterpret_cast<const R*>(A.in);
+    const R* l0 = reinterpret_cast<const R*>(A.l0);
+    const long long total = Gd.total;
+    const bool s1 = A.mode == MODE_RK3_S1 || A.mode == MODE_RK2_S1;
+    for (int w = tid; w < SL::HALO; w += NTH) {
+        const int hx = w % SL::HX, hy = (w / SL::HX) % SL::HY, hz = w / (SL::HX * SL::HY);
+        const int px = org[0] + hx, py = org[1] + hy, pz = org[2] + hz;
+        if (px < Gd.t[0] && py < Gd.t[1] && pz < Gd.t[2]) {
+            const long long gi = gidx(Gd, px, py, pz);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                cp_async_elem(su + k * SL::HALO + w, in + k * total + gi);
+                if (s1) cp_async_elem(l0s + k * SL::HALO + w, l0 + k * total + gi);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                su[k * SL::HALO + w] = R(1);
+                if (s1) l0s[k * SL::HALO + w] = R(0);  // L0 c + 1 = 1
+            }
+        }
+    }
+    cp_async_commit();
+}
+
+// Waits for the prefetched halo; the stage-1 modes then form U1 = L0 c + U0.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH>
+__device__ __forceinline__ void stage_tile_prefetch_finish(const StageArgs& A, R* su, const R* l0s) {
+    constexpr int NV = Physics<R, EQ, FLUX>::NV;
+    using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    cp_async_wait_all();
+    __syncthreads();
+    if (A.mode == MODE_RK3_S1 || A.mode == MODE_RK2_S1) {
+        const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
+        for (int w = threadIdx.x; w < SL::HALO; w += NTH) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = madd(l0s[k * SL::HALO + w], scale, su[k * SL::HALO + w]);
+        }
+        __syncthreads();
+    }
+}
+
+// Phases 2-4 of a tile whose halo is in su; work holds the per-direction
+// line buffers (reconstructed face values and face fluxes).
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+__device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int* org, const C* su, C* work,
+                                                   C* wred) {
+    using Ph = Physics<C, EQ, FLUX>;
+    using PhR = Physics<R, EQ, FLUX>;
+    constexpr int NV = Ph::NV;
+    constexpr int G = ReconTraits<RC>::ghosts;
+    using SL = SmemLayout<C, NV, G, DIM, TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;  // cells of the tile
+    static_assert(NT <= NTH && NTH % 32 == 0, "one thread per cell at least, whole warps");
+    constexpr bool kSame = std::is_same<R, C>::value;
+    C* rl = work;
+    C* rr = rl + NV * SL::REC;
+    C* fc = rr + NV * SL::REC;
+
+    const Grid& Gd = A.G;
+    const int tid = threadIdx.x;
+    const R* in = reinterpret_cast<const R*>(A.in);
+    const R* u0 = reinterpret_cast<const R*>(A.u0);
+    const R* l0 = reinterpret_cast<const R*>(A.l0);
+    R* out = reinterpret_cast<R*>(A.out);
+    const long long total = Gd.total;
+    const int mode = A.mode;
+    const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
 
     // 2. flux difference per direction
     C acc[NV];
@@ -385,6 +466,18 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
 }
 
+// One tile of one stage with a synchronous halo load. Shared memory: the halo
+// tile, then the line buffers.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+__device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
+                                           C* wred) {
+    constexpr int NV = Physics<C, EQ, FLUX>::NV;
+    using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    C* su = reinterpret_cast<C*>(smem_raw);
+    stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, su);
+    stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, su, su + NV * SL::HALO, wred);
+}
+
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -393,6 +486,39 @@ __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
     stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
+}
+
+// The stage arguments of ensemble tile t (its member's buffers for the stage
+// mode); false when the member's run is done.
+__device__ __forceinline__ bool batch_tile_args(const BatchArgs& B, int t, StageArgs& A, int* org) {
+    const int4 tile = B.tiles[t];
+    StepState* st = B.states + tile.x;
+    if (st->done) return false;  // the same value for every thread of the CTA
+    const BatchMember& m = B.members[tile.x];
+    // ensemble RK2 alternates the two state buffers instead of copying
+    void* cur = st->parity ? m.v : m.u;
+    void* other = st->parity ? m.u : m.v;
+    A.G = m.G;
+    A.st = st;
+    A.gamma = B.gamma;
+    A.gamma_f = B.gamma_f;
+    A.mode = B.mode;
+    A.periodic = B.periodic;
+    A.check = 0;
+    A.l0 = nullptr;
+    if (B.mode == MODE_L) {
+        A.in = cur; A.u0 = cur; A.out = m.l;
+    } else if (B.mode == MODE_RK3_S1) {
+        A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other;
+    } else if (B.mode == MODE_RK3_S2) {
+        A.in = other; A.u0 = cur; A.out = cur; A.check = 1;
+    } else {  // MODE_RK2_S1
+        A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
+    }
+    org[0] = tile.y;
+    org[1] = tile.z;
+    org[2] = tile.w;
+    return true;
 }
 
 // Persistent ensemble stage: each CTA walks the tile list (tiles of every
@@ -406,35 +532,48 @@ __global__ void __launch_bounds__(NTH, (std::is_same<C, float>::value ? 5 : 1)) 
     __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
     C* wred = reinterpret_cast<C*>(wred_raw);
     const int ntiles = *B.ntiles;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int4 tile = B.tiles[t];
-        StepState* st = B.states + tile.x;
-        if (st->done) continue;  // the same value for every thread of the CTA
-        const BatchMember& m = B.members[tile.x];
-        // ensemble RK2 alternates the two state buffers instead of copying
-        void* cur = st->parity ? m.v : m.u;
-        void* other = st->parity ? m.u : m.v;
-        StageArgs A;
-        A.G = m.G;
-        A.st = st;
-        A.gamma = B.gamma;
-        A.gamma_f = B.gamma_f;
-        A.mode = B.mode;
-        A.periodic = B.periodic;
-        A.check = 0;
-        A.l0 = nullptr;
-        if (B.mode == MODE_L) {
-            A.in = cur; A.u0 = cur; A.out = m.l;
-        } else if (B.mode == MODE_RK3_S1) {
-            A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other;
-        } else if (B.mode == MODE_RK3_S2) {
-            A.in = other; A.u0 = cur; A.out = cur; A.check = 1;
-        } else {  // MODE_RK2_S1
-            A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
+    if constexpr (std::is_same<R, C>::value) {
+        // Software pipeline: the next tile's halo streams into the second
+        // halo buffer (cp.async) while the current tile computes. Shared
+        // memory: halo A, halo B, L0 halo, line buffers.
+        constexpr int NV = Physics<C, EQ, FLUX>::NV;
+        using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+        C* cur_h = reinterpret_cast<C*>(smem_raw);
+        C* next_h = cur_h + NV * SL::HALO;
+        C* l0h = next_h + NV * SL::HALO;
+        C* work = l0h + NV * SL::HALO;
+        StageArgs A, An;
+        int org[3], orgn[3];
+        int t = blockIdx.x;
+        while (t < ntiles && !batch_tile_args(B, t, A, org)) t += gridDim.x;
+        if (t >= ntiles) return;
+        stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, cur_h);
+        while (true) {
+            int tn = t + gridDim.x;
+            while (tn < ntiles && !batch_tile_args(B, tn, An, orgn)) tn += gridDim.x;
+            const bool more = tn < ntiles;
+            if (more) stage_tile_prefetch<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(An, orgn, next_h, l0h);
+            stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, cur_h, work, wred);
+            __syncthreads();
+            if (!more) break;
+            stage_tile_prefetch_finish<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(An, next_h, l0h);
+            C* tmp = cur_h;
+            cur_h = next_h;
+            next_h = tmp;
+            A = An;
+            org[0] = orgn[0];
+            org[1] = orgn[1];
+            org[2] = orgn[2];
+            t = tn;
         }
-        const int org[3] = {tile.y, tile.z, tile.w};
-        stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
-        __syncthreads();
+    } else {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            StageArgs A;
+            int org[3];
+            if (!batch_tile_args(B, t, A, org)) continue;
+            stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
+            __syncthreads();
+        }
     }
 }
 

@@ -58,7 +58,12 @@ struct StageEntry {
 template <int EQ, int FLUX, int RC, int DIM>
 struct BatchEntry {
     using TS = TileShape<DIM, FV_VARIANT>;
-    using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    using SL0 = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
+    // the pipelined ensemble kernel (storage = arithmetic type) double-buffers the halo
+    struct SL {
+        static constexpr size_t bytes =
+            SL0::bytes + (std::is_same<Real, Compute>::value ? SL0::prefetch_bytes : (size_t)0);
+    };
     static int launch(const BatchArgs& a, int ctas, cudaStream_t s) {
         auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, Compute>;
         static int resident = 0;
