@@ -29,6 +29,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + C
 
 VARIANTS = (0, 1, 2, 3)   # fp64, fp64 exact, fp32, fp64 state with double-float arithmetic
 EQUATIONS = (0, 1, 2, 3)  # burgers, euler1, euler2, euler3
+TUNED_VARIANTS = (0, 1, 2)  # variants with autotuning candidates (TMA staging needs storage = arithmetic type)
 
 
 def _nvcc():
@@ -45,7 +46,10 @@ def _units():
             flags = ["-DFV_VARIANT=%d" % v, "-DFV_EQ=%d" % e]
             if v == 1:
                 flags += ["-DFV_EXACT", "-fmad=false"]
-            units.append(("fv_variant.cu", "fv_v%d_e%d.o" % (v, e), flags))
+            units.append(("fv_variant.cu", "fv_v%d_e%d.o" % (v, e), flags + ["-DFV_PART=0"]))
+            if v in TUNED_VARIANTS:
+                units.append(("fv_variant.cu", "fv_v%d_e%d_tune.o" % (v, e), flags + ["-DFV_PART=1"]))
+    units.append(("gbfv_tune.cu", "gbfv_tune.o", []))
     units.append(("gbfv_api.cu", "gbfv_api.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_stats.cu", "gbfv_stats.o", []))
     units.append(("gbfv_structure.cu", "gbfv_structure.o", []))

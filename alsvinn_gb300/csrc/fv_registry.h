@@ -21,7 +21,9 @@ inline bool flux_applies(int eq, int fl) {
     return fl == FL_HLL || fl == FL_HLL3 || fl == FL_CENTRAL;
 }
 
-typedef int (*StageLauncher)(const StageArgs& a, cudaStream_t s);
+// Single-grid stage launch; `maps` holds the tensor maps of a.in and a.l0
+// for the TMA-staged kernels (null otherwise).
+typedef int (*StageLauncher)(const StageArgs& a, const TmaMaps* maps, cudaStream_t s);
 typedef int (*ApplyLauncher)(const StageArgs& a, cudaStream_t s);
 
 typedef int (*ReconLauncher)(const ReconArgs& a, cudaStream_t s);
@@ -31,16 +33,35 @@ typedef int (*CheckLauncher)(const CheckArgs& a, cudaStream_t s);
 // Persistent ensemble stage launch: grid = ctas (0: one wave of resident CTAs).
 typedef int (*BatchLauncher)(const BatchArgs& a, int ctas, cudaStream_t s);
 
+// One compiled configuration of a scheme's stage kernels: the tile shape,
+// the threads per CTA (a thread owns cells / threads cells when the tile has
+// more cells than threads) and how the tile + halo reaches shared memory
+// (TMA box copies or per-thread loads). Candidate 0 of every scheme is the
+// default; the autotuner times the others on the caller's grid.
+struct StageCandidate {
+    StageLauncher stage;
+    BatchLauncher batch;
+    int tile[3];
+    int threads;
+    int tma;      // 1: the kernels stage the halo by TMA (needs tensor maps)
+    int halo[3];  // TMA box: the tile plus the ghost halo in each active dimension
+    int nv;       // variables per cell (the box's fourth extent)
+};
+constexpr int kMaxCandidates = 6;
+
 struct Registry {
-    // [variant][equation][flux][recon][dim-1]
-    StageLauncher stage[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
+    // [variant][equation][flux][recon][dim-1][candidate]
+    StageCandidate cand[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3][kMaxCandidates];
+    int ncand[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
     ApplyLauncher apply[NUM_VARIANTS][NUM_EQ];
     ReconLauncher recon[NUM_VARIANTS][NUM_EQ][NUM_RECON];
     CheckLauncher check[NUM_VARIANTS][NUM_EQ];
-    BatchLauncher batch[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
-    size_t stage_smem[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
 };
 
 Registry& registry();
+
+// The candidates of one scheme (candidate 0 first); *count = 0 when the
+// scheme has no kernel.
+const StageCandidate* candidates(int var, int eq, int fl, int rc, int dim, int* count);
 
 }  // namespace gbfv

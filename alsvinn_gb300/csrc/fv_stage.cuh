@@ -23,6 +23,7 @@
 
 #include "fv_df.cuh"
 #include "fv_math.cuh"
+#include "fv_tma.cuh"
 #include "fv_types.h"
 
 namespace gbfv {
@@ -136,9 +137,31 @@ struct SmemLayout {
     static constexpr int FAC1 = DIM > 1 ? TX * (TY + 1) * TZ : 0;
     static constexpr int FAC2 = DIM > 2 ? TX * TY * (TZ + 1) : 0;
     static constexpr int FAC = FAC0 > FAC1 ? (FAC0 > FAC2 ? FAC0 : FAC2) : (FAC1 > FAC2 ? FAC1 : FAC2);
-    static constexpr size_t bytes = sizeof(R) * ((size_t)NV * HALO + 2 * (size_t)NV * REC + (size_t)NV * FAC);
-    // the ensemble kernel's second halo buffer and L0 halo
-    static constexpr size_t prefetch_bytes = sizeof(R) * 2 * (size_t)NV * HALO;
+    static constexpr size_t round128(size_t b) { return (b + 127) & ~(size_t)127; }
+    static constexpr size_t box_bytes = sizeof(R) * (size_t)NV * HALO;  // one halo of every variable
+    static constexpr size_t halo_bytes = round128(box_bytes);           // its slot (TMA wants 128 B aligned)
+    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NV * REC + (size_t)NV * FAC);
+    // Dynamic shared memory per kernel, plus 128 bytes to align the base:
+    //   plain staging:    halo | line buffers
+    //   TMA staging:      halo | line buffers, which first hold the L0 halo of the stage-1 modes
+    //   ensemble (R = C): halo A | halo B | L0 halo | line buffers
+    static constexpr size_t bytes = 128 + halo_bytes + work_bytes;
+    static constexpr size_t tma_bytes = 128 + halo_bytes + (work_bytes > halo_bytes ? work_bytes : halo_bytes);
+    static constexpr size_t pipe_bytes = 128 + 3 * halo_bytes + work_bytes;
+};
+
+// The dynamic shared memory base rounded up to 128 bytes.
+__device__ __forceinline__ unsigned char* align_smem(unsigned char* p) {
+    return p + ((128u - (smem_addr(p) & 127u)) & 127u);
+}
+
+// Cells of the tile each thread owns in the accumulate and combine phases:
+// thread t owns cells t, t + NTH, ... (NTH >= cells: one cell for the first
+// `cells` threads; the rest join the reconstruction and flux phases only).
+template <int NT, int NTH> struct CellsPerThread {
+    static_assert(NTH % 32 == 0, "whole warps");
+    static_assert(NT <= NTH || NT % NTH == 0, "a whole number of cells per thread");
+    static constexpr int value = NT <= NTH ? 1 : NT / NTH;
 };
 
 
@@ -149,7 +172,7 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
-    constexpr int NT = TX * TY * TZ;  // cells of the tile (NTH threads >= NT)
+    constexpr int NT = TX * TY * TZ;  // cells of the tile
     constexpr int TD = D == 0 ? TX : (D == 1 ? TY : TZ);
     constexpr int O1 = D == 0 ? TY : TX;          // extent of the first other dimension
     constexpr int LEN = TD + 2;
@@ -233,9 +256,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         if (valid) wsmax = fmax_(wsmax, w);
     }
     __syncthreads();
-    // this thread's cell: acc += (-F_{i+1/2}) + F_{i-1/2}
-    if (tid < NT) {
-        const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
+    // this thread's cells: acc += (-F_{i+1/2}) + F_{i-1/2}
+    constexpr int CPT = CellsPerThread<NT, NTH>::value;
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+        const int cell = tid + j * NTH;
+        if (cell >= NT) continue;
+        const int cx = cell % TX, cy = (cell / TX) % TY, cz = cell / (TX * TY);
         const int cd = D == 0 ? cx : (D == 1 ? cy : cz);
         const int p = D == 0 ? cy : cx;
         const int q = D == 2 ? cy : cz;
@@ -247,9 +274,9 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
             const R fl = fc[k * NFACE + fli];
             const R fr = fc[k * NFACE + fri];
             if constexpr (!kExact && D == 0)
-                acc[k] = fl - fr;  // the first direction starts the sum
+                acc[j * NV + k] = fl - fr;  // the first direction starts the sum
             else
-                acc[k] = acc[k] + ((-fr) + fl);
+                acc[j * NV + k] = acc[j * NV + k] + ((-fr) + fl);
         }
     }
     __syncthreads();
@@ -374,7 +401,7 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     constexpr int G = ReconTraits<RC>::ghosts;
     using SL = SmemLayout<C, NV, G, DIM, TX, TY, TZ>;
     constexpr int NT = TX * TY * TZ;  // cells of the tile
-    static_assert(NT <= NTH && NTH % 32 == 0, "one thread per cell at least, whole warps");
+    constexpr int CPT = CellsPerThread<NT, NTH>::value;
     constexpr bool kSame = std::is_same<R, C>::value;
     C* rl = work;
     C* rr = rl + NV * SL::REC;
@@ -390,10 +417,10 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     const int mode = A.mode;
     const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
 
-    // 2. flux difference per direction
-    C acc[NV];
+    // 2. flux difference per direction, per owned cell
+    C acc[CPT * NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = C(0);
+    for (int k = 0; k < CPT * NV; ++k) acc[k] = C(0);
     // wave-speed maxima in the arithmetic type (the max is exact, so one
     // conversion per thread gives the same double as converting every face)
     C wsd[3] = {C(0), C(0), C(0)};
@@ -423,17 +450,21 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
         }
     }
 
-    // 4. this thread's cell: combine and write with its ghost images
-    if (tid >= NT) return;  // no barrier follows
-    const int cx = tid % TX, cy = (tid / TX) % TY, cz = tid / (TX * TY);
+    // 4. this thread's cells: combine and write with their ghost images (no
+    // barrier follows)
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+    const int cell = tid + j * NTH;
+    if (cell >= NT) continue;
+    const int cx = cell % TX, cy = (cell / TX) % TY, cz = cell / (TX * TY);
     const int ix = org[0] + cx, iy = org[1] + cy, iz = org[2] + cz;
-    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) return;  // no barrier follows
+    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) continue;
     const int sidx = ((cz + SL::GZ) * SL::HY + (cy + SL::GY)) * SL::HX + (cx + SL::GX);
     const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
     R res[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const R acck = (R)acc[k];
+        const R acck = (R)acc[j * NV + k];
         if (mode == MODE_L) {
             res[k] = acck;
         } else {
@@ -461,31 +492,99 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
         }
     }
     if (A.check && !PhR::obeys(res, uniform_value<R>(A.gamma, A.gamma_f))) {
-        if (atomicExch(&A.st->status, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
+        if (atomicCAS(&A.st->status, 0, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
+    }
+}
+
+// TMA staging of one tile (thread 0 only): the halo box of the stage input
+// into su and, for the stage-1 modes, that of L0 into l0s, both signalling
+// bar. `global_maps`: the maps live in global memory, written by the host.
+template <class R, class SL, int DIM>
+__device__ __forceinline__ void tma_stage_issue(const StageArgs& A, const CUtensorMap* tm_in, const CUtensorMap* tm_l0,
+                                                const int* org, R* su, R* l0s, unsigned long long* bar,
+                                                bool global_maps) {
+    const bool s1 = A.mode == MODE_RK3_S1 || A.mode == MODE_RK2_S1;
+    if (global_maps) {
+        fence_tensormap_acquire(tm_in);
+        if (s1) fence_tensormap_acquire(tm_l0);
+    }
+    // earlier generic accesses of su / l0s (the previous tile) before the copies
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, (unsigned)((s1 ? 2 : 1) * SL::box_bytes));
+    tma_load_halo<DIM>(su, tm_in, bar, org[0], org[1], org[2]);
+    if (s1) tma_load_halo<DIM>(l0s, tm_l0, bar, org[0], org[1], org[2]);
+}
+
+// Every thread: waits for the TMA staging of phase `phase`, then the stage-1
+// modes form U1 = L0 c + U0 in su. Returns false (the same for every thread)
+// when the copies did not complete within the time limit; the step state then
+// records kStatusTmaTimeout and the caller returns without touching su.
+template <class R, class SL, int NTH>
+__device__ __forceinline__ bool tma_stage_finish(const StageArgs& A, R* su, const R* l0s, unsigned long long* bar,
+                                                 unsigned phase) {
+    constexpr int NV = (int)(SL::box_bytes / (sizeof(R) * SL::HALO));
+    if (!__syncthreads_and(mbar_wait_bounded(bar, phase))) {
+        if (threadIdx.x == 0 && atomicCAS(&A.st->status, 0, kStatusTmaTimeout) == 0)
+            A.st->failed_step = (int)A.st->steps + 1;
+        mbar_wait_bounded(bar, phase);  // copies still in flight get the time limit once more
+        return false;
+    }
+    if (A.mode == MODE_RK3_S1 || A.mode == MODE_RK2_S1) {
+        const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
+        for (int w = threadIdx.x; w < SL::HALO; w += NTH) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = madd(l0s[k * SL::HALO + w], scale, su[k * SL::HALO + w]);
+        }
+        __syncthreads();
+    }
+    return true;
 }
 
 // One tile of one stage with a synchronous halo load. Shared memory: the halo
 // tile, then the line buffers.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
-__device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* smem_raw,
-                                           C* wred) {
+__device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, unsigned char* base, C* wred) {
     constexpr int NV = Physics<C, EQ, FLUX>::NV;
     using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
-    C* su = reinterpret_cast<C*>(smem_raw);
+    C* su = reinterpret_cast<C*>(base);
     stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, su);
-    stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, su, su + NV * SL::HALO, wred);
+    stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, su,
+                                                                 reinterpret_cast<C*>(base + SL::halo_bytes), wred);
 }
 
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
 __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
     C* wred = reinterpret_cast<C*>(wred_raw);
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
-    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
+    stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, align_smem(smem_raw), wred);
+}
+
+// The single-grid stage with the tile + halo staged by TMA (storage type =
+// arithmetic type). The maps are kernel parameters; shared memory: halo, then
+// the line buffers, which hold the L0 halo until U1 is formed.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH>
+__global__ void __launch_bounds__(NTH) stage_kernel_tma(StageArgs A, const __grid_constant__ TmaMaps M) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(R)];
+    __shared__ __align__(8) unsigned long long bar;
+    constexpr int NV = Physics<R, EQ, FLUX>::NV;
+    using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    R* wred = reinterpret_cast<R*>(wred_raw);
+    if (A.st->done) return;
+    unsigned char* base = align_smem(smem_raw);
+    R* su = reinterpret_cast<R*>(base);
+    R* work = reinterpret_cast<R*>(base + SL::halo_bytes);
+    const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) tma_stage_issue<R, SL, DIM>(A, &M.in, &M.l0, org, su, work, &bar, false);
+    if (!tma_stage_finish<R, SL, NTH>(A, su, work, &bar, 0)) return;
+    stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, R>(A, org, su, work, wred);
 }
 
 // The stage arguments of ensemble tile t (its member's buffers for the stage
@@ -515,6 +614,10 @@ __device__ __forceinline__ bool batch_tile_args(const BatchArgs& B, int t, Stage
     } else {  // MODE_RK2_S1
         A.in = cur; A.u0 = cur; A.l0 = m.l; A.out = other; A.check = 1;
     }
+    // the member's tensor maps: [0] u, [1] v, [2] l
+    const CUtensorMap* mm = (B.maps && m.tma) ? B.maps + 3 * tile.x : nullptr;
+    A.tm_in = mm ? mm + ((B.mode == MODE_RK3_S2) != (st->parity != 0) ? 1 : 0) : nullptr;
+    A.tm_l0 = mm ? mm + 2 : nullptr;
     org[0] = tile.y;
     org[1] = tile.z;
     org[2] = tile.w;
@@ -525,53 +628,99 @@ __device__ __forceinline__ bool batch_tile_args(const BatchArgs& B, int t, Stage
 // member grid, heterogeneous sizes) with stride gridDim.x. A member whose run
 // is done is skipped as a whole; the per-member wave-speed maxima land in
 // that member's step state (a segmented reduction), so every member gets its
-// own dt.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
-__global__ void __launch_bounds__(NTH, (std::is_same<C, float>::value ? 5 : 1)) batch_stage_kernel(BatchArgs B) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+// own dt. With storage type = arithmetic type the CTA runs a software
+// pipeline: the next tile's halo streams into a second buffer (TMA when the
+// kernel is built for it and the member has tensor maps, cp.async otherwise)
+// while the current tile computes.
+// Resident CTAs per SM the FP32 ensemble kernel is compiled for (register
+// cap): 1280 threads, or fewer CTAs when their shared memory does not fit.
+template <class C, int NTH, size_t SMEM> struct BatchMinBlocks {
+    static constexpr int by_threads = 1280 / NTH > 0 ? 1280 / NTH : 1;
+    static constexpr int by_smem = (int)((225 * 1024) / SMEM) > 0 ? (int)((225 * 1024) / SMEM) : 1;
+    static constexpr int value =
+        std::is_same<C, float>::value ? (by_threads < by_smem ? by_threads : by_smem) : 1;
+};
+
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R, bool TMA = false>
+__global__ void __launch_bounds__(
+    NTH, (BatchMinBlocks<C, NTH,
+                         SmemLayout<C, Physics<C, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>::pipe_bytes>::value))
+    batch_stage_kernel(BatchArgs B) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
+    __shared__ __align__(8) unsigned long long bar;
     C* wred = reinterpret_cast<C*>(wred_raw);
+    unsigned char* base = align_smem(smem_raw);
     const int ntiles = *B.ntiles;
     if constexpr (std::is_same<R, C>::value) {
-        // Software pipeline: the next tile's halo streams into the second
-        // halo buffer (cp.async) while the current tile computes. Shared
-        // memory: halo A, halo B, L0 halo, line buffers.
+        // shared memory: halo A, halo B, L0 halo, line buffers
         constexpr int NV = Physics<C, EQ, FLUX>::NV;
         using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
-        C* cur_h = reinterpret_cast<C*>(smem_raw);
-        C* next_h = cur_h + NV * SL::HALO;
-        C* l0h = next_h + NV * SL::HALO;
-        C* work = l0h + NV * SL::HALO;
-        StageArgs A, An;
-        int org[3], orgn[3];
+        C* cur_h = reinterpret_cast<C*>(base);
+        C* next_h = reinterpret_cast<C*>(base + SL::halo_bytes);
+        C* l0h = reinterpret_cast<C*>(base + 2 * SL::halo_bytes);
+        C* work = reinterpret_cast<C*>(base + 3 * SL::halo_bytes);
+        if constexpr (TMA) {
+            if (threadIdx.x == 0) mbar_init(&bar, 1);
+            __syncthreads();
+        }
+        unsigned phase = 0;
+        StageArgs A;
+        int org[3];
         int t = blockIdx.x;
         while (t < ntiles && !batch_tile_args(B, t, A, org)) t += gridDim.x;
         if (t >= ntiles) return;
-        stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, cur_h);
+        if (TMA && A.tm_in) {
+            if (threadIdx.x == 0) tma_stage_issue<R, SL, DIM>(A, A.tm_in, A.tm_l0, org, cur_h, l0h, &bar, true);
+            if (!tma_stage_finish<R, SL, NTH>(A, cur_h, l0h, &bar, phase)) return;
+            phase ^= 1u;
+        } else {
+            stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, cur_h);
+        }
         while (true) {
+            // issue the next tile's staging; only its index and kind stay
+            // live across the compute phase (its arguments are rebuilt after)
             int tn = t + gridDim.x;
-            while (tn < ntiles && !batch_tile_args(B, tn, An, orgn)) tn += gridDim.x;
-            const bool more = tn < ntiles;
-            if (more) stage_tile_prefetch<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(An, orgn, next_h, l0h);
+            bool next_tma = false;
+            {
+                StageArgs An;
+                int orgn[3];
+                while (tn < ntiles && !batch_tile_args(B, tn, An, orgn)) tn += gridDim.x;
+                if (tn < ntiles) {
+                    next_tma = TMA && An.tm_in != nullptr;
+                    if (next_tma) {
+                        if (threadIdx.x == 0)
+                            tma_stage_issue<R, SL, DIM>(An, An.tm_in, An.tm_l0, orgn, next_h, l0h, &bar, true);
+                    } else {
+                        stage_tile_prefetch<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(An, orgn, next_h, l0h);
+                    }
+                }
+            }
             stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, cur_h, work, wred);
+            // this thread's generic writes of the halo buffers (U1 combine,
+            // edge fill) before later TMA writes into them
+            if constexpr (TMA) fence_proxy_async_smem();
             __syncthreads();
-            if (!more) break;
-            stage_tile_prefetch_finish<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(An, next_h, l0h);
+            if (tn >= ntiles) break;
+            batch_tile_args(B, tn, A, org);  // the member's done flag is fixed during the launch
+            if (next_tma) {
+                if (!tma_stage_finish<R, SL, NTH>(A, next_h, l0h, &bar, phase)) return;
+                phase ^= 1u;
+            } else {
+                stage_tile_prefetch_finish<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>(A, next_h, l0h);
+            }
             C* tmp = cur_h;
             cur_h = next_h;
             next_h = tmp;
-            A = An;
-            org[0] = orgn[0];
-            org[1] = orgn[1];
-            org[2] = orgn[2];
             t = tn;
         }
     } else {
+        (void)bar;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             StageArgs A;
             int org[3];
             if (!batch_tile_args(B, t, A, org)) continue;
-            stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, smem_raw, wred);
+            stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, base, wred);
             __syncthreads();
         }
     }

@@ -1,6 +1,7 @@
 // Types shared by the kernel translation units and the C-ABI layer: grid
 // geometry, the device-resident step state and the launch argument blocks.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace gbfv {
@@ -137,11 +138,21 @@ __device__ __forceinline__ void store_with_images(R* out, long long total, const
 }
 
 
+// Tensor maps of one single-grid stage launch, passed by value as a
+// __grid_constant__ kernel parameter (TMA halo staging): the stage input and,
+// for the stage-1 modes, the stage-0 flux difference L0.
+struct TmaMaps {
+    CUtensorMap in;
+    CUtensorMap l0;
+};
+
 struct StageArgs {
     const void* in;   // U (MODE_L, MODE_RK3_S2) or U0 (stage-1 modes)
     const void* u0;   // U0 for the combination
     const void* l0;   // L0 for stage-1 modes
     void* out;
+    const CUtensorMap* tm_in;  // tensor maps of in and l0 (TMA staging; null: plain loads)
+    const CUtensorMap* tm_l0;
     StepState* st;
     Grid G;
     double gamma;
@@ -178,6 +189,7 @@ struct BatchMember {
     void* v;  // second state buffer
     void* l;  // stage-0 flux difference
     Grid G;
+    int tma;  // the member's tensor maps (u, v, l) are valid for the launch's halo box
 };
 
 // Arguments of one ensemble stage launch. tiles[i] = (member, ox, oy, oz);
@@ -188,6 +200,7 @@ struct BatchArgs {
     StepState* states;
     const int4* tiles;
     const int* ntiles;
+    const CUtensorMap* maps;  // per member slot s: maps[3 s + {0, 1, 2}] of u, v, l
     double gamma;
     float gamma_f;
     int mode;

@@ -1,6 +1,9 @@
 // Kernel instantiations for one arithmetic variant and one equation. This file
-// is compiled once per (FV_VARIANT, FV_EQ) pair; the exact variant is built
-// with -fmad=false and FV_EXACT so that no multiply-add is contracted.
+// is compiled twice per (FV_VARIANT, FV_EQ) pair (FV_PART 0: every scheme's
+// default stage kernels and the operator-level kernels; FV_PART 1: the
+// autotuning candidates), so the units build in parallel; the exact variant
+// is built with -fmad=false and FV_EXACT so that no multiply-add is
+// contracted.
 //   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic,
 //               3 fp64 state with double-float arithmetic on the FP32 pipes
 //   FV_EQ:      0 burgers, 1 euler1, 2 euler2, 3 euler3
@@ -30,55 +33,92 @@ typedef gbfv::dfloat Compute;
 typedef Real Compute;
 #endif
 
+#ifndef FV_PART
+#define FV_PART 0  // 0: default candidates and the other launchers, 1: autotuning candidates
+#endif
+
 #define FV_CAT2(a, b, c, d) a##b##c##d
 #define FV_CAT(a, b, c, d) FV_CAT2(a, b, c, d)
 #define FV_REGISTER_FN FV_CAT(gbfv_register_v, FV_VARIANT, _e, FV_EQ)
+#define FV_TUNE_FN FV_CAT(gbfv_tune_v, FV_VARIANT, _e, FV_EQ)
 
 namespace gbfv {
 namespace GBFV_VARIANT_NS {
 
-template <int EQ, int FLUX, int RC, int DIM>
-struct StageEntry {
-    using TS = TileShape<DIM, FV_VARIANT>;
-    using SL = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
-    static int launch(const StageArgs& a, cudaStream_t s) {
-        auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, Compute>;
-        static int configured = 0;
-        if (!configured) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
-            if (e != cudaSuccess) return (int)e;
-            configured = 1;
+// One candidate configuration of a scheme's stage kernels (tile TX x TY x TZ,
+// NTH threads, TMA or plain halo staging) and its launchers.
+template <int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, bool TMA>
+struct Cand {
+    static constexpr int NV = Physics<Real, EQ, FLUX>::NV;
+    static constexpr int G = ReconTraits<RC>::ghosts;
+    using SL = SmemLayout<Compute, NV, G, DIM, TX, TY, TZ>;
+    static constexpr bool kSame = std::is_same<Real, Compute>::value;
+    static_assert(!TMA || kSame, "TMA staging copies the storage type into shared memory");
+    static_assert(!TMA || (SL::HX * sizeof(Real)) % 16 == 0, "a TMA box row must be a multiple of 16 bytes");
+    static_assert(!TMA || (TX * sizeof(Real)) % 16 == 0, "TMA box origins must be 16-byte aligned along x");
+    static_assert(!TMA || (SL::HX <= 256 && SL::HY <= 256 && SL::HZ <= 256), "TMA box extents are at most 256");
+    static constexpr size_t stage_smem = TMA ? SL::tma_bytes : SL::bytes;
+    // the ensemble kernel pipelines the halo when storage and arithmetic types agree
+    static constexpr size_t batch_smem = kSame ? SL::pipe_bytes : SL::bytes;
+
+    static int launch(const StageArgs& a, const TmaMaps* maps, cudaStream_t s) {
+        const dim3 grid((a.G.n[0] + TX - 1) / TX, (a.G.n[1] + TY - 1) / TY, (a.G.n[2] + TZ - 1) / TZ);
+        if constexpr (TMA) {
+            if (!maps) return (int)cudaErrorInvalidValue;
+            auto k = stage_kernel_tma<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>;
+            static int configured = 0;
+            if (!configured) {
+                cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_smem);
+                if (e != cudaSuccess) return (int)e;
+                configured = 1;
+            }
+            k<<<grid, NTH, stage_smem, s>>>(a, *maps);
+        } else {
+            auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute>;
+            static int configured = 0;
+            if (!configured) {
+                cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_smem);
+                if (e != cudaSuccess) return (int)e;
+                configured = 1;
+            }
+            k<<<grid, NTH, stage_smem, s>>>(a);
         }
-        dim3 grid((a.G.n[0] + TS::X - 1) / TS::X, (a.G.n[1] + TS::Y - 1) / TS::Y, (a.G.n[2] + TS::Z - 1) / TS::Z);
-        k<<<grid, TS::THREADS, SL::bytes, s>>>(a);
         return (int)cudaGetLastError();
     }
-};
 
-template <int EQ, int FLUX, int RC, int DIM>
-struct BatchEntry {
-    using TS = TileShape<DIM, FV_VARIANT>;
-    using SL0 = SmemLayout<Compute, Physics<Real, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TS::X, TS::Y, TS::Z>;
-    // the pipelined ensemble kernel (storage = arithmetic type) double-buffers the halo
-    struct SL {
-        static constexpr size_t bytes =
-            SL0::bytes + (std::is_same<Real, Compute>::value ? SL0::prefetch_bytes : (size_t)0);
-    };
-    static int launch(const BatchArgs& a, int ctas, cudaStream_t s) {
-        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, Compute>;
+    static int launch_batch(const BatchArgs& a, int ctas, cudaStream_t s) {
+        auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute, TMA>;
         static int resident = 0;
         if (!resident) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem);
             if (e != cudaSuccess) return (int)e;
             int per_sm = 0, dev = 0, sms = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TS::THREADS, SL::bytes);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NTH, batch_smem);
             if (e == cudaSuccess) e = cudaGetDevice(&dev);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return (int)e;
             resident = (per_sm > 0 ? per_sm : 1) * sms;
         }
-        k<<<ctas > 0 ? ctas : resident, TS::THREADS, SL::bytes, s>>>(a);
+        k<<<ctas > 0 ? ctas : resident, NTH, batch_smem, s>>>(a);
         return (int)cudaGetLastError();
+    }
+
+    static void add(Registry& R, int flux, int rc) {
+        constexpr int V = FV_VARIANT, E = EQ;
+        int& n = R.ncand[V][E][flux][rc][DIM - 1];
+        if (n >= kMaxCandidates) return;
+        StageCandidate& c = R.cand[V][E][flux][rc][DIM - 1][n++];
+        c.stage = &launch;
+        c.batch = &launch_batch;
+        c.tile[0] = TX;
+        c.tile[1] = TY;
+        c.tile[2] = TZ;
+        c.threads = NTH;
+        c.tma = TMA ? 1 : 0;
+        c.halo[0] = SL::HX;
+        c.halo[1] = SL::HY;
+        c.halo[2] = SL::HZ;
+        c.nv = NV;
     }
 };
 
@@ -151,12 +191,12 @@ static int launch_check(const CheckArgs& a, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
+#if FV_PART == 0
+// The default candidate of a scheme: the variant's tile shape, plain loads.
 template <int FLUX, int RC, int DIM>
 static void reg_one(Registry& R) {
-    constexpr int V = FV_VARIANT, E = FV_EQ;
-    R.stage[V][E][FLUX][RC][DIM - 1] = &StageEntry<E, FLUX, RC, DIM>::launch;
-    R.batch[V][E][FLUX][RC][DIM - 1] = &BatchEntry<E, FLUX, RC, DIM>::launch;
-    R.stage_smem[V][E][FLUX][RC][DIM - 1] = StageEntry<E, FLUX, RC, DIM>::SL::bytes;
+    using TS = TileShape<DIM, FV_VARIANT>;
+    Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false>::add(R, FLUX, RC);
 }
 
 // Every reconstruction for one flux in one dimension. The double-float
@@ -177,10 +217,40 @@ static void reg_dim(Registry& R) {
 #endif
 #endif
 }
+#else
+// Autotuning candidates of the tuned schemes (WENO2 with HLL3 for Euler in
+// its own dimension, WENO2 with Godunov for 1D Burgers): TMA staging of the
+// default tile, taller / wider tiles with two cells per thread, and square
+// tiles; 1D adds narrower tiles, which give small grids more CTAs. Every
+// candidate computes the same values in the same order per cell (the tile
+// only changes which CTA computes a cell), so the states are bit-identical.
+template <int FLUX, int DIM>
+static void reg_tuned(Registry& R) {
+    constexpr int E = FV_EQ, RC = RC_WENO2;
+    if constexpr (DIM == 1) {
+        Cand<E, FLUX, RC, 1, 128, 1, 1, 128, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 1, 64, 1, 1, 64, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 1, 32, 1, 1, 32, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 1, 240, 1, 1, 256, true>::add(R, FLUX, RC);
+    } else if constexpr (DIM == 2) {
+        Cand<E, FLUX, RC, 2, 32, 8, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 16, 16, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 64, 8, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 16, 1, 512, true>::add(R, FLUX, RC);
+    } else {
+        Cand<E, FLUX, RC, 3, 8, 8, 4, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 3, 16, 8, 4, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 3, 8, 8, 8, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 3, 16, 16, 2, 256, true>::add(R, FLUX, RC);
+    }
+}
+#endif
 
 }  // namespace GBFV_VARIANT_NS
 }  // namespace gbfv
 
+#if FV_PART == 0
 extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     using namespace gbfv;
     using namespace gbfv::GBFV_VARIANT_NS;
@@ -220,3 +290,18 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     R->recon[V][E][RC_WENOF2] = &launch_recon<E, RC_WENOF2>;
 #endif
 }
+#else
+// Runs after the default registration (candidate 0 first).
+extern "C" void FV_TUNE_FN(gbfv::Registry* R) {
+    using namespace gbfv;
+    using namespace gbfv::GBFV_VARIANT_NS;
+#if FV_VARIANT != 3
+#if FV_EQ == 0
+    reg_tuned<FL_GODUNOV, 1>(*R);
+#else
+    reg_tuned<FL_HLL3, FV_EQ>(*R);
+#endif
+#endif
+    (void)R;
+}
+#endif

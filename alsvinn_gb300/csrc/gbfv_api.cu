@@ -4,6 +4,7 @@
 // primitive-to-conserved conversion round exactly as the reference does.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -12,27 +13,44 @@
 #include <vector>
 
 #include "fv_registry.h"
+#include "fv_tma.cuh"
 #include "gbfv.h"
+#include "gbfv_internal.h"
 
 #define GBFV_REGISTER_DECL(v, e) extern "C" void gbfv_register_v##v##_e##e(gbfv::Registry*);
 GBFV_REGISTER_DECL(0, 0) GBFV_REGISTER_DECL(0, 1) GBFV_REGISTER_DECL(0, 2) GBFV_REGISTER_DECL(0, 3)
 GBFV_REGISTER_DECL(1, 0) GBFV_REGISTER_DECL(1, 1) GBFV_REGISTER_DECL(1, 2) GBFV_REGISTER_DECL(1, 3)
 GBFV_REGISTER_DECL(2, 0) GBFV_REGISTER_DECL(2, 1) GBFV_REGISTER_DECL(2, 2) GBFV_REGISTER_DECL(2, 3)
 GBFV_REGISTER_DECL(3, 0) GBFV_REGISTER_DECL(3, 1) GBFV_REGISTER_DECL(3, 2) GBFV_REGISTER_DECL(3, 3)
+#define GBFV_TUNE_DECL(v, e) extern "C" void gbfv_tune_v##v##_e##e(gbfv::Registry*);
+GBFV_TUNE_DECL(0, 0) GBFV_TUNE_DECL(0, 1) GBFV_TUNE_DECL(0, 2) GBFV_TUNE_DECL(0, 3)
+GBFV_TUNE_DECL(1, 0) GBFV_TUNE_DECL(1, 1) GBFV_TUNE_DECL(1, 2) GBFV_TUNE_DECL(1, 3)
+GBFV_TUNE_DECL(2, 0) GBFV_TUNE_DECL(2, 1) GBFV_TUNE_DECL(2, 2) GBFV_TUNE_DECL(2, 3)
 
 namespace gbfv {
 
 Registry& registry() {
-    static Registry R = [] {
-        Registry r;
-        std::memset(&r, 0, sizeof r);
-        gbfv_register_v0_e0(&r); gbfv_register_v0_e1(&r); gbfv_register_v0_e2(&r); gbfv_register_v0_e3(&r);
-        gbfv_register_v1_e0(&r); gbfv_register_v1_e1(&r); gbfv_register_v1_e2(&r); gbfv_register_v1_e3(&r);
-        gbfv_register_v2_e0(&r); gbfv_register_v2_e1(&r); gbfv_register_v2_e2(&r); gbfv_register_v2_e3(&r);
-        gbfv_register_v3_e0(&r); gbfv_register_v3_e1(&r); gbfv_register_v3_e2(&r); gbfv_register_v3_e3(&r);
+    // ~1 MB of launcher table: built once on the heap
+    static Registry* R = [] {
+        Registry* r = new Registry();
+        std::memset(r, 0, sizeof *r);
+        gbfv_register_v0_e0(r); gbfv_register_v0_e1(r); gbfv_register_v0_e2(r); gbfv_register_v0_e3(r);
+        gbfv_register_v1_e0(r); gbfv_register_v1_e1(r); gbfv_register_v1_e2(r); gbfv_register_v1_e3(r);
+        gbfv_register_v2_e0(r); gbfv_register_v2_e1(r); gbfv_register_v2_e2(r); gbfv_register_v2_e3(r);
+        gbfv_register_v3_e0(r); gbfv_register_v3_e1(r); gbfv_register_v3_e2(r); gbfv_register_v3_e3(r);
+        // autotuning candidates after every default
+        gbfv_tune_v0_e0(r); gbfv_tune_v0_e1(r); gbfv_tune_v0_e2(r); gbfv_tune_v0_e3(r);
+        gbfv_tune_v1_e0(r); gbfv_tune_v1_e1(r); gbfv_tune_v1_e2(r); gbfv_tune_v1_e3(r);
+        gbfv_tune_v2_e0(r); gbfv_tune_v2_e1(r); gbfv_tune_v2_e2(r); gbfv_tune_v2_e3(r);
         return r;
     }();
-    return R;
+    return *R;
+}
+
+const StageCandidate* candidates(int var, int eq, int fl, int rc, int dim, int* count) {
+    Registry& R = registry();
+    *count = R.ncand[var][eq][fl][rc][dim - 1];
+    return R.cand[var][eq][fl][rc][dim - 1];
 }
 
 // ------------------------------------------------------- step kernels
@@ -229,6 +247,13 @@ struct gbfv_solver {
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;  // stage launches while profiling
     std::vector<cudaEvent_t> event_pool;
+    // stage kernel configuration: the candidate in use (-1: chosen by the
+    // autotuner at the first advance) and its tensor maps of U, V, L
+    int cand = -1;
+    bool pinned = false;  // set by gbfv_select_candidate: the autotuner leaves it alone
+    CUtensorMap tm[3];
+    bool tm_ok = false;
+    std::vector<double> tune_ms;  // the autotuner's MODE_L time per candidate (-1: not eligible)
 };
 
 static size_t state_bytes(const gbfv_solver* s) { return (size_t)s->nvar * s->G.total * s->elem; }
@@ -291,8 +316,9 @@ int gbfv_create(const gbfv_desc* d, gbfv_solver** out) {
     const int g = kReconGhosts[rc];
     for (int k = 0; k < dim; ++k)
         if (d->n[k] < g) return fail(GBFV_ERR_UNSUPPORTED, "every active dimension needs at least as many cells as ghost cells");
-    Registry& R = registry();
-    if (!R.stage[d->precision][eq][fl][rc][dim - 1]) return fail(GBFV_ERR_UNSUPPORTED, "no kernel for this combination");
+    int ncand = 0;
+    candidates(d->precision, eq, fl, rc, dim, &ncand);
+    if (ncand == 0) return fail(GBFV_ERR_UNSUPPORTED, "no kernel for this combination");
 
     gbfv_solver* s = new gbfv_solver();
     s->eq = eq; s->fl = fl; s->rc = rc; s->in = in; s->periodic = bc; s->var = d->precision;
@@ -479,6 +505,8 @@ static StageArgs stage_args(gbfv_solver* s, StepState* st, const void* in, const
     a.G = s->G;
     a.gamma = s->gamma;
     a.gamma_f = (float)s->gamma;
+    a.tm_in = nullptr;
+    a.tm_l0 = nullptr;
     a.mode = mode;
     a.periodic = s->periodic;
     a.check = check;
@@ -496,15 +524,36 @@ static cudaEvent_t take_event(gbfv_solver* s) {
     return e;
 }
 
+// Tensor maps of a stage launch on the solver's own buffers (U, V, L).
+static const CUtensorMap* solver_map(const gbfv_solver* s, const void* p) {
+    if (p == s->U) return &s->tm[0];
+    if (p == s->V) return &s->tm[1];
+    if (p == s->L) return &s->tm[2];
+    return nullptr;
+}
+
+// Launches candidate c of the solver's scheme; TMA candidates get the maps of
+// a.in and a.l0 (which must be the solver's buffers).
+static int launch_candidate(gbfv_solver* s, const StageCandidate& c, const StageArgs& a) {
+    if (!c.tma) return c.stage(a, nullptr, s->stream);
+    const CUtensorMap* mi = solver_map(s, a.in);
+    const CUtensorMap* ml = a.l0 ? solver_map(s, a.l0) : mi;
+    if (!s->tm_ok || !mi || !ml) return (int)cudaErrorInvalidValue;
+    TmaMaps m;
+    m.in = *mi;
+    m.l0 = *ml;
+    return c.stage(a, &m, s->stream);
+}
+
 // One stage launch, bracketed by events while profiling.
-static int launch_stage(gbfv_solver* s, StageLauncher stage, const StageArgs& a) {
+static int launch_stage(gbfv_solver* s, const StageCandidate& c, const StageArgs& a) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (s->profiling) {
         e0 = take_event(s);
         e1 = take_event(s);
         CUDA_TRY(cudaEventRecord(e0, s->stream));
     }
-    LAUNCH_TRY(stage(a, s->stream));
+    LAUNCH_TRY(launch_candidate(s, c, a));
     s->launches += 1;
     if (s->profiling) {
         CUDA_TRY(cudaEventRecord(e1, s->stream));
@@ -522,7 +571,8 @@ static int launch_stage(gbfv_solver* s, StageLauncher stage, const StageArgs& a)
 // Enqueues one time step; every kernel returns at once when st->done is set.
 static int enqueue_step(gbfv_solver* s, const StepParams& P) {
     Registry& R = registry();
-    const StageLauncher stage = R.stage[s->var][s->eq][s->fl][s->rc][s->G.dim - 1];
+    int ncand = 0;
+    const StageCandidate& stage = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &ncand)[s->cand < 0 ? 0 : s->cand];
     cudaStream_t q = s->stream;
     STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->U, s->U, nullptr, s->L, MODE_L, 0)));
     dt_kernel<<<1, 1, 0, q>>>(s->st, P);
@@ -549,7 +599,13 @@ static int enqueue_step(gbfv_solver* s, const StepParams& P) {
     return GBFV_OK;
 }
 
+static int tune(gbfv_solver* s, bool force);
+
 static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
+    if (s->cand < 0 && !s->pinned) {
+        const int r = tune(s, false);
+        if (r) return r;
+    }
     begin_kernel<<<1, 1, 0, s->stream>>>(s->st, P.end_time, limit);
     CUDA_TRY(cudaGetLastError());
     s->launches += 1;
@@ -566,6 +622,12 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
         // (done), leaving the state and the saved mask as that step left them
         if (chunk < 64) chunk *= 2;
     }
+    if (s->st_host->status == kStatusTmaTimeout) {
+        char msg[256];
+        snprintf(msg, sizeof msg, "a TMA halo copy did not complete within the time limit (step %d)",
+                 s->st_host->failed_step);
+        return fail(GBFV_ERR_CUDA, msg);
+    }
     if (s->st_host->status != 0) {
         char msg[256];
         snprintf(msg, sizeof msg,
@@ -574,6 +636,78 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
         return fail(GBFV_ERR_CONSTRAINT, msg);
     }
     return GBFV_OK;
+}
+
+// Makes candidate idx current: encodes its tensor maps of U, V, L (TMA
+// candidates whose maps cannot be encoded are refused).
+static int use_candidate(gbfv_solver* s, int idx) {
+    int n = 0;
+    const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
+    if (idx < 0 || idx >= n) return fail(GBFV_ERR_ARGUMENT, "no such stage kernel candidate");
+    if (c[idx].tma) {
+        CUtensorMap m[3];
+        void* bufs[3] = {s->U, s->V, s->L};
+        for (int k = 0; k < 3; ++k)
+            if (!gbfv_encode_state_map(&m[k], bufs[k], s->G, s->nvar, s->elem, c[idx].halo[0], c[idx].halo[1],
+                                       c[idx].halo[2]))
+                return fail(GBFV_ERR_UNSUPPORTED, "this grid cannot be staged by TMA (padded rows must be multiples of 16 bytes)");
+        std::memcpy(s->tm, m, sizeof m);
+        s->tm_ok = true;
+    }
+    s->cand = idx;
+    return GBFV_OK;
+}
+
+// The autotuner: times MODE_L launches of every candidate on the solver's
+// current state (out = L, a scratch step state: no effect on the solve) and
+// keeps the fastest; the choice is cached per scheme and grid for the
+// process. GBFV_AUTOTUNE=0 in the environment keeps candidate 0.
+static int tune(gbfv_solver* s, bool force) {
+    int n = 0;
+    const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
+    s->tune_ms.assign(n, -1.0);
+    char key[160];
+    snprintf(key, sizeof key, "solver:%d:%d:%d:%d:%d:%d:%d:%d", s->var, s->eq, s->fl, s->rc, s->in, s->G.n[0],
+             s->G.n[1], s->G.n[2]);
+    int best = 0;
+    if (n <= 1 || !gbfv_autotune_enabled()) return use_candidate(s, 0);
+    if (!force && gbfv_tune_cache_get(key, &best) && use_candidate(s, best) == GBFV_OK) return GBFV_OK;
+    StepState z;
+    std::memset(&z, 0, sizeof z);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    double best_ms = 0;
+    best = 0;
+    const int kTimed = 3;
+    int err = GBFV_OK;
+    for (int i = 0; i < n && err == GBFV_OK; ++i) {
+        if (use_candidate(s, i) != GBFV_OK) continue;  // not eligible (TMA rules)
+        const StageArgs a = stage_args(s, s->st_op, s->U, s->U, nullptr, s->L, MODE_L, 0);
+        cudaError_t e = cudaMemcpyAsync(s->st_op, &z, sizeof z, cudaMemcpyHostToDevice, s->stream);
+        int r = e == cudaSuccess ? launch_candidate(s, c[i], a) : (int)e;  // warm-up
+        if (!r) r = (int)cudaEventRecord(e0, s->stream);
+        for (int k = 0; k < kTimed && !r; ++k) r = launch_candidate(s, c[i], a);
+        if (!r) r = (int)cudaEventRecord(e1, s->stream);
+        if (!r) r = (int)cudaEventSynchronize(e1);
+        float ms = 0;
+        if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+        if (r) {
+            err = fail(GBFV_ERR_CUDA, std::string("autotuning launch: ") + cudaGetErrorString((cudaError_t)r));
+            break;
+        }
+        s->launches += 1 + kTimed;
+        s->tune_ms[i] = ms / kTimed;
+        if (i == 0 || s->tune_ms[i] < best_ms) {
+            best_ms = s->tune_ms[i];
+            best = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err) return err;
+    gbfv_tune_cache_put(key, best);
+    return use_candidate(s, best);
 }
 
 static StepParams step_params(const gbfv_solver* s, double end_time) {
@@ -618,6 +752,53 @@ int gbfv_advance_schedule(gbfv_solver* s, const gbfv_schedule* sch, int* saved_m
 int gbfv_stream(gbfv_solver* s, void** stream) {
     if (!s || !stream) return fail(GBFV_ERR_ARGUMENT, "null argument");
     *stream = (void*)s->stream;
+    return GBFV_OK;
+}
+
+int gbfv_candidate_count(gbfv_solver* s, int* count) {
+    if (!s || !count) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, count);
+    return GBFV_OK;
+}
+
+int gbfv_candidate_info(gbfv_solver* s, int idx, int tile[3], int* threads, int* tma) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    int n = 0;
+    const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
+    if (idx < 0 || idx >= n) return fail(GBFV_ERR_ARGUMENT, "no such stage kernel candidate");
+    if (tile)
+        for (int k = 0; k < 3; ++k) tile[k] = c[idx].tile[k];
+    if (threads) *threads = c[idx].threads;
+    if (tma) *tma = c[idx].tma;
+    return GBFV_OK;
+}
+
+int gbfv_select_candidate(gbfv_solver* s, int idx) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    if (idx < 0) {
+        s->cand = -1;
+        s->pinned = false;
+        return GBFV_OK;
+    }
+    const int r = use_candidate(s, idx);
+    if (r == GBFV_OK) s->pinned = true;
+    return r;
+}
+
+int gbfv_current_candidate(gbfv_solver* s, int* idx) {
+    if (!s || !idx) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    *idx = s->cand;
+    return GBFV_OK;
+}
+
+int gbfv_autotune(gbfv_solver* s, int* chosen, double* ms, int capacity) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    const int r = tune(s, true);
+    if (r) return r;
+    s->pinned = false;
+    if (chosen) *chosen = s->cand;
+    if (ms)
+        for (int i = 0; i < capacity; ++i) ms[i] = i < (int)s->tune_ms.size() ? s->tune_ms[i] : -1.0;
     return GBFV_OK;
 }
 
@@ -671,9 +852,9 @@ int gbfv_compute_flux(gbfv_solver* s, const void* U, void* out, double ws[3]) {
     StepState z;
     std::memset(&z, 0, sizeof z);
     CUDA_TRY(cudaMemcpyAsync(s->st_op, &z, sizeof z, cudaMemcpyHostToDevice, s->stream));
-    Registry& R = registry();
-    LAUNCH_TRY(R.stage[s->var][s->eq][s->fl][s->rc][s->G.dim - 1](
-        stage_args(s, s->st_op, U, U, nullptr, out, MODE_L, 0), s->stream));
+    int ncand = 0;
+    const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &ncand);
+    LAUNCH_TRY(c[0].stage(stage_args(s, s->st_op, U, U, nullptr, out, MODE_L, 0), nullptr, s->stream));
     CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st_op, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     if (ws)
@@ -832,11 +1013,15 @@ int gbfv_internal_begin(StepState* st, double end_time, long long step_limit, cu
 int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* st, const StepParams& P,
                        cudaStream_t q) {
     Registry& R = registry();
-    const StageLauncher stage = R.stage[p.var][p.eq][p.fl][p.rc][p.G.dim - 1];
+    int ncand = 0;
+    // caller buffers: the default candidate (plain halo loads, no tensor maps)
+    const StageLauncher launch0 = candidates(p.var, p.eq, p.fl, p.rc, p.G.dim, &ncand)[0].stage;
+    auto stage = [&](const StageArgs& a, cudaStream_t qq) { return launch0(a, nullptr, qq); };
     auto args = [&](const void* in, const void* u0, const void* l0, void* out, int mode, int check) {
         StageArgs a;
         a.in = in; a.u0 = u0; a.l0 = l0; a.out = out; a.st = st; a.G = p.G; a.gamma = p.gamma;
         a.gamma_f = (float)p.gamma;
+        a.tm_in = nullptr; a.tm_l0 = nullptr;
         a.mode = mode; a.periodic = p.periodic; a.check = check;
         return a;
     };

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "fv_registry.h"
+#include "fv_tma.cuh"
 #include "gbfv_internal.h"
 
 using namespace gbfv;
@@ -205,6 +206,16 @@ struct gbfv_batch {
     cudaGraphExec_t step_graph = nullptr;
     int graph_chunk = 0;
     long long launches = 0;
+    // stage kernel configuration: the candidate in use, whether the
+    // autotuner has settled it (or the caller pinned it), and the members'
+    // tensor maps for its halo box (3 per slot: u, v, l)
+    int cand = 0;
+    bool tuned = false;
+    bool pinned = false;
+    std::vector<CUtensorMap> h_maps;
+    CUtensorMap* d_maps = nullptr;
+    StepState* d_tune_states = nullptr;
+    std::vector<double> tune_ms;
 };
 
 namespace {
@@ -217,7 +228,34 @@ int bfail(int code, const std::string& m) { return gbfv_internal_fail(code, m.c_
         if (e_ != cudaSuccess) return bfail(GBFV_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-int tile_shape(const gbfv_batch* b, int k) { return tile_extent(b->scheme.var, b->dim, k); }
+const StageCandidate& current(const gbfv_batch* b) {
+    int n = 0;
+    const GbfvPlan& p = b->scheme;
+    return candidates(p.var, p.eq, p.fl, p.rc, b->dim, &n)[b->cand];
+}
+
+int tile_shape(const gbfv_batch* b, int k) { return current(b).tile[k]; }
+
+// Host side: the tensor maps of member `slot` for the current candidate's
+// halo box; the member keeps plain loads when they cannot be encoded.
+void encode_member_maps(gbfv_batch* b, int slot) {
+    auto& h = b->members[slot];
+    const StageCandidate& c = current(b);
+    h.m.tma = 0;
+    if (!h.active || !c.tma) return;
+    void* bufs[3] = {h.m.u, h.m.v, h.m.l};
+    for (int k = 0; k < 3; ++k)
+        if (!gbfv_encode_state_map(&b->h_maps[3 * slot + k], bufs[k], h.m.G, b->scheme.nvar, b->scheme.elem,
+                                   c.halo[0], c.halo[1], c.halo[2]))
+            return;
+    h.m.tma = 1;
+}
+
+int upload_maps(gbfv_batch* b, int first, int count) {
+    BCUDA(cudaMemcpyAsync(b->d_maps + 3 * first, &b->h_maps[3 * first], (size_t)3 * count * sizeof(CUtensorMap),
+                          cudaMemcpyHostToDevice, b->stream));
+    return GBFV_OK;
+}
 
 int rebuild_tiles(gbfv_batch* b) {
     std::vector<int4> tiles;
@@ -265,15 +303,15 @@ int upload_members(gbfv_batch* b) {
 
 // One ensemble time step (the body of the captured graph).
 int enqueue_batch_step(gbfv_batch* b) {
-    Registry& R = registry();
     const GbfvPlan& p = b->scheme;
-    const BatchLauncher launch = R.batch[p.var][p.eq][p.fl][p.rc][b->dim - 1];
+    const BatchLauncher launch = current(b).batch;
     if (!launch) return bfail(GBFV_ERR_UNSUPPORTED, "no ensemble kernel for this scheme and precision");
     BatchArgs a;
     a.members = b->d_members;
     a.states = b->d_states;
     a.tiles = b->d_tiles;
     a.ntiles = b->d_ntiles;
+    a.maps = b->d_maps;
     a.gamma = p.gamma;
     a.gamma_f = (float)p.gamma;
     a.periodic = p.periodic;
@@ -314,6 +352,116 @@ int enqueue_batch_step(gbfv_batch* b) {
     return GBFV_OK;
 }
 
+// Makes candidate idx current: members' tensor maps re-encoded for its halo
+// box, tile list rebuilt for its tile shape, the step graph dropped.
+int set_candidate(gbfv_batch* b, int idx) {
+    int n = 0;
+    const GbfvPlan& p = b->scheme;
+    candidates(p.var, p.eq, p.fl, p.rc, b->dim, &n);
+    if (idx < 0 || idx >= n) return bfail(GBFV_ERR_ARGUMENT, "no such stage kernel candidate");
+    if (idx == b->cand) return GBFV_OK;
+    BCUDA(cudaStreamSynchronize(b->stream));
+    b->cand = idx;
+    for (int s = 0; s < b->max_members; ++s) encode_member_maps(b, s);
+    int r = upload_maps(b, 0, b->max_members);
+    if (!r) r = upload_members(b);
+    if (r) return r;
+    b->tiles_dirty = true;
+    if (b->step_graph) {
+        cudaGraphExecDestroy(b->step_graph);
+        b->step_graph = nullptr;
+    }
+    return GBFV_OK;
+}
+
+// Interior cells of the members that still run (the tuning workload).
+long long running_cells(const gbfv_batch* b) {
+    long long c = 0;
+    for (int s = 0; s < b->max_members; ++s) {
+        const auto& h = b->members[s];
+        if (!h.active || b->h_states[s].done) continue;
+        c += (long long)h.m.G.n[0] * h.m.G.n[1] * h.m.G.n[2];
+    }
+    return c;
+}
+
+// The ensemble autotuner: with the step states of the current advance on the
+// device (after the begin kernel), times MODE_L launches of every candidate
+// over the running members (out = each member's L buffer, wave speeds into a
+// copy of the step states: no effect on the run) and keeps the fastest. The
+// choice is cached per scheme for the process; ensembles below 2^22 running
+// cells keep their current candidate and are tuned at a later advance (small
+// ensembles are launch-latency bound and time every candidate alike).
+int tune_batch(gbfv_batch* b, bool force) {
+    const GbfvPlan& p = b->scheme;
+    int n = 0;
+    candidates(p.var, p.eq, p.fl, p.rc, b->dim, &n);
+    b->tune_ms.assign(n, -1.0);
+    if (n <= 1 || !gbfv_autotune_enabled()) {
+        b->tuned = true;
+        return set_candidate(b, 0);
+    }
+    char key[128];
+    snprintf(key, sizeof key, "batch:%d:%d:%d:%d:%d:%d", p.var, p.eq, p.fl, p.rc, p.in, b->dim);
+    int best = 0;
+    if (!force && gbfv_tune_cache_get(key, &best)) {
+        b->tuned = true;
+        return set_candidate(b, best);
+    }
+    if (!force && running_cells(b) < (1LL << 22)) return GBFV_OK;
+    const int M = b->max_members;
+    if (!b->d_tune_states) BCUDA(cudaMalloc(&b->d_tune_states, M * sizeof(StepState)));
+    cudaEvent_t e0, e1;
+    BCUDA(cudaEventCreate(&e0));
+    BCUDA(cudaEventCreate(&e1));
+    double best_ms = 0;
+    int err = GBFV_OK;
+    const int kTimed = 2;
+    for (int i = 0; i < n && !err; ++i) {
+        err = set_candidate(b, i);
+        if (!err) err = rebuild_tiles(b);
+        if (err) break;
+        BatchArgs a;
+        a.members = b->d_members;
+        a.states = b->d_tune_states;
+        a.tiles = b->d_tiles;
+        a.ntiles = b->d_ntiles;
+        a.maps = b->d_maps;
+        a.gamma = p.gamma;
+        a.gamma_f = (float)p.gamma;
+        a.periodic = p.periodic;
+        a.mode = MODE_L;
+        const BatchLauncher launch = current(b).batch;
+        cudaError_t e = cudaMemcpyAsync(b->d_tune_states, b->d_states, M * sizeof(StepState),
+                                        cudaMemcpyDeviceToDevice, b->stream);
+        int r = e == cudaSuccess ? launch(a, 0, b->stream) : (int)e;  // warm-up
+        if (!r) r = (int)cudaEventRecord(e0, b->stream);
+        for (int k = 0; k < kTimed && !r; ++k) r = launch(a, 0, b->stream);
+        if (!r) r = (int)cudaEventRecord(e1, b->stream);
+        if (!r) r = (int)cudaEventSynchronize(e1);
+        float ms = 0;
+        if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+        if (r) {
+            err = bfail(GBFV_ERR_CUDA, std::string("ensemble autotuning launch: ") + cudaGetErrorString((cudaError_t)r));
+            break;
+        }
+        b->launches += 1 + kTimed;
+        b->tune_ms[i] = ms / kTimed;
+        if (i == 0 || b->tune_ms[i] < best_ms) {
+            best_ms = b->tune_ms[i];
+            best = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err) return err;
+    gbfv_tune_cache_put(key, best);
+    b->tuned = true;
+    err = set_candidate(b, best);
+    if (!err) err = rebuild_tiles(b);
+    return err;
+}
+
 }  // namespace
 
 extern "C" {
@@ -352,6 +500,7 @@ int gbfv_batch_create(const gbfv_desc* scheme, long long pool_bytes, int max_mem
     if (e == cudaSuccess) e = cudaMalloc(&b->d_members, max_members * sizeof(BatchMember));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_params, max_members * sizeof(MemberParam));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_states, max_members * sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_maps, (size_t)3 * max_members * sizeof(CUtensorMap));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_states, max_members * sizeof(StepState));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_list, max_members * sizeof(int2));
@@ -376,7 +525,10 @@ int gbfv_batch_create(const gbfv_desc* scheme, long long pool_bytes, int max_mem
     }
     b->capacity = (size_t)pool_bytes;
     b->free_blocks[0] = b->capacity;
-    int rr = upload_members(b);
+    b->h_maps.resize((size_t)3 * max_members);
+    std::memset(b->h_maps.data(), 0, b->h_maps.size() * sizeof(CUtensorMap));
+    int rr = upload_maps(b, 0, max_members);
+    if (!rr) rr = upload_members(b);
     if (rr) {
         gbfv_batch_destroy(b);
         return rr;
@@ -398,6 +550,8 @@ int gbfv_batch_destroy(gbfv_batch* b) {
     cudaFree(b->d_members);
     cudaFree(b->d_params);
     cudaFree(b->d_states);
+    cudaFree(b->d_maps);
+    cudaFree(b->d_tune_states);
     cudaFree(b->d_tiles);
     cudaFree(b->d_ntiles);
     cudaFree(b->d_list);
@@ -519,7 +673,9 @@ int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const d
     z.group = group;
     b->h_states[slot] = z;
     BCUDA(cudaMemcpyAsync(b->d_states + slot, &b->h_states[slot], sizeof(StepState), cudaMemcpyHostToDevice, b->stream));
-    r = upload_members(b);
+    encode_member_maps(b, slot);
+    r = upload_maps(b, slot, 1);
+    if (!r) r = upload_members(b);
     if (r) return r;
     b->tiles_dirty = true;
     *slot_out = slot;
@@ -582,6 +738,10 @@ int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int 
     BCUDA(cudaGetLastError());
     BCUDA(cudaMemcpyAsync(b->h_states, b->d_states, M * sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
     BCUDA(cudaStreamSynchronize(b->stream));
+    if (!b->tuned && !b->pinned) {
+        r = tune_batch(b, false);
+        if (r) return r;
+    }
     b->tiles_dirty = true;
     r = rebuild_tiles(b);
     if (r) return r;
@@ -628,6 +788,13 @@ int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int 
     BCUDA(cudaMemcpyAsync(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost,
                           b->stream));
     BCUDA(cudaStreamSynchronize(b->stream));
+    for (int s = 0; s < M; ++s)
+        if (b->members[s].active && b->h_states[s].status == kStatusTmaTimeout) {
+            char msg[256];
+            snprintf(msg, sizeof msg, "member %d: a TMA halo copy did not complete within the time limit (step %d)",
+                     s, b->h_states[s].failed_step);
+            return bfail(GBFV_ERR_CUDA, msg);
+        }
     for (int s = 0; s < M; ++s)
         if (b->members[s].active && b->h_states[s].status != 0) {
             char msg[256];
@@ -735,6 +902,35 @@ int gbfv_batch_active(const gbfv_batch* b, int* count) {
 int gbfv_batch_launches(gbfv_batch* b, long long* launches) {
     if (!b || !launches) return bfail(GBFV_ERR_ARGUMENT, "null argument");
     *launches = b->launches;
+    return GBFV_OK;
+}
+
+int gbfv_batch_select_candidate(gbfv_batch* b, int idx) {
+    if (!b) return bfail(GBFV_ERR_ARGUMENT, "null batch");
+    if (idx < 0) {
+        b->pinned = false;
+        b->tuned = false;
+        return GBFV_OK;
+    }
+    const int r = set_candidate(b, idx);
+    if (r == GBFV_OK) b->pinned = true;
+    return r;
+}
+
+int gbfv_batch_current_candidate(gbfv_batch* b, int* idx, int* member_tma) {
+    if (!b || !idx) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    *idx = b->cand;
+    if (member_tma) {
+        int c = 0;
+        for (int s = 0; s < b->max_members; ++s) c += (b->members[s].active && b->members[s].m.tma) ? 1 : 0;
+        *member_tma = c;
+    }
+    return GBFV_OK;
+}
+
+int gbfv_batch_autotune_result(gbfv_batch* b, double* ms, int capacity) {
+    if (!b || (capacity > 0 && !ms)) return bfail(GBFV_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < capacity; ++i) ms[i] = i < (int)b->tune_ms.size() ? b->tune_ms[i] : -1.0;
     return GBFV_OK;
 }
 

@@ -26,3 +26,10 @@ int gbfv_internal_prim_to_cons(const gbfv::GbfvPlan& p, const double* prim, doub
 int gbfv_internal_load_state(const gbfv::GbfvPlan& p, const double* host, void* dev, cudaStream_t q);
 int gbfv_internal_step(const gbfv::GbfvPlan& p, void* U, void* V, void* L, gbfv::StepState* st,
                        const gbfv::StepParams& P, cudaStream_t q);
+
+// Autotuner support (gbfv_tune.cu): GBFV_AUTOTUNE=0 in the environment
+// disables tuning; the cache maps a scheme / grid key to the chosen candidate
+// for the life of the process (thread safe).
+int gbfv_autotune_enabled();
+bool gbfv_tune_cache_get(const char* key, int* cand);
+void gbfv_tune_cache_put(const char* key, int cand);

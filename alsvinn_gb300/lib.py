@@ -118,6 +118,17 @@ _SIGNATURES = {
     "gbfv_batch_stats_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "gbfv_batch_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_batch_select_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_batch_current_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                                    ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_batch_autotune_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "gbfv_candidate_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_candidate_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_select_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                     ctypes.c_int]),
+    "gbfv_current_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "gbfv_init_sod": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                      ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "gbfv_init_kelvin_helmholtz": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
@@ -355,6 +366,38 @@ class Solver:
     def profile(self, enable=True):
         _check(load().gbfv_profile(self.h, 1 if enable else 0))
 
+    # -- stage kernel candidates and the autotuner -------------------------
+
+    def candidates(self):
+        """[(tile (x, y, z), threads, tma)] of the scheme's stage kernel
+        configurations; index 0 is the default."""
+        n = ctypes.c_int()
+        _check(load().gbfv_candidate_count(self.h, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            tile = (ctypes.c_int * 3)()
+            th, tma = ctypes.c_int(), ctypes.c_int()
+            _check(load().gbfv_candidate_info(self.h, i, tile, ctypes.byref(th), ctypes.byref(tma)))
+            out.append((tuple(tile), th.value, bool(tma.value)))
+        return out
+
+    def select_candidate(self, idx):
+        """Pins candidate idx (-1: let the autotuner choose at the next advance)."""
+        _check(load().gbfv_select_candidate(self.h, int(idx)))
+
+    def current_candidate(self):
+        i = ctypes.c_int()
+        _check(load().gbfv_current_candidate(self.h, ctypes.byref(i)))
+        return i.value
+
+    def autotune(self):
+        """Runs the autotuner now: (chosen index, [ms per MODE_L launch or -1])."""
+        n = len(self.candidates())
+        ms = (ctypes.c_double * max(n, 1))()
+        chosen = ctypes.c_int()
+        _check(load().gbfv_autotune(self.h, ctypes.byref(chosen), ms, n))
+        return chosen.value, list(ms)[:n]
+
     def profile_read(self):
         ms = ctypes.c_double()
         n = ctypes.c_longlong()
@@ -562,6 +605,21 @@ class Batch:
         p = ctypes.c_void_p()
         _check(load().gbfv_batch_stream(self.h, ctypes.byref(p)))
         return p.value
+
+    def select_candidate(self, idx):
+        """Pins stage kernel candidate idx for the ensemble (-1: autotuner)."""
+        _check(load().gbfv_batch_select_candidate(self.h, int(idx)))
+
+    def current_candidate(self):
+        """(candidate index, members staged by TMA)."""
+        i, m = ctypes.c_int(), ctypes.c_int()
+        _check(load().gbfv_batch_current_candidate(self.h, ctypes.byref(i), ctypes.byref(m)))
+        return i.value, m.value
+
+    def autotune_result(self, n=6):
+        ms = (ctypes.c_double * n)()
+        _check(load().gbfv_batch_autotune_result(self.h, ms, n))
+        return list(ms)
 
 
 REQUEST_BURGERS, REQUEST_KELVIN_HELMHOLTZ = 0, 1

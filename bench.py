@@ -200,6 +200,14 @@ def run_gpu(args):
     stream = torch.cuda.ExternalStream(s.stream())
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
+    # the autotuner (the same one the first advance runs), its table reported
+    chosen, tune_ms = s.autotune()
+    cands = s.candidates()
+    stage_kernel = {"candidate": chosen, "tile": list(cands[chosen][0]), "threads": cands[chosen][1],
+                    "tma": cands[chosen][2],
+                    "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
+                                               for c, m in zip(cands, tune_ms)]}
+
     # warm-up
     s.advance(2.0, 0, args.warmup)
     torch.cuda.synchronize()
@@ -298,7 +306,9 @@ def run_gpu(args):
     achieved = alg_bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profile_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "stage_kernel<double,euler2,hll3,weno2,2D>", "launch_ms": per_launch_ms,
+                "kernel": "%s<double,euler2,hll3,weno2,2D> tile %dx%d, %d threads" % (
+                    "stage_kernel_tma" if stage_kernel["tma"] else "stage_kernel", stage_kernel["tile"][0],
+                    stage_kernel["tile"][1], stage_kernel["threads"]), "launch_ms": per_launch_ms,
                 "alg_bytes_per_launch": alg_bytes_per_launch,
                 "note": "FP64 arithmetic on GB300 issues at ~1/64 of the FP32 rate; this step is FP64-compute "
                         "bound, not HBM bound",
@@ -318,7 +328,8 @@ def run_gpu(args):
                 "config": {"workload": WORKLOAD, "grid": [N, N], "equation": "euler2", "reconstruction": "weno2",
                            "flux": "hll3", "integrator": "rungekutta3", "precision": "fp64",
                            "l2": "flushed before every timed step (512 MiB memset, outside the events)",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "stage_kernel": stage_kernel},
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clk,
                 "gpu_launches": int(launches1 - launches0), "fp64_df": df,
                 "sim": {"t": t_sim, "steps": steps_done}}
@@ -380,11 +391,20 @@ def run_uq(args):
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = b.launches() - launches0
+    cand, tma_members = b.current_candidate()
+    tune_ms = b.autotune_result()
     cells = float(sum(int(n) ** 2 for n in sizes))
     rate = cells * args.steps / (ms * 1e-3)
     work_to_T = sum((int(n) ** 2) * (T / dts[int(n)]) for n in sizes)
     samples_per_s = S * rate / work_to_T
     b.close()
+    probe = lib.Solver(*scheme, (128, 128, 1), (0, 0, 0), (1, 1, 0), precision=lib.FP32)
+    cands = probe.candidates()
+    probe.close()
+    stage_kernel = {"candidate": cand, "tile": list(cands[cand][0]), "threads": cands[cand][1],
+                    "tma": cands[cand][2], "members_staged_by_tma": tma_members,
+                    "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
+                                               for c, m in zip(cands, tune_ms)]}
 
     # plain FP64, one solve at a time, each size
     plain_step_ms = {}
@@ -410,7 +430,8 @@ def run_uq(args):
             "data": "synthetic (seeded KH perturbation per member, generator sample = member index)",
             "config": {"workload": "uq_kh_%d_samples_128_256_512_fp32" % S, "samples": S,
                        "size_counts": {str(n): int((sizes == n).sum()) for n in sizes_choice},
-                       "end_time": T, "l2": "working set %.1f GB >> L2" % (pool / 1e9)},
+                       "end_time": T, "l2": "working set %.1f GB >> L2" % (pool / 1e9),
+                       "stage_kernel": stage_kernel},
             "batched_cell_updates_per_s": rate,
             "plain_fp64_one_at_a_time_samples_per_s": plain_samples_per_s,
             "speedup_vs_plain_fp64": samples_per_s / plain_samples_per_s,

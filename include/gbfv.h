@@ -150,6 +150,27 @@ int gbfv_profile_read(gbfv_solver* s, double* stage_ms, long long* stage_launche
 /* Time, step count and the dt of the last step. */
 int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt);
 
+/* Stage kernel candidates and the autotuner (no counterpart in the
+ * reference, whose CUDA kernels use fixed launch shapes). A scheme has one
+ * or more compiled configurations of its stage kernels: tile shape, threads
+ * per CTA (threads < cells: several cells per thread) and halo staging by TMA
+ * box copies (tma = 1) or per-thread loads. Candidate 0 is the default. At
+ * the first advance the autotuner times every eligible candidate on the
+ * solver's state and keeps the fastest (cached per scheme and grid for the
+ * process; GBFV_AUTOTUNE=0 in the environment keeps candidate 0). Every
+ * candidate gives bit-identical states. TMA candidates need padded rows
+ * (t_x * element size) that are multiples of 16 bytes.
+ *   gbfv_select_candidate: pin candidate idx (-1: back to the autotuner);
+ *     GBFV_ERR_UNSUPPORTED when the grid cannot be staged by TMA.
+ *   gbfv_autotune: tune now; ms[i] = the candidate's time per MODE_L launch
+ *     (-1: not eligible), *chosen = the candidate kept.
+ *   gbfv_current_candidate: the candidate in use (-1: not chosen yet). */
+int gbfv_candidate_count(gbfv_solver* s, int* count);
+int gbfv_candidate_info(gbfv_solver* s, int idx, int tile[3], int* threads, int* tma);
+int gbfv_select_candidate(gbfv_solver* s, int idx);
+int gbfv_autotune(gbfv_solver* s, int* chosen, double* ms, int capacity);
+int gbfv_current_candidate(gbfv_solver* s, int* idx);
+
 /* Same as gbfv_advance, reading the state from host memory first and writing
  * it back after: the call a host-side Volume owner makes per step. */
 int gbfv_advance_host(gbfv_solver* s, double* state_host_inout, double end_time, int number_of_saves,
@@ -281,6 +302,21 @@ int gbfv_batch_active(const gbfv_batch* b, int* count);
 /* Kernels launched by the ensemble since creation, and its CUDA stream. */
 int gbfv_batch_launches(gbfv_batch* b, long long* launches);
 int gbfv_batch_stream(gbfv_batch* b, void** stream);
+
+/* Stage kernel candidates of the ensemble (the same set as the single-grid
+ * solver's for the scheme). The autotuner runs at the first advance whose
+ * running members hold at least 2^22 cells (or finds the process's cached
+ * choice for the scheme); smaller ensembles keep candidate 0 until then.
+ * Members whose arrays break a TMA rule stage their halo with per-thread
+ * loads inside a TMA candidate.
+ *   gbfv_batch_select_candidate: pin candidate idx (-1: back to the autotuner).
+ *   gbfv_batch_current_candidate: the candidate in use; *member_tma = members
+ *     staged by TMA.
+ *   gbfv_batch_autotune_result: per candidate the time of one MODE_L launch
+ *     over the running members when the autotuner ran (-1: not timed). */
+int gbfv_batch_select_candidate(gbfv_batch* b, int idx);
+int gbfv_batch_current_candidate(gbfv_batch* b, int* idx, int* member_tma);
+int gbfv_batch_autotune_result(gbfv_batch* b, double* ms, int capacity);
 
 /* ----------------------------------------------------------- serving */
 
