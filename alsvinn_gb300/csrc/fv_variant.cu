@@ -1,9 +1,11 @@
 // Kernel instantiations for one arithmetic variant and one equation. This file
 // is compiled twice per (FV_VARIANT, FV_EQ) pair (FV_PART 0: every scheme's
 // default stage kernels and the operator-level kernels; FV_PART 1: the
-// autotuning candidates), so the units build in parallel; the exact variant
-// is built with -fmad=false and FV_EXACT so that no multiply-add is
-// contracted.
+// autotuning candidates), so the units build in parallel. The fp64, fp64
+// exact and fp32 variants are built with -fmad=false: no multiply-add is
+// contracted unless the source writes the FMA, so every candidate of a
+// scheme rounds alike; the exact variant (FV_EXACT) writes none and follows
+// the reference's operation order.
 //   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic,
 //               3 fp64 state with double-float arithmetic on the FP32 pipes
 //   FV_EQ:      0 burgers, 1 euler1, 2 euler2, 3 euler3
@@ -220,8 +222,10 @@ static void reg_dim(Registry& R) {
 #else
 // Autotuning candidates of the tuned schemes (WENO2 with HLL3 for Euler in
 // its own dimension, WENO2 with Godunov for 1D Burgers): TMA staging of the
-// default tile, taller / wider tiles with two cells per thread, and square
-// tiles; 1D adds narrower tiles, which give small grids more CTAs. Every
+// default tile, taller / wider tiles with two cells per thread, a square
+// tile and a 32 x 12 tile on 384 threads (less halo work per cell than 32 x 8
+// at the same 24 resident warps per SM for FP64); 1D adds narrower tiles,
+// which give small grids more CTAs. Every
 // candidate computes the same values in the same order per cell (the tile
 // only changes which CTA computes a cell), so the states are bit-identical.
 template <int FLUX, int DIM>
@@ -237,7 +241,7 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 16, 16, 1, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 64, 8, 1, 256, true>::add(R, FLUX, RC);
-        Cand<E, FLUX, RC, 2, 32, 16, 1, 512, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 12, 1, 384, true>::add(R, FLUX, RC);
     } else {
         Cand<E, FLUX, RC, 3, 8, 8, 4, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 3, 16, 8, 4, 256, true>::add(R, FLUX, RC);

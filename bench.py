@@ -200,9 +200,14 @@ def run_gpu(args):
     stream = torch.cuda.ExternalStream(s.stream())
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
-    # the autotuner (the same one the first advance runs), its table reported
-    chosen, tune_ms = s.autotune()
+    # the autotuner (the same one the first advance runs), its table reported;
+    # --candidate pins one configuration instead (reproducible profiler runs)
     cands = s.candidates()
+    if args.candidate >= 0:
+        s.select_candidate(args.candidate)
+        chosen, tune_ms = args.candidate, [-1.0] * len(cands)
+    else:
+        chosen, tune_ms = s.autotune()
     stage_kernel = {"candidate": chosen, "tile": list(cands[chosen][0]), "threads": cands[chosen][1],
                     "tma": cands[chosen][2],
                     "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
@@ -365,6 +370,8 @@ def run_uq(args):
     b0.close()
     t0 = time.perf_counter()
     b = lib.Batch(*scheme, pool, S, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    if args.candidate >= 0:
+        b.select_candidate(args.candidate)
     slots = []
     for s in range(S):
         n = int(sizes[s])
@@ -548,6 +555,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64-df", "fp64-exact"])
     ap.add_argument("--no-df", action="store_true", help="skip the double-float measurement")
+    ap.add_argument("--candidate", type=int, default=-1,
+                    help="pin this stage kernel configuration instead of autotuning (profiler runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

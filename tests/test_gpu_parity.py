@@ -26,7 +26,10 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FLUX_GRIDS = {"euler1": (24, 1, 1), "euler2": (10, 9, 1), "euler3": (9, 8, 8), "burgers": (24, 1, 1)}
 TOL = {lib.FP64_EXACT: 0.0, lib.FP64: 1e-10, lib.FP64_DF: 1e-10, lib.FP32: 1e-4}
-FP32_TOL = {"burgers96_eno4_rk3": 2e-2}
+# FP32 through a shock with ENO stencils: FP32 rounding flips the stencil
+# choice where two undivided differences nearly tie, which moves cells near
+# the discontinuity by far more than the rounding itself
+FP32_TOL = {"burgers96_eno4_rk3": 2e-2, "sod128_hll_eno3_rk2": 5e-4}
 
 
 def scaled_l1(a, b):
