@@ -321,7 +321,7 @@ def run_gpu(args):
                               "issue_frac": profile_summary().get("fp64_issue_frac"),
                               "source": "ncu sm__pipe_fp64_cycles_active and DADD+DFMA+DMUL thread "
                                         "instructions per cycle over the 2 per SM per cycle peak "
-                                        "(profiles/stage_kernel_kh1024_fp64.md)"}}
+                                        "(profiles/stage_kernel_tma_kh1024_fp64.md)"}}
     clk = clocks.summary()
     line = None
     if rank == 0:
