@@ -57,6 +57,7 @@ def _units():
     units.append(("gbfv_api.cu", "gbfv_api.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_stats.cu", "gbfv_stats.o", []))
     units.append(("gbfv_structure.cu", "gbfv_structure.o", []))
+    units.append(("gbfv_functional.cu", "gbfv_functional.o", ["-fmad=false"]))
     units.append(("gbfv_noalloc.cu", "gbfv_noalloc.o", []))
     units.append(("gbfv_batch.cu", "gbfv_batch.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_init.cpp", "gbfv_init.o", ["-Xcompiler", "-ffp-contract=off"]))

@@ -38,6 +38,8 @@ SUPPORTED_FVM_NODES = {
     "functionals",
 }
 PLATFORMS = ("cpu", "cuda", "gb300")
+# alsuq statistics (REGISTER_STATISTICS in alsuq/src/stats/)
+STATISTICS = ("meanvar", "structure_cube", "functional", "onepointmoment", "bv", "bv_direction")
 EQUATIONS = ("burgers", "euler1", "euler2", "euler3")
 PRIMITIVE_VARIABLES = {
     "burgers": ("u",),
@@ -91,6 +93,7 @@ class FvmConfig:
     init_parameters: Dict[str, List[float]]
     writer: Optional[WriterConfig]
     diffusion: str = "none"
+    functionals: List["FunctionalConfig"] = field(default_factory=list)
 
     @property
     def dim(self):
@@ -115,21 +118,81 @@ class UQParameter:
 
 
 @dataclass
+class FunctionalConfig:
+    """A functional and its parameters, read from a <functional> node of
+    <fvm><functionals> or from a functional statistic's node, with the
+    reference's parameter names (alsfvm/src/functional/*.cpp constructors)."""
+    name: str
+    degree: int = 0
+    min_value: float = 0.0
+    max_value: float = 1.0
+    variables: str = ""
+    gamma: float = 1.4
+    p: float = 1.0
+    number_of_h: int = 1
+    number_of_saves: int = 0
+    writer: Optional["WriterConfig"] = None
+
+    def params(self):
+        return dict(degree=self.degree, min_value=self.min_value, max_value=self.max_value,
+                    variables=self.variables, gamma=self.gamma, p=self.p, number_of_h=self.number_of_h)
+
+
+FUNCTIONALS = ("identity", "moment", "legendre_pointwise", "log_entropy", "bv", "structure_cube")
+
+
+def _functional(node, name, gamma=None):
+    """FunctionalConfig of `name` from `node`; each functional reads the
+    parameters its constructor reads (missing ones raise, as
+    Parameters::get* throws)."""
+    if name not in FUNCTIONALS:
+        raise ConfigError("Unknown functional: %s (supported: %s)" % (name, ", ".join(FUNCTIONALS)))
+    f = FunctionalConfig(name=name)
+    if name in ("moment", "legendre_pointwise", "bv"):
+        f.degree = int(_text(node, "degree"))
+    if name == "legendre_pointwise":
+        f.min_value = float(_text(node, "minValue"))
+        f.max_value = float(_text(node, "maxValue"))
+        f.variables = _text(node, "variables", default="", required=False) or ""
+    if name == "log_entropy":
+        g = _text(node, "gamma", required=False)
+        if g is None and gamma is None:
+            raise ConfigError("log_entropy needs gamma")
+        f.gamma = float(g) if g is not None else float(gamma)
+    if name == "structure_cube":
+        f.p = float(_text(node, "p"))
+        f.number_of_h = int(_text(node, "numberOfH"))
+    return f
+
+
+@dataclass
 class StatConfig:
     name: str
     number_of_saves: int
     write_initial_timestep: bool
     writer: WriterConfig
-    p: float = 2.0          # structure_cube: the exponent
+    p: float = 2.0          # structure_cube: the exponent; onepointmoment, bv, bv_direction: the power
     number_of_h: int = 1    # structure_cube: distances 0 .. numberOfH - 1
+    functional: Optional["FunctionalConfig"] = None  # the functional statistic's functional
 
     def output_names(self):
         """The statistic's output names (getStatisticsNames): MeanVariance
         gives mean and variance, StructureCube "structure_cube_" plus p as
-        std::to_string prints it."""
+        std::to_string prints a double, OnePointMoment "m<p>", BoundedVariation
+        "bv_<p>", BoundedVariationDirection "bv_x_<p>", "bv_y_<p>", "bv_z_<p>",
+        FunctionalStatistics "mean_<functionalName>"
+        (alsuq/src/stats/*.cpp constructors)."""
         if self.name == "meanvar":
             return ["mean", "variance"]
-        return ["structure_cube_%.6f" % self.p]
+        if self.name == "structure_cube":
+            return ["structure_cube_%.6f" % self.p]
+        if self.name == "onepointmoment":
+            return ["m%d" % int(self.p)]
+        if self.name == "bv":
+            return ["bv_%d" % int(self.p)]
+        if self.name == "bv_direction":
+            return ["bv_%s_%d" % (d, int(self.p)) for d in "xyz"]
+        return ["mean_" + self.functional.name]
 
     def save_interval(self, end_time):
         return end_time / self.number_of_saves if self.number_of_saves > 0 else 0.0
@@ -257,9 +320,26 @@ def read_fvm(root, base_path):
     diffusion = _text(fvm, "diffusion/name", default="none", required=False)
     if diffusion != "none":
         raise ConfigError("Diffusion operator '%s' is not supported by the GB300 path (only 'none')" % diffusion)
-    functionals = fvm.find("functionals")
-    if functionals is not None and len(list(functionals)) > 0:
-        raise ConfigError("Functionals are not supported by the GB300 path")
+    # <functionals><functional>: name, the functional's parameters (plus the
+    # equation parameters), a writer with numberOfSaves, and numberOfSaves
+    # for the FixedIntervalWriter around the IntervalFunctionalWriter
+    # (SimulatorSetup::createFunctionals, SimulatorSetup.cpp:554-650)
+    functionals = []
+    fnode = fvm.find("functionals")
+    for fn in (fnode if fnode is not None else []):
+        if fn.find("time") is not None:
+            raise ConfigError("Time-integrated functionals (time, timeRadius) are not supported by the GB300 path")
+        saves = _text(fn, "numberOfSaves", required=False)
+        if saves is None:
+            raise ConfigError("Unknown arguments for functional")
+        f = _functional(fn, _text(fn, "name"), gamma=gamma)
+        f.number_of_saves = int(saves)
+        f.writer = _writer(fn.find("writer"))
+        if f.writer is None:
+            raise ConfigError("Missing configuration node: writer.type")
+        if f.writer.type not in ("netcdf", "numpy"):
+            raise ConfigError("Unknown writer type %s (supported: netcdf, numpy)" % f.writer.type)
+        functionals.append(f)
     writer = _writer(fvm.find("writer"))
     if writer is not None and writer.type not in ("netcdf", "numpy"):
         raise ConfigError("Unknown writer type %s (supported: netcdf, numpy)" % writer.type)
@@ -267,7 +347,8 @@ def read_fvm(root, base_path):
                      boundary=boundary, flux=_text(fvm, "flux"), end_time=float(_text(fvm, "endTime")),
                      equation=equation, gamma=gamma, reconstruction=reconstruction, cfl=cfl,
                      integrator=integrator, python_file=python_file, python_program=program,
-                     init_parameters=_init_parameters(fvm, eq_params), writer=writer, diffusion=diffusion)
+                     init_parameters=_init_parameters(fvm, eq_params), writer=writer, diffusion=diffusion,
+                     functionals=functionals)
 
 
 def read_uq(root):
@@ -297,8 +378,8 @@ def read_uq(root):
     snode = uq.find("stats")
     for s in (snode if snode is not None else []):
         name = _text(s, "name")
-        if name not in ("meanvar", "structure_cube"):
-            raise ConfigError("Unknown statistics %s (supported: meanvar, structure_cube)" % name)
+        if name not in STATISTICS:
+            raise ConfigError("Unknown statistics %s (supported: %s)" % (name, ", ".join(STATISTICS)))
         saves = _text(s, "numberOfSaves", required=False)
         if saves is None:
             raise ConfigError("Statistics %s needs numberOfSaves (time-integrated statistics are not supported)"
@@ -307,6 +388,10 @@ def read_uq(root):
         extra = {}
         if name == "structure_cube":
             extra = dict(p=float(_text(s, "p")), number_of_h=int(_text(s, "numberOfH")))
+        elif name in ("onepointmoment", "bv", "bv_direction"):
+            extra = dict(p=float(int(_text(s, "p"))))
+        elif name == "functional":
+            extra = dict(functional=_functional(s, _text(s, "functionalName")))
         stats.append(StatConfig(name=name, number_of_saves=int(saves),
                                 write_initial_timestep=_bool(wit) if wit is not None else False,
                                 writer=_writer(s.find("writer"), default_saves=saves), **extra))

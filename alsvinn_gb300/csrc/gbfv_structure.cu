@@ -224,6 +224,15 @@ int gbfv_structure_add_device(gbfv_structure* s, const void* state_dev, int prec
     return GBFV_OK;
 }
 
+int gbfv_structure_reset(gbfv_structure* s) {
+    if (!s) return sfail(GBFV_ERR_ARGUMENT, "null structure function");
+    cudaError_t e = cudaMemsetAsync(s->d_sums, 0, (size_t)s->nvar * s->H * sizeof(double), s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return sfail(GBFV_ERR_CUDA, cudaGetErrorString(e));
+    s->samples = 0;
+    return GBFV_OK;
+}
+
 int gbfv_structure_export(gbfv_structure* s, double* sums_host, long long* samples) {
     if (!s) return sfail(GBFV_ERR_ARGUMENT, "null structure function");
     if (samples) *samples = s->samples;
@@ -245,3 +254,7 @@ int gbfv_structure_result(gbfv_structure* s, double* mean_host, long long* sampl
 }
 
 }  // extern "C"
+
+// The device sums (nvar x number_of_h) of the structure function, for the
+// structure_cube functional.
+double* gbfv_internal_structure_sums(gbfv_structure* s) { return s ? s->d_sums : nullptr; }

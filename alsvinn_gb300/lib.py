@@ -19,6 +19,9 @@ _c_int3 = ctypes.c_int * 3
 _c_double3 = ctypes.c_double * 3
 
 
+ERR_ARGUMENT = -1  # GBFV_ERR_ARGUMENT
+
+
 class GbfvError(RuntimeError):
     def __init__(self, code, message):
         super().__init__("gbfv error %d: %s" % (code, message))
@@ -92,6 +95,17 @@ _SIGNATURES = {
     "gbfv_structure_add_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "gbfv_structure_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_structure_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_structure_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_functional_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                              ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "gbfv_functional_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_functional_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int)]),
+    "gbfv_functional_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_functional_apply": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+    "gbfv_functional_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "gbfv_uniform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_void_p]),
     "gbfv_advance_noalloc": (ctypes.c_int, [ctypes.POINTER(_Desc), ctypes.c_void_p,
@@ -471,6 +485,73 @@ class Stats:
         n = ctypes.c_longlong()
         _check(load().gbfv_stats_export(self.h, _ptr(m), _ptr(q), ctypes.byref(n)))
         return n.value, m, q
+
+
+class _FunctionalParams(ctypes.Structure):
+    _fields_ = [("degree", ctypes.c_int), ("min_value", ctypes.c_double), ("max_value", ctypes.c_double),
+                ("variable_mask", ctypes.c_uint), ("gamma", ctypes.c_double), ("p", ctypes.c_double),
+                ("number_of_h", ctypes.c_int), ("direction", ctypes.c_int)]
+
+
+VARIABLE_NAMES = {"burgers": ["u"], "euler1": ["rho", "mx", "E"], "euler2": ["rho", "mx", "my", "E"],
+                  "euler3": ["rho", "mx", "my", "mz", "E"]}
+
+
+def variable_mask(equation, variables):
+    """Bit mask of the named variables ("rho E" or a list); 0 (all) when empty.
+    Unknown names raise, as the reference's LegendrePointWise does."""
+    names = VARIABLE_NAMES[equation]
+    mask = 0
+    for v in (variables.split() if isinstance(variables, str) else list(variables or [])):
+        if v not in names:
+            raise GbfvError(ERR_ARGUMENT, "Unknown variable name given to the functional: %s" % v)
+        mask |= 1 << names.index(v)
+    return mask
+
+
+class Functional:
+    """A functional of one state (gbfv_functional_*): identity, moment,
+    legendre_pointwise, log_entropy, bv, bv_direction, structure_cube.
+    apply() adds weight times the functional of a device state into the
+    accumulator; result() returns (nvar, output cells)."""
+
+    def __init__(self, name, equation, boundary, n, ghosts, lower, upper, degree=0, min_value=0.0, max_value=1.0,
+                 variables="", gamma=1.4, p=1.0, number_of_h=1, direction=0):
+        prm = _FunctionalParams(int(degree), float(min_value), float(max_value), variable_mask(equation, variables),
+                                float(gamma), float(p), int(number_of_h), int(direction))
+        h = ctypes.c_void_p()
+        _check(load().gbfv_functional_create(name.encode(), equation.encode(), boundary.encode(), _c_int3(*n),
+                                             int(ghosts), _c_double3(*lower), _c_double3(*upper),
+                                             ctypes.byref(prm), ctypes.byref(h)))
+        self.h = h
+        self.name = name
+        size = _c_int3()
+        nv = ctypes.c_int()
+        _check(load().gbfv_functional_size(h, size, ctypes.byref(nv)))
+        self.size = tuple(size)
+        self.nvar = nv.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gbfv_functional_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self):
+        _check(load().gbfv_functional_reset(self.h))
+
+    def apply(self, ptr, precision=FP64, weight=1.0):
+        _check(load().gbfv_functional_apply(self.h, ctypes.c_void_p(ptr), precision, float(weight)))
+
+    def result(self):
+        out = np.zeros((self.nvar, int(np.prod(self.size))))
+        _check(load().gbfv_functional_result(self.h, _ptr(out)))
+        return out
 
 
 class Structure:

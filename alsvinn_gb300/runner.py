@@ -36,6 +36,58 @@ from .simulator import Simulator
 from .writers import NetCDFWriter, NumpyWriter
 
 
+class _FunctionalAccumulator:
+    """Sum-type statistics built on device functionals (weight 1 per sample):
+    functional (FunctionalStatistics), onepointmoment (OnePointMoment:
+    addPower, the "moment" functional), bv (BoundedVariation), bv_direction
+    (BoundedVariationDirection, one functional per direction). `assign`
+    keeps only the latest sample, as BoundedVariationDirection assigns its
+    snapshot instead of adding to it (alsuq/src/stats/
+    BoundedVariationDirection.cpp:40-60); StatisticsHelper::
+    combineStatistics then sums over ranks and divides by the sample count
+    for all of them (StatisticsHelper.cpp:35-79)."""
+
+    def __init__(self, functionals, assign=False):
+        self.functionals = functionals
+        self.assign = assign
+        self.count = 0
+
+    def add_device(self, ptr, precision):
+        for f in self.functionals:
+            if self.assign:
+                f.reset()
+            f.apply(ptr, precision, 1.0)
+        self.count += 1
+
+    def export(self):
+        return self.count, np.stack([f.result() for f in self.functionals])
+
+    def close(self):
+        for f in self.functionals:
+            f.close()
+
+
+def make_statistic_accumulator(st, fvm, ghosts, nvar):
+    """The device accumulator of one save of statistic `st` on grid `fvm`."""
+    n, lo, hi = fvm.dimension, fvm.lower, fvm.upper
+    if st.name == "meanvar":
+        return lib.Stats(nvar * int(np.prod([n[d] + 2 * ghosts if d < fvm.dim else n[d] for d in range(3)])))
+    if st.name == "structure_cube":
+        return lib.Structure(fvm.boundary, n, ghosts, nvar, st.number_of_h, st.p)
+    if st.name == "onepointmoment":
+        fs = [lib.Functional("moment", fvm.equation, fvm.boundary, n, ghosts, lo, hi, degree=int(st.p))]
+    elif st.name == "bv":
+        fs = [lib.Functional("bv", fvm.equation, fvm.boundary, n, ghosts, lo, hi, degree=int(st.p))]
+    elif st.name == "bv_direction":
+        fs = [lib.Functional("bv_direction", fvm.equation, fvm.boundary, n, ghosts, lo, hi, degree=int(st.p),
+                             direction=d) for d in range(fvm.dim)]
+        return _FunctionalAccumulator(fs, assign=True)
+    else:
+        f = st.functional
+        fs = [lib.Functional(f.name, fvm.equation, fvm.boundary, n, ghosts, lo, hi, **f.params())]
+    return _FunctionalAccumulator(fs)
+
+
 def sample_parameters(uqc, samples, generator=None):
     """{sample: {name: [values]}} for the given ascending samples, drawn in
     the Runner's order on one generator."""
@@ -78,8 +130,8 @@ class Runner:
         self.stats_interval = intervals.pop() if intervals else 0.0
         self.stats_saves = stats[0].number_of_saves if stats else 0
         self.stats_initial = bool(stats and stats[0].write_initial_timestep)
-        batch_ok = (self.fvm.writer is None and self.stats_saves <= 1 and not self.stats_initial
-                    and all(st.name == "meanvar" for st in stats)
+        batch_ok = (self.fvm.writer is None and not self.fvm.functionals and self.stats_saves <= 1
+                    and not self.stats_initial and all(st.name == "meanvar" for st in stats)
                     and self.fvm.integrator in ("rungekutta2", "rungekutta3"))
         if engine == "auto":
             engine = "batch" if batch_ok else "serial"
@@ -101,8 +153,10 @@ class Runner:
         ranks (identical on every rank); rank 0 writes them. self.statistics
         holds, per configured statistic, one entry per save: (count, mean,
         variance) for meanvar (padded states (nvar, total) flattened), (count,
-        structure function (nvar, numberOfH)) for structure_cube. Returns the
-        first meanvar statistic's entries."""
+        structure function (nvar, numberOfH)) for structure_cube, (count,
+        mean (outputs, nvar, output cells)) for the functional-based ones
+        (functional, onepointmoment, bv: one output; bv_direction: one per
+        grid direction). Returns the first meanvar statistic's entries."""
         t0 = time.perf_counter()
         params = sample_parameters(self.uqc, self.samples)
         if self.engine == "batch":
@@ -129,15 +183,10 @@ class Runner:
         sim = Simulator(self.fvm, self.precision, num_samples=self.uqc.samples, output_dir=self.output_dir,
                         statistics_interval=self.stats_interval, statistics_initial=self.stats_initial)
         nsave = self.stats_saves + (1 if self.stats_initial else 0)
-        count = sim.solver.nvar * sim.solver.total
         g = lib.ghost_cells(self.fvm.reconstruction)
         acc = []  # per statistic, per save
         for st in self.uqc.stats:
-            if st.name == "meanvar":
-                acc.append([lib.Stats(count) for _ in range(nsave)])
-            else:
-                acc.append([lib.Structure(self.fvm.boundary, self.fvm.dimension, g, sim.solver.nvar,
-                                          st.number_of_h, st.p) for _ in range(nsave)])
+            acc.append([make_statistic_accumulator(st, self.fvm, g, sim.solver.nvar) for _ in range(nsave)])
         prec = self.precision if self.precision == lib.FP32 else lib.FP64
 
         def on_statistics(s, k):
@@ -200,6 +249,19 @@ class Runner:
 
     # -- output ------------------------------------------------------------
 
+    def _functional_size(self, st):
+        """Output extents of a functional-based statistic."""
+        if st.name in ("bv", "bv_direction"):
+            return (1, 1, 1)
+        if st.name == "onepointmoment":
+            return tuple(self.fvm.dimension)
+        fc = st.functional
+        if fc.name in ("log_entropy", "bv"):
+            return (1, 1, 1)
+        if fc.name == "structure_cube":
+            return (fc.number_of_h, 1, 1)
+        return tuple(self.fvm.dimension)
+
     def _write_statistics(self):
         f = self.fvm
         nv = lib.num_variables(f.equation)
@@ -211,11 +273,23 @@ class Runner:
                 outputs = [(name, [interior(np.asarray(r[idx]).reshape(nv, -1), f.dimension, g) for r in results],
                             (f.lower, f.upper, f.dimension))
                            for name, idx in (("mean", 1), ("variance", 2))]
-            else:
+            elif st.name == "structure_cube":
                 # one value per distance h: x runs over h = 0 .. numberOfH - 1
                 H = st.number_of_h
                 outputs = [(st.output_names()[0], [np.asarray(r[1]).reshape(nv, 1, 1, H) for r in results],
                             ((-0.5, 0.0, 0.0), (H - 0.5, 1.0, 1.0), (H, 1, 1)))]
+            else:
+                outputs = []
+                for k, name in enumerate(st.output_names()):
+                    size = self._functional_size(st)
+                    if st.name == "bv_direction" and k >= f.dim:
+                        # a direction the grid does not have: its snapshot is never assigned
+                        arrays = [np.zeros((nv, 1, 1, 1)) for _ in results]
+                    else:
+                        arrays = [np.asarray(r[1])[k].reshape(nv, size[2], size[1], size[0]) for r in results]
+                    grid = ((f.lower, f.upper, f.dimension) if tuple(size) == tuple(f.dimension)
+                            else (f.lower, f.upper, tuple(size)))
+                    outputs.append((name, arrays, grid))
             for name, arrays, (lo, hi, dims) in outputs:
                 base = "%s/%s_%s" % (self.output_dir, w.basename, name)
                 if w.type == "netcdf":

@@ -10,7 +10,8 @@ statistics' FixedIntervalStatistics clamp dt on the device exactly as the
 reference's timestep adjusters do, so the trajectory is the reference's.
 """
 from . import lib
-from .writers import make_writer
+from .config import ConfigError
+from .writers import NetCDFWriter, NumpyWriter, make_writer
 
 PRECISIONS = {"fp64": lib.FP64, "fp64-exact": lib.FP64_EXACT, "fp32": lib.FP32, "fp64-df": lib.FP64_DF}
 
@@ -52,9 +53,61 @@ class Simulator:
         self.on_statistics = on_statistics
         self.snapshot = 0
         self.statistics_snapshot = 0
+        self._setup_functionals(num_samples, output_dir)
+
+    def _setup_functionals(self, num_samples, output_dir):
+        """<functionals>: each an IntervalFunctionalWriter inside a
+        FixedIntervalWriter of interval endTime / numberOfSaves that writes the
+        initial state too (its writeInitialTimestep defaults to true,
+        SimulatorSetup.cpp:626-640, FixedIntervalWriter.hpp:41-43). The
+        FixedIntervalWriter is also a timestep adjuster; its save times share
+        the device's two save clamps with the writer's and the statistics'
+        (equal intervals share a clamp; more than two distinct intervals are
+        refused). The output file's time axis holds the initial write plus
+        numberOfSaves entries."""
+        import os
+        f = self.fvm
+        self.functionals = []  # [functional, writer, clamp slot, snapshot]
+        intervals = [self.write_interval if self.writer is not None else 0.0, self.statistics_interval]
+        for fc in f.functionals:
+            interval = f.end_time / fc.number_of_saves
+            if interval in intervals:
+                slot = intervals.index(interval)
+            elif 0.0 in intervals:
+                slot = intervals.index(0.0)
+                intervals[slot] = interval
+            else:
+                raise ConfigError("more than two distinct save intervals (writer, statistics, functionals) are not "
+                                  "supported")
+            fn = lib.Functional(fc.name, f.equation, f.boundary, f.dimension, self.ghosts, f.lower, f.upper,
+                                **fc.params())
+            size = fn.size
+            path = os.path.join(output_dir, fc.writer.basename)
+            if fc.writer.type == "netcdf":
+                times = [0.0] + [(k + 1) / fc.number_of_saves for k in range(fc.number_of_saves)]
+                w = NetCDFWriter(path, f.equation, f.lower, f.upper, size, num_samples, times)
+            else:
+                w = NumpyWriter(path, f.equation)
+            self.functionals.append([fn, w, slot, 0])
+        self.clamp_intervals = intervals
 
     def close(self):
+        for fn in self.functionals:
+            fn[0].close()
         self.solver.close()
+
+    def _write_functionals(self, mask=None):
+        prec = self.precision if self.precision == lib.FP32 else lib.FP64
+        for entry in self.functionals:
+            fn, w, slot, snap = entry
+            if mask is not None and not (mask >> slot) & 1:
+                continue
+            fn.reset()
+            fn.apply(self.solver.state_device(), prec, 1.0)
+            size = fn.size
+            w.write(fn.result().reshape(fn.nvar, size[2], size[1], size[0]), self.sample, snap,
+                    time=self.get_current_time())
+            entry[3] = snap + 1
 
     def set_initial_value(self, prim):
         """Interior primitive variables (nvar, nz, ny, nx); resets the time,
@@ -62,6 +115,8 @@ class Simulator:
         self.solver.set_primitive(prim)
         self.snapshot = 0
         self.statistics_snapshot = 0
+        for entry in getattr(self, "functionals", []):
+            entry[3] = 0
 
     def conserved_interior(self):
         return interior(self.solver.get_state(), self.fvm.dimension, self.ghosts)
@@ -81,15 +136,19 @@ class Simulator:
         at 1 otherwise."""
         if self.writer is not None and self.fvm.writer.write_initial_timestep:
             self._write()
+        if self.functionals:
+            self._write_functionals()
         if self.statistics_interval > 0 and self.statistics_initial:
             self._statistics()
 
     def _advance(self, max_steps):
-        mask = self.solver.advance_schedule(self.fvm.end_time, (self.write_interval, self.statistics_interval),
-                                            max_steps=max_steps, stop_at_save=True)
+        mask = self.solver.advance_schedule(self.fvm.end_time, tuple(self.clamp_intervals), max_steps=max_steps,
+                                            stop_at_save=True)
         if mask & 1 and self.writer is not None:
             self._write()
-        if mask & 2:
+        if self.functionals and mask:
+            self._write_functionals(mask)
+        if mask & 2 and self.statistics_interval > 0:
             self._statistics()
         return mask
 
@@ -106,6 +165,8 @@ class Simulator:
     def finalize(self):
         if self.writer is not None:
             self.writer.finalize()
+        for fn in self.functionals:
+            fn[1].finalize()
 
     def at_end(self):
         return self.get_current_time() >= self.fvm.end_time

@@ -246,6 +246,60 @@ int gbfv_structure_destroy(gbfv_structure* s);
 int gbfv_structure_add_device(gbfv_structure* s, const void* state_dev, int precision);
 int gbfv_structure_result(gbfv_structure* s, double* mean_host, long long* samples);
 int gbfv_structure_export(gbfv_structure* s, double* sums_host, long long* samples);
+/* Zeroes the sums and the sample count. */
+int gbfv_structure_reset(gbfv_structure* s);
+
+/* ------------------------------------------------------- functionals */
+
+/* Functionals of one state (alsfvm::functional::Functional::operator(),
+ * alsfvm/include/alsfvm/functional/Functional.hpp:26-60, the set the
+ * reference's FunctionalFactory registers for its cuda platform): a map from a
+ * padded state to a small volume of nvar variables that gbfv_functional_apply
+ * adds, times a weight, into an FP64 accumulator on the device. Names and
+ * parameters as in the reference's XML:
+ *   identity                      the interior state              (Identity.cpp)
+ *   moment (degree)               pow(u, degree), interior         (Moment.cpp)
+ *   legendre_pointwise (degree, min_value, max_value, variable_mask)
+ *                                 P_degree((u - min) / (max - min)) of the
+ *                                 selected variables (bit k: variable k; 0:
+ *                                 all); 2D grids only, and the scaled value
+ *                                 must lie in [-1, 1]             (LegendrePointWise.cpp)
+ *   log_entropy (gamma)           one value, in the energy variable: the
+ *                                 integral of -rho s / (gamma - 1),
+ *                                 s = log p - gamma log rho; Euler   (LogEntropy.cpp)
+ *   bv (degree)                   one value per variable: the total
+ *                                 variation sum (sqrt(du_y^2 + du_x^2))^degree;
+ *                                 1D / 2D                          (BoundedVariation.cpp)
+ *   bv_direction (degree, direction)
+ *                                 one value per variable: the sum of
+ *                                 |u - u(-e_direction)|^degree     (HostMemory::getTotalVariation)
+ *   structure_cube (p, number_of_h)
+ *                                 number_of_h values per variable: this
+ *                                 state's cube structure function, which
+ *                                 replaces the output (weight unused; the
+ *                                 reference zeroes its output first) (StructureCube.cpp)
+ * n, ghosts, lower, upper: the state's grid (cell lengths enter log_entropy
+ * and the 2D checks). gbfv_functional_size gives the output extents;
+ * gbfv_functional_result copies nvar x (extent product) values, x fastest. */
+typedef struct gbfv_functional gbfv_functional;
+typedef struct {
+    int degree;
+    double min_value, max_value;
+    unsigned variable_mask;
+    double gamma;
+    double p;
+    int number_of_h;
+    int direction;
+} gbfv_functional_params;
+
+int gbfv_functional_create(const char* name, const char* equation, const char* boundary, const int n[3], int ghosts,
+                           const double lower[3], const double upper[3], const gbfv_functional_params* params,
+                           gbfv_functional** out);
+int gbfv_functional_destroy(gbfv_functional* f);
+int gbfv_functional_size(const gbfv_functional* f, int size[3], int* nvar);
+int gbfv_functional_reset(gbfv_functional* f);
+int gbfv_functional_apply(gbfv_functional* f, const void* state_dev, int precision, double weight);
+int gbfv_functional_result(gbfv_functional* f, double* out_host);
 
 /* --------------------------------------------------------- ensembles */
 

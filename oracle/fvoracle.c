@@ -1079,6 +1079,173 @@ int fv_structure_cube(const char* equation, const char* boundary, const int n[3]
     return 0;
 }
 
+/* ---------------------------------------------------------- functionals */
+
+enum { FN_IDENTITY, FN_MOMENT, FN_LEGENDRE, FN_LOG_ENTROPY, FN_BV, FN_BV_DIRECTION, FN_STRUCTURE_CUBE };
+
+static int parse_functional(const char* s) {
+    if (!strcmp(s, "identity")) return FN_IDENTITY;
+    if (!strcmp(s, "moment")) return FN_MOMENT;
+    if (!strcmp(s, "legendre_pointwise")) return FN_LEGENDRE;
+    if (!strcmp(s, "log_entropy")) return FN_LOG_ENTROPY;
+    if (!strcmp(s, "bv")) return FN_BV;
+    if (!strcmp(s, "bv_direction")) return FN_BV_DIRECTION;
+    if (!strcmp(s, "structure_cube")) return FN_STRUCTURE_CUBE;
+    return -1;
+}
+
+/* Legendre polynomial P_l(x) by Bonnet's three-term recurrence in the order
+ * of Boost.Math's legendre_p / legendre_next (the reference's CPU
+ * LegendrePointWise calls boost::math::legendre_p,
+ * alsfvm/src/functional/LegendrePointWise.cpp:57-82):
+ *   P_0 = 1, P_1 = x, P_{n+1} = ((2n+1) x P_n - n P_{n-1}) / (n+1),
+ * with P_{-l-1} = P_l. The caller checks -1 <= x <= 1. */
+static double legendre_p(int l, double x) {
+    if (l < 0) l = -l - 1;
+    double p0 = 1.0, p1 = x;
+    if (l == 0) return p0;
+    for (unsigned n = 1; n < (unsigned)l; ++n) {
+        const double t = p0;
+        p0 = p1;
+        p1 = t;
+        p1 = ((double)(2 * n + 1) * x * p0 - (double)n * p1) / (double)(n + 1);
+    }
+    return p1;
+}
+
+/* HostMemory::getTotalVariation(p, start, end) over one padded variable
+ * (alsfvm/src/memory/HostMemory.cpp:325-362): 1D and 2D only; the sum over
+ * z in [0, end.z), y from start.y + 1 (1D: 0), x from start.x + 1, of
+ * (sqrt((u - u_below)^2 + (u - u_left)^2))^p, u_below = u itself in 1D. */
+static double total_variation(const grid_t* G, const double* u, int p) {
+    const long nx = G->t[0], ny = G->t[1];
+    const long sx = G->g[0] + 1, sy = G->g[1] + (ny > 1 ? 1 : 0);
+    const long ex = G->t[0] - G->g[0], ey = G->t[1] - G->g[1], ez = G->t[2] - G->g[2];
+    double bv = 0;
+    for (long z = 0; z < ez; z++)
+        for (long y = sy; y < ey; y++)
+            for (long x = sx; x < ex; x++) {
+                const long i = z * nx * ny + y * nx + x;
+                const long il = z * nx * ny + y * nx + (x - 1);
+                const long yb = ny > 1 ? y - 1 : 0;
+                const long ib = z * nx * ny + yb * nx + x;
+                bv += pow(sqrt(pow(u[i] - u[ib], 2) + pow(u[i] - u[il], 2)), p);
+            }
+    return bv;
+}
+
+/* HostMemory::getTotalVariation(direction, p, start, end)
+ * (alsfvm/src/memory/HostMemory.cpp:365-400): sum over the cells from
+ * start + e_d to end of |u - u(- e_d)|^p. */
+static double total_variation_direction(const grid_t* G, const double* u, int d, int p) {
+    const long s[3] = {G->g[0] + (d == 0), G->g[1] + (d == 1), G->g[2] + (d == 2)};
+    const long e[3] = {G->t[0] - G->g[0], G->t[1] - G->g[1], G->t[2] - G->g[2]};
+    const long off = d == 0 ? 1 : (d == 1 ? G->t[0] : (long)G->t[0] * G->t[1]);
+    double bv = 0;
+    for (long z = s[2]; z < e[2]; z++)
+        for (long y = s[1]; y < e[1]; y++)
+            for (long x = s[0]; x < e[0]; x++) {
+                const long i = IDX(G, x, y, z);
+                bv += pow(fabs(u[i] - u[i - off]), p);
+            }
+    return bv;
+}
+
+int fv_functional(const char* name, const char* equation, const char* boundary, const int n[3], int ghosts,
+                  const double lower[3], const double upper[3], int degree, double min_value, double max_value,
+                  unsigned variable_mask, double gamma, double p, int number_of_h, int direction, double weight,
+                  const double* U, double* out, int size_out[3]) {
+    const int fn = parse_functional(name), eq = parse_eq(equation);
+    if (fn < 0) return fail(-1, "Unknown functional: %s", name);
+    if (eq < 0) return fail(-1, "unknown equation");
+    grid_t G;
+    make_grid(&G, eq, n, ghosts, gamma);
+    /* Grid::computeCellLengths (alsfvm/src/grid/Grid.cpp:24-42) */
+    double len[3];
+    for (int d = 0; d < 3; ++d) len[d] = (upper[d] - lower[d]) / n[d];
+    if (n[1] == 1) len[1] = 1;
+    if (n[2] == 1) len[2] = 1;
+    const long cells = (long)n[0] * n[1] * n[2];
+    int o[3] = {n[0], n[1], n[2]};
+    if (fn == FN_LOG_ENTROPY || fn == FN_BV || fn == FN_BV_DIRECTION) o[0] = o[1] = o[2] = 1;
+    if (fn == FN_STRUCTURE_CUBE) {
+        o[0] = number_of_h;
+        o[1] = o[2] = 1;
+    }
+    if (size_out) memcpy(size_out, o, sizeof o);
+    const long oc = (long)o[0] * o[1] * o[2];
+    switch (fn) {
+        case FN_IDENTITY:    /* alsfvm/src/functional/Identity.cpp:25-49 */
+        case FN_MOMENT:      /* Moment.cpp:27-41 -> HostMemory::addPower(other, power, factor) */
+        case FN_LEGENDRE: {  /* LegendrePointWise.cpp:37-87 */
+            if (fn == FN_LEGENDRE && (len[2] > 1 || len[1] == 1))
+                return fail(-1, "For now, Legendre polynomials only support 2d");
+            for (int v = 0; v < G.nvar; ++v) {
+                if (fn == FN_LEGENDRE && variable_mask && !((variable_mask >> v) & 1u)) continue;
+                const double* u = U + (long)v * G.total;
+                double* w = out + (long)v * oc;
+                for (int k = 0; k < n[2]; ++k)
+                    for (int j = 0; j < n[1]; ++j)
+                        for (int i = 0; i < n[0]; ++i) {
+                            const double x = u[IDX(&G, i + G.g[0], j + G.g[1], k + G.g[2])];
+                            const long c = ((long)k * n[1] + j) * n[0] + i;
+                            if (fn == FN_IDENTITY) {
+                                w[c] += weight * x;
+                            } else if (fn == FN_MOMENT) {
+                                w[c] += weight * pow(x, (double)degree);
+                            } else {
+                                const double s = (x - min_value) / (max_value - min_value);
+                                if (!(s >= -1.0 && s <= 1.0))
+                                    return fail(-1, "The Legendre Polynomial is defined for -1 <= x <= 1, but got x = %.17g", s);
+                                w[c] += legendre_p(degree, s) * weight;
+                            }
+                        }
+            }
+            return 0;
+        }
+        case FN_LOG_ENTROPY: {  /* LogEntropy.cpp:21-83 */
+            if (eq == EQ_BURGERS) return fail(-1, "log_entropy needs the Euler variables");
+            const double dxdydz = len[0] * len[1] * len[2];
+            const double* rho = U;
+            const double* E = U + (long)(G.nvar - 1) * G.total;
+            double integral = 0.0;
+            for (int k = 0; k < n[2]; ++k)
+                for (int j = 0; j < n[1]; ++j)
+                    for (int i = 0; i < n[0]; ++i) {
+                        const long c = IDX(&G, i + G.g[0], j + G.g[1], k + G.g[2]);
+                        const double density = rho[c], energy = E[c];
+                        double momentumSquared = 0.0;
+                        for (int m = 0; m < G.nsd; ++m) {
+                            const double mm = U[(long)(1 + m) * G.total + c];
+                            momentumSquared += mm * mm;
+                        }
+                        const double pressure = (gamma - 1) * (energy - 1.0 / (2 * density) * momentumSquared);
+                        const double s = log(pressure) - gamma * log(density);
+                        const double e = (-density * s) / (gamma - 1);
+                        integral += e * dxdydz;
+                    }
+            out[(long)(G.nvar - 1) * oc] += weight * integral;
+            return 0;
+        }
+        case FN_BV: {  /* functional/BoundedVariation.cpp:21-40 */
+            if (len[2] > 1) return fail(-1, "For now, BoundedVariation  only support 2d and 1d");
+            if (G.t[2] > 1) return fail(-1, "Not supported for 3d yet");
+            for (int v = 0; v < G.nvar; ++v) out[(long)v * oc] += weight * total_variation(&G, U + (long)v * G.total, degree);
+            return 0;
+        }
+        case FN_BV_DIRECTION: {
+            if (direction < 0 || direction >= G.dim) return fail(-1, "direction = %d is bigger than current dimension", direction);
+            for (int v = 0; v < G.nvar; ++v)
+                out[(long)v * oc] += weight * total_variation_direction(&G, U + (long)v * G.total, direction, degree);
+            return 0;
+        }
+        default: {  /* functional/StructureCube.cpp:24-60: zeroes its output first */
+            (void)cells;
+            return fv_structure_cube(equation, boundary, n, ghosts, number_of_h, p, U, out);
+        }
+    }
+}
+
 /* ---------------------------------------------------------- statistics */
 
 /* MeanVariance::computeStatistics adds u and pow(u,2) per sample

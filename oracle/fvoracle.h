@@ -60,6 +60,17 @@ int fv_structure_cube(const char* equation, const char* boundary, const int n[3]
 int fv_meanvar(long count, int nsamples, const double* const* samples, double* mean,
                double* var);
 
+/* Functionals of one padded state: identity, moment, legendre_pointwise,
+ * log_entropy, bv, bv_direction, structure_cube. out (nvar x output cells,
+ * x fastest) receives weight times the functional added to what it holds
+ * (structure_cube overwrites and ignores the weight, as the reference does);
+ * size_out receives the output extents. variable_mask selects the variables
+ * of legendre_pointwise (bit k: variable k; 0: all). */
+int fv_functional(const char* name, const char* equation, const char* boundary, const int n[3], int ghosts,
+                  const double lower[3], const double upper[3], int degree, double min_value, double max_value,
+                  unsigned variable_mask, double gamma, double p, int number_of_h, int direction, double weight,
+                  const double* U, double* out, int size_out[3]);
+
 #ifdef __cplusplus
 }
 #endif

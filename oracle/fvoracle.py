@@ -135,6 +135,37 @@ def structure_cube(equation, boundary, n, ghosts, number_of_h, p, U):
     return out
 
 
+VARIABLE_NAMES = {"burgers": ["u"], "euler1": ["rho", "mx", "E"], "euler2": ["rho", "mx", "my", "E"],
+                  "euler3": ["rho", "mx", "my", "mz", "E"]}
+
+
+def variable_mask(equation, variables):
+    """Bit mask of the named variables ("rho E"); 0 (all) for an empty list."""
+    names = VARIABLE_NAMES[equation]
+    mask = 0
+    for v in (variables.split() if isinstance(variables, str) else list(variables or [])):
+        mask |= 1 << names.index(v)
+    return mask
+
+
+def functional(name, equation, boundary, n, ghosts, lower, upper, U, weight=1.0, degree=0, min_value=0.0,
+               max_value=1.0, variables="", gamma=1.4, p=1.0, number_of_h=1, direction=0):
+    """weight times functional `name` of one padded state (structure_cube:
+    the functional itself, which ignores the weight); returns (values
+    (nvar, output cells), output extents)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    nv = U.shape[0]
+    size = (ctypes.c_int * 3)()
+    cap = max(int(np.prod(n)), int(number_of_h), 1)
+    buf = np.zeros(nv * cap)
+    _check(load().fv_functional(name.encode(), equation.encode(), boundary.encode(), _i3(n), int(ghosts), _d3(lower),
+                                _d3(upper), int(degree), D(min_value), D(max_value),
+                                ctypes.c_uint(variable_mask(equation, variables)), D(gamma), D(p), int(number_of_h),
+                                int(direction), D(weight), _p(U), _p(buf), size))
+    cells = size[0] * size[1] * size[2]
+    return buf[:nv * cells].reshape(nv, cells), tuple(size)
+
+
 def meanvar(samples):
     samples = [np.ascontiguousarray(s, dtype=np.float64) for s in samples]
     count = samples[0].size

@@ -15,6 +15,7 @@
 #include "alsfvm/diffusion/NoDiffusion.hpp"
 #include "alsfvm/equation/CellComputerFactory.hpp"
 #include "alsfvm/equation/euler/EulerParameters.hpp"
+#include "alsfvm/functional/FunctionalFactory.hpp"
 #include "alsfvm/functional/structure_common.hpp"
 #include "alsfvm/grid/Grid.hpp"
 #include "alsfvm/init/InitialData.hpp"
@@ -477,6 +478,85 @@ int ref_structure_cube(const char* equation, const char* boundary, const int dim
         else
             functional::dispatchComputeStructureCubeCPU<boundary::NEUMANN>(*o, *in, number_of_h, p);
         copy_out(*o, out, nvar);
+        return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
+// One functional of the reference's CPU factory applied to one padded state
+// (alsfvm/src/functional/FunctionalFactory.cpp, the functional classes under
+// alsfvm/src/functional/): the output volume is created as
+// IntervalFunctionalWriter::makeVolumes does (functional size, the
+// functional's ghost cells), zeroed, the functional applied with `weight`;
+// out receives the interior of every variable, size_out its extents.
+int ref_functional(const char* name, const char* equation, const char* boundary, const int dims[3], int ghosts,
+    const double lower[3], const double upper[3], int degree, double min_value, double max_value,
+    const char* variables, double gamma, double p, int number_of_h, double weight, const double* U, double* out,
+    int size_out[3]) {
+    try {
+        Setup s(equation, "godunov", "none", boundary, "forwardeuler", dims, lower, upper, gamma, 0.5);
+        const int nvar = nvar_of(equation);
+        volume::VolumeFactory vf(equation, s.memory);
+        auto in = vf.createConservedVolume(dims[0], dims[1], dims[2], ghosts);
+        copy_in(*in, U, nvar);
+        char buf[5][64];
+        std::snprintf(buf[0], sizeof buf[0], "%d", degree);
+        std::snprintf(buf[1], sizeof buf[1], "%.17g", min_value);
+        std::snprintf(buf[2], sizeof buf[2], "%.17g", max_value);
+        std::snprintf(buf[3], sizeof buf[3], "%.17g", gamma);
+        std::snprintf(buf[4], sizeof buf[4], "%.17g", p);
+        std::map<std::string, std::string> values{{"degree", buf[0]}, {"minValue", buf[1]}, {"maxValue", buf[2]},
+                                                  {"gamma", buf[3]}, {"p", buf[4]},
+                                                  {"numberOfH", std::to_string(number_of_h)}};
+        if (variables && *variables) values["variables"] = variables;
+        alsutils::parameters::Parameters params(values);
+        functional::FunctionalFactory factory;
+        auto f = factory.makeFunctional("cpu", name, params);
+        const ivec3 fs = f->getFunctionalSize(*s.grid);
+        const ivec3 gh = f->getGhostCellSizes(*s.grid, *in);
+        auto o = vf.createConservedVolume(fs.x, fs.y, fs.z, gh.x);
+        o->makeZero();
+        (*f)(*o, *in, weight, *s.grid);
+        const size_t tx = o->getTotalNumberOfXCells(), ty = o->getTotalNumberOfYCells();
+        const size_t gx = o->getNumberOfXGhostCells(), gy = o->getNumberOfYGhostCells(),
+                     gz = o->getNumberOfZGhostCells();
+        const size_t cells = (size_t)fs.x * fs.y * fs.z;
+        for (int v = 0; v < nvar; ++v) {
+            const double* src = o->getScalarMemoryArea(v)->getPointer();
+            for (int z = 0; z < fs.z; ++z)
+                for (int y = 0; y < fs.y; ++y)
+                    for (int x = 0; x < fs.x; ++x)
+                        out[v * cells + ((size_t)z * fs.y + y) * fs.x + x] =
+                            src[(z + gz) * tx * ty + (y + gy) * tx + (x + gx)];
+        }
+        size_out[0] = fs.x;
+        size_out[1] = fs.y;
+        size_out[2] = fs.z;
+        return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
+// HostMemory::getTotalVariation(direction, p, start, end) of each variable of
+// one padded state between the ghost layers (the per-sample quantity of
+// alsuq's bv_direction statistic, alsuq/src/stats/BoundedVariationDirection.cpp).
+int ref_total_variation_direction(const char* equation, const int dims[3], int ghosts, int direction, int p,
+    const double* U, double* out) {
+    try {
+        double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+        Setup s(equation, "godunov", "none", "periodic", "forwardeuler", dims, lo, hi, 1.4, 0.5);
+        const int nvar = nvar_of(equation);
+        volume::VolumeFactory vf(equation, s.memory);
+        auto in = vf.createConservedVolume(dims[0], dims[1], dims[2], ghosts);
+        copy_in(*in, U, nvar);
+        const ivec3 start = in->getNumberOfGhostCells();
+        const ivec3 end = in->getSize() - in->getNumberOfGhostCells();
+        for (int v = 0; v < nvar; ++v)
+            out[v] = in->getScalarMemoryArea(v)->getTotalVariation(direction, p, start, end);
         return 0;
     } catch (std::exception& e) {
         g_error = e.what();

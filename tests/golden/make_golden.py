@@ -114,6 +114,35 @@ STRUCTURE_CASES = {
 }
 
 
+def functional_cases():
+    rng = np.random.default_rng(20241203)
+    out = {}
+    for name, (fn, eq, bc, n, g, lo, hi, prm, w) in workloads.FUNCTIONAL_CASES.items():
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        nv = workloads.NVAR[eq]
+        size = (ctypes.c_int * 3)()
+        o = np.zeros(nv * int(np.prod(n)) + nv * 64)
+        check(R.ref_functional(fn.encode(), eq.encode(), bc.encode(), i3(n), g, d3(lo), d3(hi),
+                               int(prm.get("degree", 0)), D(prm.get("min_value", 0.0)),
+                               D(prm.get("max_value", 1.0)), prm.get("variables", "").encode(),
+                               D(prm.get("gamma", 1.4)), D(prm.get("p", 1.0)), int(prm.get("number_of_h", 1)),
+                               D(w), P(U), P(o), size))
+        cells = size[0] * size[1] * size[2]
+        out[name + "_U"] = U
+        out[name + "_out"] = o[:nv * cells].reshape(nv, cells)
+        out[name + "_size"] = np.array(list(size))
+    for name, (eq, n, g, d, p) in workloads.BV_DIRECTION_CASES.items():
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        nv = workloads.NVAR[eq]
+        o = np.zeros(nv)
+        check(R.ref_total_variation_direction(eq.encode(), i3(n), g, d, p, P(U), P(o)))
+        out["bvdir_" + name + "_U"] = U
+        out["bvdir_" + name + "_out"] = o
+    np.savez_compressed(os.path.join(HERE, "functional.npz"), **out)
+
+
 def structure_cases():
     rng = np.random.default_rng(20240603)
     out = {}
@@ -232,6 +261,7 @@ elif __name__ == "__main__":
     flux_cases()
     flux_extra_cases()
     structure_cases()
+    functional_cases()
     boundary_cases()
     meanvar_cases()
     run_cases()

@@ -182,3 +182,47 @@ def test_structure_cube_statistics_are_read(tmp_path):
     st = config.read_config(_xml(tmp_path, base(uq=uqx))).uq.stats[0]
     assert (st.name, st.p, st.number_of_h, st.number_of_saves) == ("structure_cube", 3.0, 7, 2)
     assert st.output_names() == ["structure_cube_3.000000"]
+
+
+def test_config_reads_functionals_and_functional_statistics(tmp_path):
+    import shutil
+    shutil.copy(os.path.join(INPUTS, "kh_uq.xml"), str(tmp_path / "kh_uq.xml"))
+    shutil.copy(os.path.join(INPUTS, "kh_global.py"), str(tmp_path / "kh_global.py"))
+    xml = str(tmp_path / "kh_uq.xml")
+    text = open(xml).read()
+    text = text.replace("<stats>", "<stats><stat><name>bv_direction</name><p>2</p><numberOfSaves>1</numberOfSaves>"
+                        "<writer><type>netcdf</type><basename>b</basename></writer></stat>"
+                        "<stat><name>functional</name><functionalName>structure_cube</functionalName><p>2</p>"
+                        "<numberOfH>3</numberOfH><numberOfSaves>1</numberOfSaves>"
+                        "<writer><type>netcdf</type><basename>s</basename></writer></stat>")
+    text = text.replace("</initialData>", "</initialData><functionals><functional><name>moment</name>"
+                        "<degree>2</degree><numberOfSaves>4</numberOfSaves><writer><type>numpy</type>"
+                        "<basename>mom</basename><numberOfSaves>4</numberOfSaves></writer></functional>"
+                        "</functionals>")
+    open(xml, "w").write(text)
+    cfg = config.read_config(xml)
+    assert [st.output_names() for st in cfg.uq.stats] == [
+        ["bv_x_2", "bv_y_2", "bv_z_2"], ["mean_structure_cube"], ["mean", "variance"]]
+    assert cfg.uq.stats[1].functional.number_of_h == 3
+    (fc,) = cfg.fvm.functionals
+    assert (fc.name, fc.degree, fc.number_of_saves, fc.writer.type) == ("moment", 2, 4, "numpy")
+    # the batch engine runs mean / variance only
+    from alsvinn_gb300 import runner
+    with pytest.raises(config.ConfigError):
+        runner.Runner(cfg, engine="batch")
+
+
+def test_config_rejects_unknown_functionals_and_time_integration(tmp_path):
+    import shutil
+    shutil.copy(os.path.join(INPUTS, "sod.xml"), str(tmp_path / "sod.xml"))
+    shutil.copy(os.path.join(INPUTS, "sod.py"), str(tmp_path / "sod.py"))
+    xml = str(tmp_path / "sod.xml")
+    base = open(xml).read()
+    for body in ("<functional><name>tecno</name><numberOfSaves>1</numberOfSaves></functional>",
+                 "<functional><name>identity</name><time>0.1</time><timeRadius>0.01</timeRadius></functional>",
+                 "<functional><name>moment</name><numberOfSaves>1</numberOfSaves>"
+                 "<writer><type>netcdf</type><basename>x</basename><numberOfSaves>1</numberOfSaves></writer>"
+                 "</functional>"):
+        open(xml, "w").write(base.replace("<writer>", "<functionals>%s</functionals><writer>" % body, 1))
+        with pytest.raises(config.ConfigError):
+            config.read_config(xml)

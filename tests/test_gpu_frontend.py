@@ -170,3 +170,120 @@ def test_alsuq_structure_functions_match_the_oracle(cuda_device, tmp_path):
     with netcdf(str(tmp_path / "kh_uq_sf_structure_cube_2.000000"), "r", mmap=False) as nc:
         assert nc.dimensions["x"] == 5
         np.testing.assert_allclose(np.array(nc.variables["rho"][0, 0]).reshape(-1), want[0], rtol=1e-12)
+
+
+FUNCTIONAL_STATS = (
+    "<stat><name>onepointmoment</name><p>2</p><numberOfSaves>1</numberOfSaves>"
+    "<writer><type>netcdf</type><basename>kh_m</basename></writer></stat>"
+    "<stat><name>bv</name><p>1</p><numberOfSaves>1</numberOfSaves>"
+    "<writer><type>netcdf</type><basename>kh_bv</basename></writer></stat>"
+    "<stat><name>bv_direction</name><p>2</p><numberOfSaves>1</numberOfSaves>"
+    "<writer><type>netcdf</type><basename>kh_bvd</basename></writer></stat>"
+    "<stat><name>functional</name><functionalName>log_entropy</functionalName><gamma>1.4</gamma>"
+    "<numberOfSaves>1</numberOfSaves><writer><type>netcdf</type><basename>kh_le</basename></writer></stat>"
+    "<stat><name>functional</name><functionalName>legendre_pointwise</functionalName><degree>3</degree>"
+    "<minValue>-4</minValue><maxValue>8</maxValue><variables>rho E</variables>"
+    "<numberOfSaves>1</numberOfSaves><writer><type>netcdf</type><basename>kh_lp</basename></writer></stat>")
+
+
+def test_alsuq_functional_statistics_match_the_oracle(cuda_device, tmp_path):
+    """onepointmoment, bv, bv_direction and functional statistics (log
+    entropy, Legendre) of the serial engine against the oracle's functionals
+    of the oracle's runs, averaged over the samples."""
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
+    xml = str(tmp_path / "kh_uq.xml")
+    text = open(xml).read().replace("<stats>", "<stats>" + FUNCTIONAL_STATS)
+    open(xml, "w").write(text)
+    cfg = config.read_config(xml)
+    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path))
+    assert r.engine == "serial"
+    r.run()
+    f, u = cfg.fvm, cfg.uq
+    g = lib.ghost_cells(f.reconstruction)
+    draws = runner.sample_parameters(u, range(u.samples))
+    states = []
+    for s in range(u.samples):
+        p = dict(f.init_parameters)
+        p.update(draws[s])
+        prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, p)
+        states.append(_oracle_run(f, prim, f.end_time, 1)[0])
+
+    def mean_of(name, **kw):
+        return sum(fvoracle.functional(name, f.equation, f.boundary, f.dimension, g, f.lower, f.upper, U, **kw)[0]
+                   for U in states) / u.samples
+
+    by_name = {st.name + (st.functional.name if st.functional else ""): k for k, st in enumerate(u.stats)}
+    n, got = r.statistics[by_name["onepointmoment"]][0]
+    assert n == u.samples
+    np.testing.assert_allclose(got[0], mean_of("moment", degree=2), rtol=1e-13)
+    np.testing.assert_allclose(r.statistics[by_name["bv"]][0][1][0], mean_of("bv", degree=1), rtol=1e-12)
+    # bv_direction keeps the last sample of the rank (the reference assigns its snapshot), divided by the count
+    last = states[-1]
+    for d in range(2):
+        want = fvoracle.functional("bv_direction", f.equation, f.boundary, f.dimension, g, f.lower, f.upper, last,
+                                   degree=2, direction=d)[0] / u.samples
+        np.testing.assert_allclose(r.statistics[by_name["bv_direction"]][0][1][d], want, rtol=1e-12)
+    np.testing.assert_allclose(r.statistics[by_name["functionallog_entropy"]][0][1][0],
+                               mean_of("log_entropy", gamma=1.4), rtol=1e-12)
+    lp = mean_of("legendre_pointwise", degree=3, min_value=-4.0, max_value=8.0, variables="rho E")
+    np.testing.assert_allclose(r.statistics[by_name["functionallegendre_pointwise"]][0][1][0], lp, rtol=1e-14,
+                               atol=1e-16)
+    # the files carry the reference's statistic names
+    for base, names in (("kh_m", ["m2"]), ("kh_bv", ["bv_1"]), ("kh_bvd", ["bv_x_2", "bv_y_2", "bv_z_2"]),
+                        ("kh_le", ["mean_log_entropy"]), ("kh_lp", ["mean_legendre_pointwise"])):
+        for nm in names:
+            path = tmp_path / ("%s_%s" % (base, nm))
+            assert path.exists(), path
+            with netcdf(str(path), "r", mmap=False) as nc:
+                assert "rho" in nc.variables
+
+
+def _padded(interior_values, n, g):
+    """A padded array (nvar, total) holding the interior values, zero ghosts."""
+    dim = 3 if n[2] > 1 else (2 if n[1] > 1 else 1)
+    t = [n[d] + 2 * g if d < dim else n[d] for d in range(3)]
+    V = np.zeros((interior_values.shape[0], t[2], t[1], t[0]))
+    gz, gy = (g if dim > 2 else 0), (g if dim > 1 else 0)
+    V[:, gz:gz + n[2], gy:gy + n[1], g:g + n[0]] = interior_values.reshape(interior_values.shape[0], n[2], n[1], n[0])
+    return V.reshape(V.shape[0], -1)
+
+
+def test_alsvinncli_functionals_write_at_their_save_times(cuda_device, tmp_path):
+    """<functionals>: identity every endTime / 2 (a second save clamp beside
+    the writer's endTime / 3) and log entropy every endTime / 3 (sharing the
+    writer's clamp), both written at t = 0 and at each of their save times."""
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    _copy_inputs(tmp_path, ["sod.xml", "sod.py"])
+    xml = str(tmp_path / "sod.xml")
+    text = open(xml).read().replace("<writer>", (
+        "<functionals>"
+        "<functional><name>identity</name><numberOfSaves>2</numberOfSaves>"
+        "<writer><type>netcdf</type><basename>sod_id</basename><numberOfSaves>2</numberOfSaves></writer>"
+        "</functional>"
+        "<functional><name>log_entropy</name><numberOfSaves>3</numberOfSaves>"
+        "<writer><type>netcdf</type><basename>sod_le</basename><numberOfSaves>3</numberOfSaves></writer>"
+        "</functional></functionals><writer>"), 1)
+    open(xml, "w").write(text)
+    assert alsvinncli.main([xml, "--precision", "fp64-exact"]) == 0
+    f = config.read_config(xml).fvm
+    g = lib.ghost_cells(f.reconstruction)
+    n = f.dimension
+    prim = initdata.evaluate(f.python_program, f.equation, f.lower, f.upper, f.dimension, f.init_parameters)
+    U0 = fvoracle.prim_to_cons(f.equation, n, g, f.gamma, _padded(prim.reshape(prim.shape[0], -1), n, g))
+    with netcdf(str(tmp_path / "sod_out.nc"), "r", mmap=False) as nc:
+        states = [np.stack([np.array(nc.variables[v][0, k]) for v in ("rho", "mx", "E")]) for k in range(3)]
+    with netcdf(str(tmp_path / "sod_id"), "r", mmap=False) as nc:
+        ident = [np.stack([np.array(nc.variables[v][0, k]) for v in ("rho", "mx", "E")]) for k in range(3)]
+    with netcdf(str(tmp_path / "sod_le"), "r", mmap=False) as nc:
+        le = np.array(nc.variables["E"][0]).reshape(4)
+    # the identity at t = 0 is the initial state; at the end it equals the writer's last save
+    assert np.array_equal(ident[0].reshape(3, -1), interior(U0, n, g).reshape(3, -1))
+    assert np.array_equal(ident[2], states[2])
+    # log entropy at t = 0 and at the writer's three save times (the same clamp)
+    want = [fvoracle.functional("log_entropy", f.equation, f.boundary, n, g, f.lower, f.upper, U0, gamma=f.gamma)[0]]
+    for k in range(3):
+        Uk = _padded(states[k].reshape(3, -1), n, g)
+        want.append(fvoracle.functional("log_entropy", f.equation, f.boundary, n, g, f.lower, f.upper, Uk,
+                                        gamma=f.gamma)[0])
+    np.testing.assert_allclose(le, [w[-1, 0] for w in want], rtol=1e-12)

@@ -125,3 +125,30 @@ def test_structure_cube_matches_reference(name):
     eq, bc, n, g, H, p = STRUCTURE_CASES[name]
     out = fvoracle.structure_cube(eq, bc, n, g, H, p, z[name + "_U"])
     assert np.array_equal(out, z[name + "_S"])
+
+
+# ---------------------------------------------------------------- functionals
+
+FUNCTIONAL_CASES = workloads.FUNCTIONAL_CASES
+BV_DIRECTION_CASES = workloads.BV_DIRECTION_CASES
+
+
+@pytest.mark.parametrize("name", sorted(FUNCTIONAL_CASES))
+def test_oracle_functionals_match_the_reference(name):
+    """The CPU functionals (Identity, Moment, LegendrePointWise, LogEntropy,
+    BoundedVariation, StructureCube) of the reference's own build."""
+    z = np.load(os.path.join(GOLDEN, "functional.npz"))
+    fn, eq, bc, n, g, lo, hi, prm, w = FUNCTIONAL_CASES[name]
+    got, size = fvoracle.functional(fn, eq, bc, n, g, lo, hi, z[name + "_U"], weight=w, **prm)
+    assert tuple(z[name + "_size"]) == size
+    # the reference's operations in its loop order, the same libm: bit for bit
+    assert np.array_equal(got, z[name + "_out"]), np.abs(got - z[name + "_out"]).max()
+
+
+@pytest.mark.parametrize("name", sorted(BV_DIRECTION_CASES))
+def test_oracle_total_variation_per_direction(name):
+    z = np.load(os.path.join(GOLDEN, "functional.npz"))
+    eq, n, g, d, p = BV_DIRECTION_CASES[name]
+    got, _ = fvoracle.functional("bv_direction", eq, "periodic", n, g, (0, 0, 0), (1, 1, 1),
+                                 z["bvdir_" + name + "_U"], degree=p, direction=d)
+    assert np.array_equal(got[:, 0], z["bvdir_" + name + "_out"])

@@ -171,3 +171,40 @@ GOLDEN_RUNS = {
                                gamma=1.4, cfl=0.475, end_time=0.5, number_of_saves=1, max_steps=0,
                                prim=lambda: burgers_prim(96, -0.4)),
 }
+
+
+# Functional fixtures (tests/golden/functional.npz, made by make_golden.py)
+# name: (functional, equation, boundary, n, ghosts, lower, upper, params, weight)
+FUNCTIONAL_CASES = {
+    "identity_euler2": ("identity", "euler2", "periodic", (9, 7, 1), 2, (0, 0, 0), (1, 1, 0), {}, 0.7),
+    "identity_burgers1d": ("identity", "burgers", "neumann", (20, 1, 1), 3, (0, 0, 0), (1, 1, 1), {}, 1.0),
+    "identity_euler3": ("identity", "euler3", "periodic", (5, 4, 3), 2, (0, 0, 0), (1, 1, 1), {}, 1.3),
+    "moment2_euler2": ("moment", "euler2", "periodic", (8, 6, 1), 2, (0, 0, 0), (1, 1, 0), {"degree": 2}, 0.5),
+    "moment3_burgers1d": ("moment", "burgers", "periodic", (17, 1, 1), 2, (0, 0, 0), (1, 1, 1), {"degree": 3}, 1.0),
+    "moment1_euler3": ("moment", "euler3", "neumann", (4, 5, 3), 1, (0, 0, 0), (1, 1, 1), {"degree": 1}, 2.0),
+    "legendre3_euler2": ("legendre_pointwise", "euler2", "periodic", (7, 6, 1), 2, (0, 0, 0), (1, 1, 0),
+                         {"degree": 3, "min_value": 0.0, "max_value": 10.0}, 1.0),
+    "legendre5_euler2_rhoE": ("legendre_pointwise", "euler2", "neumann", (6, 8, 1), 2, (0, 0, 0), (1, 1, 0),
+                              {"degree": 5, "min_value": -2.0, "max_value": 8.0, "variables": "rho E"}, 0.25),
+    "legendre0_burgers2d": ("legendre_pointwise", "burgers", "periodic", (5, 6, 1), 2, (0, 0, 0), (1, 1, 0),
+                            {"degree": 0, "min_value": -1.0, "max_value": 1.0}, 1.0),
+    "log_entropy_euler2": ("log_entropy", "euler2", "periodic", (8, 7, 1), 2, (0, 0, 0), (2, 1, 0),
+                           {"gamma": 1.4}, 0.9),
+    "log_entropy_euler1": ("log_entropy", "euler1", "neumann", (16, 1, 1), 2, (-5, 0, 0), (5, 1, 1),
+                           {"gamma": 5.0 / 3.0}, 1.0),
+    "log_entropy_euler3": ("log_entropy", "euler3", "periodic", (5, 4, 3), 2, (0, 0, 0), (1, 1, 1),
+                           {"gamma": 1.4}, 1.0),
+    "bv1_euler2": ("bv", "euler2", "periodic", (8, 7, 1), 2, (0, 0, 0), (1, 1, 0), {"degree": 1}, 1.0),
+    "bv2_burgers1d": ("bv", "burgers", "periodic", (19, 1, 1), 2, (0, 0, 0), (1, 1, 1), {"degree": 2}, 0.5),
+    "bv1_euler1": ("bv", "euler1", "neumann", (12, 1, 1), 3, (0, 0, 0), (1, 1, 1), {"degree": 1}, 1.0),
+    "structure_cube_euler2": ("structure_cube", "euler2", "periodic", (8, 6, 1), 2, (0, 0, 0), (1, 1, 0),
+                              {"p": 2.0, "number_of_h": 4}, 0.3),
+}
+
+# name: (equation, n, ghosts, direction, p)
+BV_DIRECTION_CASES = {
+    "euler2_x_p1": ("euler2", (8, 7, 1), 2, 0, 1),
+    "euler2_y_p1": ("euler2", (8, 7, 1), 2, 1, 1),
+    "euler3_z_p2": ("euler3", (5, 4, 3), 2, 2, 2),
+    "burgers1d_x_p3": ("burgers", (15, 1, 1), 2, 0, 3),
+}
