@@ -127,20 +127,16 @@ struct SmemLayout {
     static constexpr int HX = TX + 2 * GX, HY = TY + 2 * GY, HZ = TZ + 2 * GZ;
     static constexpr int HALO = HX * HY * HZ;
     // per-direction line buffers: reconstructed left/right values of the
-    // (T_d + 2) cells along d and the (T_d + 1) face fluxes, times the tile's
-    // extent in the other dimensions
+    // (T_d + 2) cells along d, times the tile's extent in the other
+    // dimensions; each face flux overwrites the right value it consumed
     static constexpr int REC0 = (TX + 2) * TY * TZ;
     static constexpr int REC1 = DIM > 1 ? TX * (TY + 2) * TZ : 0;
     static constexpr int REC2 = DIM > 2 ? TX * TY * (TZ + 2) : 0;
     static constexpr int REC = REC0 > REC1 ? (REC0 > REC2 ? REC0 : REC2) : (REC1 > REC2 ? REC1 : REC2);
-    static constexpr int FAC0 = (TX + 1) * TY * TZ;
-    static constexpr int FAC1 = DIM > 1 ? TX * (TY + 1) * TZ : 0;
-    static constexpr int FAC2 = DIM > 2 ? TX * TY * (TZ + 1) : 0;
-    static constexpr int FAC = FAC0 > FAC1 ? (FAC0 > FAC2 ? FAC0 : FAC2) : (FAC1 > FAC2 ? FAC1 : FAC2);
     static constexpr size_t round128(size_t b) { return (b + 127) & ~(size_t)127; }
     static constexpr size_t box_bytes = sizeof(R) * (size_t)NV * HALO;  // one halo of every variable
     static constexpr size_t halo_bytes = round128(box_bytes);           // its slot (TMA wants 128 B aligned)
-    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NV * REC + (size_t)NV * FAC);
+    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NV * REC);
     // Dynamic shared memory per kernel, plus 128 bytes to align the base:
     //   plain staging:    halo | line buffers
     //   TMA staging:      halo | line buffers, which first hold the L0 halo of the stage-1 modes
@@ -167,7 +163,7 @@ template <int NT, int NTH> struct CellsPerThread {
 
 // One direction D of the tile: reconstruct, face fluxes, accumulate into acc.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, int D>
-__device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc, R* acc, int tid,
+__device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc, int tid,
                                                const int* org, const Grid& G, R gamma, R& wsmax) {
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
@@ -242,7 +238,9 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         }
         const R w = Ph::template face_flux<D>(a, bb, gamma, F);
 #pragma unroll
-        for (int k = 0; k < NV; ++k) fc[k * NFACE + f] = F[k];
+        // the flux of face b replaces the right value of cell b - 1 (item il),
+        // which no other face reads
+        for (int k = 0; k < NV; ++k) rr[k * NREC + il] = F[k];
         // the face counts if both neighbours lie in the grid's interior range
         int c[3];
         c[D] = b;
@@ -266,13 +264,14 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* fc,
         const int cd = D == 0 ? cx : (D == 1 ? cy : cz);
         const int p = D == 0 ? cy : cx;
         const int q = D == 2 ? cy : cz;
-        // faces cd (left) and cd + 1 (right) of this cell's line
-        const int fli = D == 0 ? (p + O1 * q) * (TD + 1) + cd : (q * (TD + 1) + cd) * O1 + p;
+        // faces cd (left) and cd + 1 (right) of this cell's line, stored at
+        // the items of cells cd - 1 and cd
+        const int fli = D == 0 ? (p + O1 * q) * LEN + cd : (q * LEN + cd) * O1 + p;
         const int fri = D == 0 ? fli + 1 : fli + O1;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R fl = fc[k * NFACE + fli];
-            const R fr = fc[k * NFACE + fri];
+            const R fl = rr[k * NREC + fli];
+            const R fr = rr[k * NREC + fri];
             if constexpr (!kExact && D == 0)
                 acc[j * NV + k] = fl - fr;  // the first direction starts the sum
             else
@@ -405,7 +404,6 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     constexpr bool kSame = std::is_same<R, C>::value;
     C* rl = work;
     C* rr = rl + NV * SL::REC;
-    C* fc = rr + NV * SL::REC;
 
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;
@@ -425,11 +423,11 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     // conversion per thread gives the same double as converting every face)
     C wsd[3] = {C(0), C(0), C(0)};
     const C gamma = uniform_value<C>(A.gamma, A.gamma_f);
-    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[0]);
+    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[0]);
     if constexpr (DIM > 1)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[1]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[1]);
     if constexpr (DIM > 2)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 2>(su, rl, rr, fc, acc, tid, org, Gd, gamma, wsd[2]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 2>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[2]);
 
     // 3. wave speeds (stage 0 only): warp max, CTA max, one atomic per direction
     if (mode == MODE_L) {
