@@ -46,6 +46,7 @@ struct StageCandidate {
     int tma;      // 1: the kernels stage the halo by TMA (needs tensor maps)
     int halo[3];  // TMA box: the tile plus the ghost halo in each active dimension
     int nv;       // variables per cell (the box's fourth extent)
+    int min_blocks;  // resident CTAs per SM the single-grid kernel is compiled for
 };
 constexpr int kMaxCandidates = 6;
 

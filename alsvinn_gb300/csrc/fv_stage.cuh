@@ -565,8 +565,8 @@ __global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
 // The single-grid stage with the tile + halo staged by TMA (storage type =
 // arithmetic type). The maps are kernel parameters; shared memory: halo, then
 // the line buffers, which hold the L0 halo until U1 is formed.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH>
-__global__ void __launch_bounds__(NTH) stage_kernel_tma(StageArgs A, const __grid_constant__ TmaMaps M) {
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, int MINB = 1>
+__global__ void __launch_bounds__(NTH, MINB) stage_kernel_tma(StageArgs A, const __grid_constant__ TmaMaps M) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(R)];
     __shared__ __align__(8) unsigned long long bar;

@@ -49,7 +49,7 @@ namespace GBFV_VARIANT_NS {
 
 // One candidate configuration of a scheme's stage kernels (tile TX x TY x TZ,
 // NTH threads, TMA or plain halo staging) and its launchers.
-template <int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, bool TMA>
+template <int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, bool TMA, int MINB = 1>
 struct Cand {
     static constexpr int NV = Physics<Real, EQ, FLUX>::NV;
     static constexpr int G = ReconTraits<RC>::ghosts;
@@ -67,7 +67,7 @@ struct Cand {
         const dim3 grid((a.G.n[0] + TX - 1) / TX, (a.G.n[1] + TY - 1) / TY, (a.G.n[2] + TZ - 1) / TZ);
         if constexpr (TMA) {
             if (!maps) return (int)cudaErrorInvalidValue;
-            auto k = stage_kernel_tma<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH>;
+            auto k = stage_kernel_tma<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, MINB>;
             static int configured = 0;
             if (!configured) {
                 cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_smem);
@@ -121,6 +121,7 @@ struct Cand {
         c.halo[1] = SL::HY;
         c.halo[2] = SL::HZ;
         c.nv = NV;
+        c.min_blocks = MINB;
     }
 };
 
@@ -223,9 +224,9 @@ static void reg_dim(Registry& R) {
 // Autotuning candidates of the tuned schemes (WENO2 with HLL3 for Euler in
 // its own dimension, WENO2 with Godunov for 1D Burgers): TMA staging of the
 // default tile, taller / wider tiles with two cells per thread, a square
-// tile and a 32 x 12 tile on 384 threads (less halo work per cell than 32 x 8
-// at the same 24 resident warps per SM for FP64); 1D adds narrower tiles,
-// which give small grids more CTAs. Every
+// tile, and the 32 x 16 tile compiled for three resident CTAs per SM (a
+// register cap: more warps for the FP64 pipe's latency); 1D adds narrower
+// tiles, which give small grids more CTAs. Every
 // candidate computes the same values in the same order per cell (the tile
 // only changes which CTA computes a cell), so the states are bit-identical.
 template <int FLUX, int DIM>
@@ -241,7 +242,8 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 16, 16, 1, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 64, 8, 1, 256, true>::add(R, FLUX, RC);
-        Cand<E, FLUX, RC, 2, 32, 12, 1, 384, true>::add(R, FLUX, RC);
+        // 32 x 16 compiled for three resident CTAs per SM (register cap)
+        Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true, 3>::add(R, FLUX, RC);
     } else {
         Cand<E, FLUX, RC, 3, 8, 8, 4, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 3, 16, 8, 4, 256, true>::add(R, FLUX, RC);
