@@ -39,7 +39,7 @@ SUPPORTED_FVM_NODES = {
 }
 PLATFORMS = ("cpu", "cuda", "gb300")
 # alsuq statistics (REGISTER_STATISTICS in alsuq/src/stats/)
-STATISTICS = ("meanvar", "structure_cube", "functional", "onepointmoment", "bv", "bv_direction")
+STATISTICS = ("meanvar", "structure_cube", "structure_basic", "functional", "onepointmoment", "bv", "bv_direction")
 EQUATIONS = ("burgers", "euler1", "euler2", "euler3")
 PRIMITIVE_VARIABLES = {
     "burgers": ("u",),
@@ -174,11 +174,12 @@ class StatConfig:
     p: float = 2.0          # structure_cube: the exponent; onepointmoment, bv, bv_direction: the power
     number_of_h: int = 1    # structure_cube: distances 0 .. numberOfH - 1
     functional: Optional["FunctionalConfig"] = None  # the functional statistic's functional
+    direction: int = 0      # structure_basic: the axis
 
     def output_names(self):
         """The statistic's output names (getStatisticsNames): MeanVariance
         gives mean and variance, StructureCube "structure_cube_" plus p as
-        std::to_string prints a double, OnePointMoment "m<p>", BoundedVariation
+        std::to_string prints a double (StructureBasic likewise), OnePointMoment "m<p>", BoundedVariation
         "bv_<p>", BoundedVariationDirection "bv_x_<p>", "bv_y_<p>", "bv_z_<p>",
         FunctionalStatistics "mean_<functionalName>"
         (alsuq/src/stats/*.cpp constructors)."""
@@ -186,6 +187,8 @@ class StatConfig:
             return ["mean", "variance"]
         if self.name == "structure_cube":
             return ["structure_cube_%.6f" % self.p]
+        if self.name == "structure_basic":
+            return ["structure_basic_%.6f" % self.p]
         if self.name == "onepointmoment":
             return ["m%d" % int(self.p)]
         if self.name == "bv":
@@ -388,6 +391,9 @@ def read_uq(root):
         extra = {}
         if name == "structure_cube":
             extra = dict(p=float(_text(s, "p")), number_of_h=int(_text(s, "numberOfH")))
+        elif name == "structure_basic":
+            extra = dict(p=float(_text(s, "p")), number_of_h=int(_text(s, "numberOfH")),
+                         direction=int(_text(s, "direction")))
         elif name in ("onepointmoment", "bv", "bv_direction"):
             extra = dict(p=float(int(_text(s, "p"))))
         elif name == "functional":

@@ -117,6 +117,48 @@ __global__ void __launch_bounds__(kThreads) structure_kernel(const T* __restrict
     }
 }
 
+// Structure function along one axis (alsuq's StructureBasic,
+// alsuq/src/stats/StructureBasic.cpp:50-92): for h in 0 .. H-1,
+//     S(h) = sum over cells x of |u(x) - u(x + h e_dir)|^p / (nx ny nz),
+// the shifted point wrapped (periodic) or clamped (Neumann) to the interior
+// (ValueAtBoundary.hpp); pow as the reference's std::pow, one division per
+// term.
+template <class T>
+__global__ void __launch_bounds__(kThreads) structure_basic_kernel(const T* __restrict__ U, StructGrid G, int H,
+                                                                  double p, int dir, double* __restrict__ partial) {
+    __shared__ double red[kThreads / 32];
+    const int v = blockIdx.y;
+    const long long cells = (long long)G.n[0] * G.n[1] * G.n[2];
+    const long long c = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = c < cells;
+    int i = 0, j = 0, k = 0;
+    double uc = 0.0;
+    const T* u = U + (long long)v * G.total;
+    if (active) {
+        i = (int)(c % G.n[0]);
+        j = (int)((c / G.n[0]) % G.n[1]);
+        k = (int)(c / ((long long)G.n[0] * G.n[1]));
+        uc = (double)u[((long long)(k + G.g[2]) * G.t[1] + (j + G.g[1])) * G.t[0] + (i + G.g[0])];
+    }
+    const double ncells = (double)(G.n[0] * G.n[1] * G.n[2]);
+    for (int h = 0; h < H; ++h) {
+        double s = 0.0;
+        if (active) {
+            const double uh = (double)u[struct_index(G, i + (dir == 0) * h, j + (dir == 1) * h, k + (dir == 2) * h)];
+            s = pow(fabs(uc - uh), p) / ncells;
+        }
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+            partial[((long long)v * H + h) * gridDim.x + blockIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
 // sums[v * H + h] += the partials of (v, h) in block order
 __global__ void structure_finish(const double* __restrict__ partial, int nblocks, int count, double* sums) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -138,6 +180,7 @@ struct gbfv_structure {
     int ip = 0;
     int nblocks = 0;
     long long samples = 0;
+    int basic_dir = -1;  // >= 0: the axis structure function (structure_basic) along this axis
     double* d_partial = nullptr;
     double* d_sums = nullptr;
     cudaStream_t stream = nullptr;
@@ -146,6 +189,10 @@ struct gbfv_structure {
 template <class T>
 static void launch_structure(gbfv_structure* s, const T* U) {
     const dim3 grid((unsigned)s->nblocks, (unsigned)s->nvar);
+    if (s->basic_dir >= 0) {
+        structure_basic_kernel<T><<<grid, kThreads, 0, s->stream>>>(U, s->G, s->H, s->p, s->basic_dir, s->d_partial);
+        return;
+    }
     const double inv = 1.0 / ((double)s->G.n[0] * s->G.n[1] * s->G.n[2]);
     switch (s->ip) {
         case 1: structure_kernel<T, 1><<<grid, kThreads, 0, s->stream>>>(U, s->G, s->H, s->p, inv, s->d_partial); break;
@@ -196,6 +243,17 @@ int gbfv_structure_create(const char* boundary, const int n[3], int ghosts, int 
         return sfail(GBFV_ERR_MEMORY, std::string("gbfv_structure_create: ") + cudaGetErrorString(e));
     }
     *out = s;
+    return GBFV_OK;
+}
+
+int gbfv_structure_create_basic(const char* boundary, const int n[3], int ghosts, int nvar, int number_of_h,
+                                double p, int direction, gbfv_structure** out) {
+    if (!n || !out) return sfail(GBFV_ERR_ARGUMENT, "null argument");
+    const int dim = n[2] > 1 ? 3 : (n[1] > 1 ? 2 : 1);
+    if (direction < 0 || direction >= dim) return sfail(GBFV_ERR_ARGUMENT, "direction outside the grid's dimension");
+    const int r = gbfv_structure_create(boundary, n, ghosts, nvar, number_of_h, p, out);
+    if (r) return r;
+    (*out)->basic_dir = direction;
     return GBFV_OK;
 }
 

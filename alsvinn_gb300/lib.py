@@ -96,6 +96,9 @@ _SIGNATURES = {
     "gbfv_structure_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_structure_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_structure_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbfv_structure_create_basic": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_void_p)]),
     "gbfv_functional_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                               ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
@@ -557,10 +560,16 @@ class Functional:
 class Structure:
     """Cube structure function statistic (gbfv_structure_*)."""
 
-    def __init__(self, boundary, n, ghosts, nvar, number_of_h, p):
+    def __init__(self, boundary, n, ghosts, nvar, number_of_h, p, direction=None):
+        """direction None: the cube structure function (structure_cube);
+        0, 1, 2: the axis structure function along that axis (structure_basic)."""
         h = ctypes.c_void_p()
-        _check(load().gbfv_structure_create(boundary.encode(), _c_int3(*n), int(ghosts), int(nvar),
-                                            int(number_of_h), float(p), ctypes.byref(h)))
+        if direction is None:
+            _check(load().gbfv_structure_create(boundary.encode(), _c_int3(*n), int(ghosts), int(nvar),
+                                                int(number_of_h), float(p), ctypes.byref(h)))
+        else:
+            _check(load().gbfv_structure_create_basic(boundary.encode(), _c_int3(*n), int(ghosts), int(nvar),
+                                                      int(number_of_h), float(p), int(direction), ctypes.byref(h)))
         self.h = h
         self.nvar = int(nvar)
         self.number_of_h = int(number_of_h)

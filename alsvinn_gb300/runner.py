@@ -74,6 +74,8 @@ def make_statistic_accumulator(st, fvm, ghosts, nvar):
         return lib.Stats(nvar * int(np.prod([n[d] + 2 * ghosts if d < fvm.dim else n[d] for d in range(3)])))
     if st.name == "structure_cube":
         return lib.Structure(fvm.boundary, n, ghosts, nvar, st.number_of_h, st.p)
+    if st.name == "structure_basic":
+        return lib.Structure(fvm.boundary, n, ghosts, nvar, st.number_of_h, st.p, direction=st.direction)
     if st.name == "onepointmoment":
         fs = [lib.Functional("moment", fvm.equation, fvm.boundary, n, ghosts, lo, hi, degree=int(st.p))]
     elif st.name == "bv":
@@ -273,7 +275,7 @@ class Runner:
                 outputs = [(name, [interior(np.asarray(r[idx]).reshape(nv, -1), f.dimension, g) for r in results],
                             (f.lower, f.upper, f.dimension))
                            for name, idx in (("mean", 1), ("variance", 2))]
-            elif st.name == "structure_cube":
+            elif st.name in ("structure_cube", "structure_basic"):
                 # one value per distance h: x runs over h = 0 .. numberOfH - 1
                 H = st.number_of_h
                 outputs = [(st.output_names()[0], [np.asarray(r[1]).reshape(nv, 1, 1, H) for r in results],

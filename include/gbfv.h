@@ -248,6 +248,13 @@ int gbfv_structure_result(gbfv_structure* s, double* mean_host, long long* sampl
 int gbfv_structure_export(gbfv_structure* s, double* sums_host, long long* samples);
 /* Zeroes the sums and the sample count. */
 int gbfv_structure_reset(gbfv_structure* s);
+/* The axis structure function of alsuq's StructureBasic
+ * (alsuq/src/stats/StructureBasic.cpp:50-92): per variable and h = 0 ..
+ * number_of_h - 1, the sum over cells of |u(x) - u(x + h e_direction)|^p /
+ * (nx ny nz), the shifted point wrapped (periodic) or clamped (Neumann).
+ * The other gbfv_structure_* calls apply unchanged. */
+int gbfv_structure_create_basic(const char* boundary, const int n[3], int ghosts, int nvar, int number_of_h,
+                                double p, int direction, gbfv_structure** out);
 
 /* ------------------------------------------------------- functionals */
 

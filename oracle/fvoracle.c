@@ -1079,6 +1079,36 @@ int fv_structure_cube(const char* equation, const char* boundary, const int n[3]
     return 0;
 }
 
+/* StructureBasic::computeStructure (alsuq/src/stats/StructureBasic.cpp:
+ * 50-92): per variable, for every interior cell in the reference's loop
+ * order and h = 0 .. H-1, out[h] += pow(|u(x) - u(x + h e_d)|, p) / (nx ny nz),
+ * the shifted point through ValueAtBoundary (wrap or clamp). */
+int fv_structure_basic(const char* equation, const char* boundary, const int n[3], int ghosts, int number_of_h,
+                       double p, int direction, const double* U, double* out) {
+    const int eq = parse_eq(equation), bc = parse_bc(boundary);
+    if (eq < 0 || bc < 0 || number_of_h < 1) return fail(-1, "bad arguments");
+    grid_t G;
+    make_grid(&G, eq, n, ghosts, 1.4);
+    if (direction < 0 || direction >= G.dim) return fail(-1, "bad direction");
+    const int nx = n[0], ny = n[1], nz = n[2];
+    const int periodic = bc == BC_PERIODIC;
+    for (int v = 0; v < G.nvar; ++v) {
+        const double* u = U + (long)v * G.total;
+        double* o = out + (long)v * number_of_h;
+        for (int h = 0; h < number_of_h; ++h) o[h] = 0.0;
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    for (int h = 0; h < number_of_h; ++h) {
+                        const double uc = u[IDX(&G, i + G.g[0], j + G.g[1], k + G.g[2])];
+                        const double uh = u[structure_index(&G, periodic, i + (direction == 0) * h,
+                                                            j + (direction == 1) * h, k + (direction == 2) * h)];
+                        o[h] += pow(fabs(uc - uh), p) / (nx * ny * nz);
+                    }
+    }
+    return 0;
+}
+
 /* ---------------------------------------------------------- functionals */
 
 enum { FN_IDENTITY, FN_MOMENT, FN_LEGENDRE, FN_LOG_ENTROPY, FN_BV, FN_BV_DIRECTION, FN_STRUCTURE_CUBE };

@@ -59,6 +59,8 @@ int fv_structure_cube(const char* equation, const char* boundary, const int n[3]
                       double p, const double* U, double* out);
 int fv_meanvar(long count, int nsamples, const double* const* samples, double* mean,
                double* var);
+int fv_structure_basic(const char* equation, const char* boundary, const int n[3], int ghosts, int number_of_h,
+                       double p, int direction, const double* U, double* out);
 
 /* Functionals of one padded state: identity, moment, legendre_pointwise,
  * log_entropy, bv, bv_direction, structure_cube. out (nvar x output cells,

@@ -166,6 +166,15 @@ def functional(name, equation, boundary, n, ghosts, lower, upper, U, weight=1.0,
     return buf[:nv * cells].reshape(nv, cells), tuple(size)
 
 
+def structure_basic(equation, boundary, n, ghosts, number_of_h, p, direction, U):
+    """One sample's axis structure function (StructureBasic): (nvar, number_of_h)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    out = np.zeros((U.shape[0], number_of_h))
+    _check(load().fv_structure_basic(equation.encode(), boundary.encode(), _i3(n), int(ghosts), int(number_of_h),
+                                     D(p), int(direction), _p(U), _p(out)))
+    return out
+
+
 def meanvar(samples):
     samples = [np.ascontiguousarray(s, dtype=np.float64) for s in samples]
     count = samples[0].size

@@ -33,6 +33,7 @@
 #include "alsuq/generator/STLMersenne.hpp"
 #include "alsuq/mpi/Configuration.hpp"
 #include "alsuq/stats/MeanVariance.hpp"
+#include "alsuq/stats/StructureBasic.hpp"
 #include "alsuq/stats/StatisticsParameters.hpp"
 #include "alsutils/debug/stacktrace.hpp"
 
@@ -535,6 +536,42 @@ int ref_functional(const char* name, const char* equation, const char* boundary,
         size_out[1] = fs.y;
         size_out[2] = fs.z;
         return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
+// One sample's StructureBasic statistic (alsuq/src/stats/StructureBasic.cpp)
+// through the reference's StatisticsHelper on one rank: out receives nvar
+// arrays of number_of_h values.
+int ref_structure_basic(const char* equation, const char* boundary, const int dims[3], int ghosts, int number_of_h,
+    double p, int direction, const double* U, double* out) {
+    try {
+        double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+        Setup s(equation, "godunov", "none", boundary, "forwardeuler", dims, lo, hi, 1.4, 0.5);
+        boost::property_tree::ptree tree;
+        tree.put("direction", direction);
+        tree.put("p", p);
+        tree.put("numberOfH", number_of_h);
+        auto& sp = *new alsuq::stats::StatisticsParameters(tree);
+        sp.setNumberOfSamples(1);
+        sp.setPlatform("cpu");
+        sp.setMpiConfiguration(std::make_shared<alsutils::mpi::Configuration>(MPI_COMM_WORLD, "cpu"));
+        auto& sb = *new alsuq::stats::StructureBasic(sp);
+        const int nvar = nvar_of(equation);
+        auto w = std::make_shared<CaptureWriter>(out, nvar);
+        std::shared_ptr<io::Writer> ww(w);
+        sb.addWriter(sb.getStatisticsNames()[0], ww);
+        volume::VolumeFactory vf(equation, s.memory);
+        auto v = vf.createConservedVolume(dims[0], dims[1], dims[2], ghosts);
+        copy_in(*v, U, nvar);
+        simulator::TimestepInformation info(0.5, 1);
+        sb.computeStatistics(*v, *s.grid, info);
+        sb.combineStatistics();
+        sb.finalizeStatistics();
+        sb.writeStatistics(*s.grid);
+        return w->writes == 1 ? 0 : -1;
     } catch (std::exception& e) {
         g_error = e.what();
         return -1;

@@ -143,6 +143,20 @@ def functional_cases():
     np.savez_compressed(os.path.join(HERE, "functional.npz"), **out)
 
 
+def structure_basic_cases():
+    rng = np.random.default_rng(20241204)
+    out = {}
+    for name, (eq, bc, n, g, H, p, d) in workloads.STRUCTURE_BASIC_CASES.items():
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        nv = workloads.NVAR[eq]
+        o = np.zeros((nv, H))
+        check(R.ref_structure_basic(eq.encode(), bc.encode(), i3(n), g, H, D(p), d, P(U), P(o)))
+        out[name + "_U"] = U
+        out[name + "_S"] = o
+    np.savez_compressed(os.path.join(HERE, "structure_basic.npz"), **out)
+
+
 def structure_cases():
     rng = np.random.default_rng(20240603)
     out = {}
@@ -261,6 +275,7 @@ elif __name__ == "__main__":
     flux_cases()
     flux_extra_cases()
     structure_cases()
+    structure_basic_cases()
     functional_cases()
     boundary_cases()
     meanvar_cases()

@@ -152,3 +152,12 @@ def test_oracle_total_variation_per_direction(name):
     got, _ = fvoracle.functional("bv_direction", eq, "periodic", n, g, (0, 0, 0), (1, 1, 1),
                                  z["bvdir_" + name + "_U"], degree=p, direction=d)
     assert np.array_equal(got[:, 0], z["bvdir_" + name + "_out"])
+
+
+@pytest.mark.parametrize("name", sorted(workloads.STRUCTURE_BASIC_CASES))
+def test_oracle_structure_basic_matches_the_reference(name):
+    """StructureBasic (alsuq/src/stats/StructureBasic.cpp) of the reference's own build."""
+    z = np.load(os.path.join(GOLDEN, "structure_basic.npz"))
+    eq, bc, n, g, H, p, d = workloads.STRUCTURE_BASIC_CASES[name]
+    got = fvoracle.structure_basic(eq, bc, n, g, H, p, d, z[name + "_U"])
+    assert np.array_equal(got, z[name + "_S"]), np.abs(got - z[name + "_S"]).max()

@@ -208,3 +208,12 @@ BV_DIRECTION_CASES = {
     "euler3_z_p2": ("euler3", (5, 4, 3), 2, 2, 2),
     "burgers1d_x_p3": ("burgers", (15, 1, 1), 2, 0, 3),
 }
+
+# Axis structure functions (StructureBasic; tests/golden/structure_basic.npz)
+# name: (equation, boundary, n, ghosts, number_of_h, p, direction)
+STRUCTURE_BASIC_CASES = {
+    "euler2_periodic_x_p2": ("euler2", "periodic", (12, 10, 1), 2, 5, 2.0, 0),
+    "euler2_neumann_y_p1_5": ("euler2", "neumann", (9, 11, 1), 2, 6, 1.5, 1),
+    "burgers1d_periodic_p3": ("burgers", "periodic", (20, 1, 1), 3, 7, 3.0, 0),
+    "euler3_periodic_z_p2": ("euler3", "periodic", (5, 4, 6), 2, 4, 2.0, 2),
+}
