@@ -29,7 +29,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + C
 
 VARIANTS = (0, 1, 2, 3)   # fp64, fp64 exact, fp32, fp64 state with double-float arithmetic
 EQUATIONS = (0, 1, 2, 3)  # burgers, euler1, euler2, euler3
-TUNED_VARIANTS = (0, 1, 2)  # variants with autotuning candidates (TMA staging needs storage = arithmetic type)
+TUNED_VARIANTS = (0, 1, 2, 3)  # variants with autotuning candidates (all; TMA where storage = arithmetic type)
 
 
 def _nvcc():

@@ -552,8 +552,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const int* org, u
                                                                  reinterpret_cast<C*>(base + SL::halo_bytes), wred);
 }
 
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
-__global__ void __launch_bounds__(NTH) stage_kernel(StageArgs A) {
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R, int MINB = 1>
+__global__ void __launch_bounds__(NTH, MINB) stage_kernel(StageArgs A) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
     C* wred = reinterpret_cast<C*>(wred_raw);

@@ -1,11 +1,10 @@
 // Kernel instantiations for one arithmetic variant and one equation. This file
 // is compiled twice per (FV_VARIANT, FV_EQ) pair (FV_PART 0: every scheme's
 // default stage kernels and the operator-level kernels; FV_PART 1: the
-// autotuning candidates), so the units build in parallel. The fp64, fp64
-// exact and fp32 variants are built with -fmad=false: no multiply-add is
-// contracted unless the source writes the FMA, so every candidate of a
-// scheme rounds alike; the exact variant (FV_EXACT) writes none and follows
-// the reference's operation order.
+// autotuning candidates), so the units build in parallel. Every variant is
+// built with -fmad=false: no multiply-add is contracted unless the source
+// writes the FMA, so every candidate of a scheme rounds alike; the exact
+// variant (FV_EXACT) writes none and follows the reference's operation order.
 //   FV_VARIANT: 0 fp64, 1 fp64 exact, 2 fp32 state and arithmetic,
 //               3 fp64 state with double-float arithmetic on the FP32 pipes
 //   FV_EQ:      0 burgers, 1 euler1, 2 euler2, 3 euler3
@@ -76,7 +75,7 @@ struct Cand {
             }
             k<<<grid, NTH, stage_smem, s>>>(a, *maps);
         } else {
-            auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute>;
+            auto k = stage_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute, MINB>;
             static int configured = 0;
             if (!configured) {
                 cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_smem);
@@ -229,6 +228,22 @@ static void reg_dim(Registry& R) {
 // tiles, which give small grids more CTAs. Every
 // candidate computes the same values in the same order per cell (the tile
 // only changes which CTA computes a cell), so the states are bit-identical.
+#if FV_VARIANT == 3
+// The double-float variant stages through registers (FP64 -> double-float
+// pairs), so its candidates use per-thread loads: the default 16 x 12 tile
+// capped for four resident CTAs per SM, and 32 x 16 / 32 x 8 tiles for three
+// (2D; its kernels are barrier-bound and gain from more resident warps).
+template <int FLUX, int DIM>
+static void reg_tuned(Registry& R) {
+    constexpr int E = FV_EQ, RC = RC_WENO2;
+    if constexpr (DIM == 2) {
+        Cand<E, FLUX, RC, 2, 16, 12, 1, 256, false, 4>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 16, 1, 256, false, 3>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 8, 1, 256, false, 3>::add(R, FLUX, RC);
+    }
+    (void)R;
+}
+#else
 template <int FLUX, int DIM>
 static void reg_tuned(Registry& R) {
     constexpr int E = FV_EQ, RC = RC_WENO2;
@@ -251,6 +266,7 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 3, 16, 16, 2, 256, true>::add(R, FLUX, RC);
     }
 }
+#endif
 #endif
 
 }  // namespace GBFV_VARIANT_NS
@@ -301,13 +317,10 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
 extern "C" void FV_TUNE_FN(gbfv::Registry* R) {
     using namespace gbfv;
     using namespace gbfv::GBFV_VARIANT_NS;
-#if FV_VARIANT != 3
 #if FV_EQ == 0
     reg_tuned<FL_GODUNOV, 1>(*R);
 #else
     reg_tuned<FL_HLL3, FV_EQ>(*R);
 #endif
-#endif
-    (void)R;
 }
 #endif
