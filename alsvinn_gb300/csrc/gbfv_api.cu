@@ -640,23 +640,32 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
     return GBFV_OK;
 }
 
-// Makes candidate idx current: encodes its tensor maps of U, V, L (TMA
-// candidates whose maps cannot be encoded are refused).
-static int use_candidate(gbfv_solver* s, int idx) {
+// Makes candidate idx current: encodes its tensor maps of U, V, L. False
+// (nothing changed) when the grid cannot be staged by TMA.
+static bool try_candidate(gbfv_solver* s, int idx) {
     int n = 0;
     const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
-    if (idx < 0 || idx >= n) return fail(GBFV_ERR_ARGUMENT, "no such stage kernel candidate");
     if (c[idx].tma) {
         CUtensorMap m[3];
         void* bufs[3] = {s->U, s->V, s->L};
         for (int k = 0; k < 3; ++k)
             if (!gbfv_encode_state_map(&m[k], bufs[k], s->G, s->nvar, s->elem, c[idx].halo[0], c[idx].halo[1],
                                        c[idx].halo[2]))
-                return fail(GBFV_ERR_UNSUPPORTED, "this grid cannot be staged by TMA (padded rows must be multiples of 16 bytes)");
+                return false;
         std::memcpy(s->tm, m, sizeof m);
         s->tm_ok = true;
     }
     s->cand = idx;
+    return true;
+}
+
+static int use_candidate(gbfv_solver* s, int idx) {
+    int n = 0;
+    candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
+    if (idx < 0 || idx >= n) return fail(GBFV_ERR_ARGUMENT, "no such stage kernel candidate");
+    if (!try_candidate(s, idx))
+        return fail(GBFV_ERR_UNSUPPORTED,
+                    "this grid cannot be staged by TMA (padded rows must be multiples of 16 bytes)");
     return GBFV_OK;
 }
 
@@ -673,7 +682,7 @@ static int tune(gbfv_solver* s, bool force) {
              s->G.n[1], s->G.n[2]);
     int best = 0;
     if (n <= 1 || !gbfv_autotune_enabled()) return use_candidate(s, 0);
-    if (!force && gbfv_tune_cache_get(key, &best) && use_candidate(s, best) == GBFV_OK) return GBFV_OK;
+    if (!force && gbfv_tune_cache_get(key, &best) && best < n && try_candidate(s, best)) return GBFV_OK;
     StepState z;
     std::memset(&z, 0, sizeof z);
     cudaEvent_t e0, e1;
@@ -684,7 +693,7 @@ static int tune(gbfv_solver* s, bool force) {
     const int kTimed = 3;
     int err = GBFV_OK;
     for (int i = 0; i < n && err == GBFV_OK; ++i) {
-        if (use_candidate(s, i) != GBFV_OK) continue;  // not eligible (TMA rules)
+        if (!try_candidate(s, i)) continue;  // not eligible (TMA rules)
         const StageArgs a = stage_args(s, s->st_op, s->U, s->U, nullptr, s->L, MODE_L, 0);
         cudaError_t e = cudaMemcpyAsync(s->st_op, &z, sizeof z, cudaMemcpyHostToDevice, s->stream);
         int r = e == cudaSuccess ? launch_candidate(s, c[i], a) : (int)e;  // warm-up
