@@ -263,6 +263,51 @@ __device__ __forceinline__ void euler_conserved(const EulerState<R, NSD>& a, R* 
     c[1 + NSD] = a.E;
 }
 
+// The HLL3 branches given the wave-speed estimates, computing the point flux
+// of the one side each branch uses (the FP32 and double-float kernels: the
+// FP64 kernel computes both before branching, which costs fewer registers
+// there). The star branch's transverse velocities use
+// fR - fL - sR mR + sL mL = (uR - sR) mR - (uL - sL) mL, since the momentum
+// point fluxes are u_D m_k.
+template <class R, int NSD, int D>
+__device__ __forceinline__ R hll3_branches_one_side(const EulerState<R, NSD>& L, const EulerState<R, NSD>& Rs,
+                                                    R speedLeft, R speedRight, R* F) {
+    constexpr int NV = NSD + 2;
+    if (is0(speedLeft)) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) F[k] = R(0);
+    } else if (gt0(speedLeft)) {
+        euler_point_flux<R, NSD, D>(L, F);
+    } else if (lt0(speedRight)) {
+        euler_point_flux<R, NSD, D>(Rs, F);
+    } else {
+        const R udl = L.u[D] - speedLeft;
+        const R udr = Rs.u[D] - speedRight;
+        const R ainv = rcp_(fma(udr, Rs.rho, -(udl * L.rho)));
+        const R sm = (fma(Rs.m[D], udr, -(L.m[D] * udl)) + Rs.p - L.p) * ainv;
+        const bool leftSide = ge0(sm);
+        const EulerState<R, NSD>& S = leftSide ? L : Rs;
+        const R s = leftSide ? speedLeft : speedRight;
+        const R ud = leftSide ? udl : udr;
+        R fS[NV];
+        euler_point_flux<R, NSD, D>(S, fS);
+        // F = fS + s (U* - U) with each star component formed as a product
+        // minus the conserved value in one FMA
+        const R sinv = rcp_(sm - s);
+        const R mid0 = S.rho * ud * sinv;
+        F[0] = fma(s, mid0 - S.rho, fS[0]);
+#pragma unroll
+        for (int k = 0; k < NSD; ++k) {
+            const R usk = (k == D) ? sm : fma(udr, Rs.m[k], -(udl * L.m[k])) * ainv;
+            F[1 + k] = fma(s, fma(mid0, usk, -S.m[k]), fS[1 + k]);
+        }
+        const R pp = fma(S.rho * (S.u[D] - sm), ud, S.p);
+        const R eS = fma(ud, S.E, fma(S.p, S.u[D], -(pp * sm)));
+        F[1 + NSD] = fma(s, fma(eS, sinv, -S.E), fS[1 + NSD]);
+    }
+    return fmax_(fabs(speedLeft), fabs(speedRight));
+}
+
 // HLL3 (HLLC-type) flux F(left, right) in direction D with the reference's
 // extended speed estimate and its speedLeft == 0 -> F = 0 rule
 // (alsfvm/include/alsfvm/numflux/euler/HLL3.hpp:52-148). Returns
@@ -307,6 +352,10 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
             speedLeft = fmin_(L.u[D] + correct - cfLeft, ud - cs);
             speedRight = fmax_(Rs.u[D] - correct + cfRight, ud + cs);
         }
+    }
+    if constexpr (!kExact && !std::is_same<R, double>::value) {
+        // FP32 and double-float: evaluate only the point flux a branch uses
+        return hll3_branches_one_side<R, NSD, D>(L, Rs, speedLeft, speedRight, F);
     }
     R fluxLeft[NV], fluxRight[NV];
     euler_point_flux<R, NSD, D>(L, fluxLeft);

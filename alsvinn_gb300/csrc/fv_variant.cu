@@ -222,10 +222,10 @@ static void reg_dim(Registry& R) {
 #else
 // Autotuning candidates of the tuned schemes (WENO2 with HLL3 for Euler in
 // its own dimension, WENO2 with Godunov for 1D Burgers): TMA staging of the
-// default tile, taller / wider tiles with two cells per thread, a square
-// tile, and the 32 x 16 tile compiled for three resident CTAs per SM (a
-// register cap: more warps for the FP64 pipe's latency); 1D adds narrower
-// tiles, which give small grids more CTAs. Every
+// default tile, taller / wider tiles with two cells per thread and a square
+// tile; the 32 x 8, 16 x 16 and one 32 x 16 configuration are compiled for
+// three resident CTAs per SM (a register cap: more warps for the FP64 pipe's
+// latency); 1D adds narrower tiles, which give small grids more CTAs. Every
 // candidate computes the same values in the same order per cell (the tile
 // only changes which CTA computes a cell), so the states are bit-identical.
 #if FV_VARIANT == 3
@@ -253,9 +253,9 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 1, 32, 1, 1, 32, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 1, 240, 1, 1, 256, true>::add(R, FLUX, RC);
     } else if constexpr (DIM == 2) {
-        Cand<E, FLUX, RC, 2, 32, 8, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 32, 8, 1, 256, true, 3>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true>::add(R, FLUX, RC);
-        Cand<E, FLUX, RC, 2, 16, 16, 1, 256, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 2, 16, 16, 1, 256, true, 3>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 2, 64, 8, 1, 256, true>::add(R, FLUX, RC);
         // 32 x 16 compiled for three resident CTAs per SM (register cap)
         Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true, 3>::add(R, FLUX, RC);
