@@ -29,6 +29,7 @@ struct StepState {
     long long number_saved2;        // second save clamp's counter (FixedIntervalStatistics, starts at 1)
     int saved_mask;                 // bit k: save counter k advanced in the step just finished
     float scale_f;                  // scale rounded to float once, for the FP32 kernels
+    int just_saved;                 // ensemble: save index reached in the step just finished (-1: none)
 };
 
 struct StepParams {

@@ -77,7 +77,11 @@ __global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M,
     const MemberParam& P = mp[s];
     S.t = S.t + S.dt;
     S.steps += 1;
-    if (P.time_interval > 0 && S.t >= (double)S.number_saved * P.time_interval + 0.0) S.number_saved += 1;
+    S.just_saved = -1;
+    if (P.time_interval > 0 && S.t >= (double)S.number_saved * P.time_interval + 0.0) {
+        S.just_saved = (int)(S.number_saved - 1);  // save index k reached: t >= (k + 1) * interval
+        S.number_saved += 1;
+    }
     S.ws_bits[0] = S.ws_bits[1] = S.ws_bits[2] = 0ull;
     if (alternate) S.parity ^= 1;
     const bool reached = !(S.t < S.end_time);
@@ -102,23 +106,33 @@ __global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, 
     S.done = (!(S.t < end_time) || S.status != 0) ? 1 : 0;
 }
 
-// Welford order: members that reached end_time in this step, in member order.
-__global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* groups, int ngroups, int2* list, int* nlist) {
+// Welford order: members to fold in this step, in member order. With one
+// statistics save a member is folded when it reaches end_time; with nsaves
+// saves (FixedIntervalStatistics at (k + 1) end_time / nsaves) it is folded
+// into accumulator (group, k) at each save k its clamp stopped it at.
+// list[i] = (member, accumulator, count after the fold).
+__global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* accs, int nacc, int nsaves, int4* list,
+                                    int* nlist) {
     int m = 0;
     for (int s = 0; s < M; ++s) {
-        if (!st[s].just_done) continue;
+        const int done = st[s].just_done;
+        const int saved = st[s].just_saved;
         st[s].just_done = 0;
+        st[s].just_saved = -1;
+        const int k = nsaves <= 1 ? (done ? 0 : -1) : (st[s].status == 0 ? saved : -1);
+        if (k < 0 || k >= nsaves) continue;
         const int g = st[s].group;
-        if (g < 0 || g >= ngroups) continue;
-        groups[g].count += 1;
-        list[m++] = make_int2(s, (int)groups[g].count);
+        const int a = g * nsaves + k;
+        if (g < 0 || a >= nacc || !accs[a].mean) continue;
+        accs[a].count += 1;
+        list[m++] = make_int4(s, a, (int)accs[a].count, 0);
     }
     *nlist = m;
 }
 
 template <class R>
 __global__ void batch_stats_kernel(const BatchMember* members, const StepState* st, const GroupAcc* groups,
-                                   int ngroups, long long total_cells, const int2* list, const int* nlist) {
+                                   int ngroups, long long total_cells, const int4* list, const int* nlist) {
     const int m = *nlist;
     if (m == 0) return;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total_cells;
@@ -133,11 +147,11 @@ __global__ void batch_stats_kernel(const BatchMember* members, const StepState* 
         double mean = groups[g].mean[c], m2 = groups[g].m2[c];
         bool touched = false;
         for (int k = 0; k < m; ++k) {
+            if (list[k].y != g) continue;
             const int s = list[k].x;
-            if (st[s].group != g) continue;
             const R* u = reinterpret_cast<const R*>(st[s].parity ? members[s].v : members[s].u);
             const double x = (double)u[c];
-            const double n = (double)list[k].y;
+            const double n = (double)list[k].z;
             const double delta = x - mean;
             mean = mean + delta / n;
             m2 = m2 + delta * (x - mean);
@@ -193,10 +207,12 @@ struct gbfv_batch {
     size_t tile_cap = 0;
     bool tiles_dirty = true;
     // statistics
+    // accumulators: index group * stats_saves + save
     std::vector<GroupAcc> groups;
-    std::vector<int> group_dims;  // nvar*total per group
+    std::vector<int> group_dims;  // nvar*total per accumulator
     GroupAcc* d_groups = nullptr;
-    int2* d_list = nullptr;
+    int stats_saves = 1;
+    int4* d_list = nullptr;
     int* d_nlist = nullptr;
     long long stats_cells = 0;
     // running count
@@ -336,8 +352,8 @@ int enqueue_batch_step(gbfv_batch* b) {
     if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
     batch_finish_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.in == 1 ? 1 : 0);
     if (!b->groups.empty()) {
-        batch_assign_kernel<<<1, 1, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->d_list,
-                                            b->d_nlist);
+        batch_assign_kernel<<<1, 1, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->stats_saves,
+                                            b->d_list, b->d_nlist);
         const long long cells = b->stats_cells;
         unsigned nb = (unsigned)std::min<long long>((cells + 255) / 256, 152 * 8);
         if (b->scheme.elem == 8)
@@ -503,7 +519,7 @@ int gbfv_batch_create(const gbfv_desc* scheme, long long pool_bytes, int max_mem
     if (e == cudaSuccess) e = cudaMalloc(&b->d_maps, (size_t)3 * max_members * sizeof(CUtensorMap));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_states, max_members * sizeof(StepState));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ntiles, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_list, max_members * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_list, max_members * sizeof(int4));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_nlist, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_running, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_running, sizeof(int));
@@ -608,25 +624,29 @@ int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const d
         }
     if (off == (size_t)-1) return bfail(GBFV_ERR_MEMORY, "gbfv_batch_add: the ensemble pool has no room for this member");
     if (group >= 0) {
-        while ((int)b->groups.size() <= group) {
+        // the accumulators of this group, one per statistics save
+        const int S = b->stats_saves;
+        while ((int)b->groups.size() < (group + 1) * S) {
             GroupAcc g;
             std::memset(&g, 0, sizeof g);
             b->groups.push_back(g);
             b->group_dims.push_back(0);
         }
-        GroupAcc& g = b->groups[group];
         const long long cells = (long long)p.nvar * p.G.total;
-        if (g.mean && g.cells != cells) {
+        if (b->groups[group * S].mean && b->groups[group * S].cells != cells) {
             b->free_blocks[off] = need;
             return bfail(GBFV_ERR_ARGUMENT, "members of one statistics group must share their grid");
         }
-        if (!g.mean) {
-            BCUDA(cudaMalloc(&g.mean, cells * sizeof(double)));
-            BCUDA(cudaMalloc(&g.m2, cells * sizeof(double)));
-            BCUDA(cudaMemsetAsync(g.mean, 0, cells * sizeof(double), b->stream));
-            BCUDA(cudaMemsetAsync(g.m2, 0, cells * sizeof(double), b->stream));
-            g.cells = cells;
-            g.count = 0;
+        if (!b->groups[group * S].mean) {
+            for (int k = 0; k < S; ++k) {
+                GroupAcc& g = b->groups[group * S + k];
+                BCUDA(cudaMalloc(&g.mean, cells * sizeof(double)));
+                BCUDA(cudaMalloc(&g.m2, cells * sizeof(double)));
+                BCUDA(cudaMemsetAsync(g.mean, 0, cells * sizeof(double), b->stream));
+                BCUDA(cudaMemsetAsync(g.m2, 0, cells * sizeof(double), b->stream));
+                g.cells = cells;
+                g.count = 0;
+            }
             if (b->d_groups) cudaFree(b->d_groups);
             b->d_groups = nullptr;
             BCUDA(cudaMalloc(&b->d_groups, b->groups.size() * sizeof(GroupAcc)));
@@ -833,12 +853,19 @@ int gbfv_batch_member_state(gbfv_batch* b, int slot, double* host) {
     return GBFV_OK;
 }
 
+static int stats_index(const gbfv_batch* b, int group, int save) {
+    if (save < 0) save = b->stats_saves - 1;  // the last save (the end time)
+    const int a = group * b->stats_saves + save;
+    if (group < 0 || save >= b->stats_saves || a >= (int)b->groups.size() || !b->groups[a].mean) return -1;
+    return a;
+}
+
 int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double* var_host, long long* count) {
-    if (!b || group < 0 || group >= (int)b->groups.size() || !b->groups[group].mean)
-        return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group");
+    const int a = b ? stats_index(b, group, -1) : -1;
+    if (a < 0) return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group");
     BCUDA(cudaStreamSynchronize(b->stream));
     BCUDA(cudaMemcpy(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost));
-    const GroupAcc& g = b->groups[group];
+    const GroupAcc& g = b->groups[a];
     if (count) *count = g.count;
     if (g.count == 0) return bfail(GBFV_ERR_ARGUMENT, "no member of this group has reached the end time");
     std::vector<double> m2(g.cells);
@@ -851,11 +878,16 @@ int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double*
 }
 
 int gbfv_batch_stats_export(gbfv_batch* b, int group, double* mean_host, double* m2_host, long long* count) {
-    if (!b || group < 0 || group >= (int)b->groups.size() || !b->groups[group].mean)
-        return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group");
+    return gbfv_batch_stats_export_save(b, group, -1, mean_host, m2_host, count);
+}
+
+int gbfv_batch_stats_export_save(gbfv_batch* b, int group, int save, double* mean_host, double* m2_host,
+                                 long long* count) {
+    const int a = b ? stats_index(b, group, save) : -1;
+    if (a < 0) return bfail(GBFV_ERR_ARGUMENT, "unknown statistics group or save");
     BCUDA(cudaStreamSynchronize(b->stream));
     BCUDA(cudaMemcpy(b->groups.data(), b->d_groups, b->groups.size() * sizeof(GroupAcc), cudaMemcpyDeviceToHost));
-    const GroupAcc& g = b->groups[group];
+    const GroupAcc& g = b->groups[a];
     if (count) *count = g.count;
     if (mean_host) BCUDA(cudaMemcpy(mean_host, g.mean, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
     if (m2_host) BCUDA(cudaMemcpy(m2_host, g.m2, g.cells * sizeof(double), cudaMemcpyDeviceToHost));
@@ -902,6 +934,13 @@ int gbfv_batch_active(const gbfv_batch* b, int* count) {
 int gbfv_batch_launches(gbfv_batch* b, long long* launches) {
     if (!b || !launches) return bfail(GBFV_ERR_ARGUMENT, "null argument");
     *launches = b->launches;
+    return GBFV_OK;
+}
+
+int gbfv_batch_set_statistics_saves(gbfv_batch* b, int saves) {
+    if (!b || saves < 1) return bfail(GBFV_ERR_ARGUMENT, "statistics saves must be >= 1");
+    if (!b->groups.empty()) return bfail(GBFV_ERR_UNSUPPORTED, "set the statistics saves before adding members");
+    b->stats_saves = saves;
     return GBFV_OK;
 }
 

@@ -136,6 +136,9 @@ _SIGNATURES = {
     "gbfv_batch_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "gbfv_batch_select_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_batch_set_statistics_saves": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "gbfv_batch_stats_export_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                    ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_current_candidate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                                     ctypes.POINTER(ctypes.c_int)]),
     "gbfv_batch_autotune_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
@@ -674,14 +677,19 @@ class Batch:
         _check(load().gbfv_batch_stats_result(self.h, int(group), _ptr(m), _ptr(v), ctypes.byref(c)))
         return m, v, c.value
 
-    def stats_export(self, group, total):
-        """(count, mean, M2) of one group: the raw Welford triple for a
-        cross-rank merge (alsvinn_gb300.uq.combine_statistics)."""
+    def stats_export(self, group, total, save=-1):
+        """(count, mean, M2) of one group at statistics save `save` (-1: the
+        last): the raw Welford triple for a cross-rank merge
+        (alsvinn_gb300.uq.combine_statistics)."""
         m = np.zeros((self.nvar, total))
         q = np.zeros((self.nvar, total))
         c = ctypes.c_longlong()
-        _check(load().gbfv_batch_stats_export(self.h, int(group), _ptr(m), _ptr(q), ctypes.byref(c)))
+        _check(load().gbfv_batch_stats_export_save(self.h, int(group), int(save), _ptr(m), _ptr(q), ctypes.byref(c)))
         return c.value, m, q
+
+    def set_statistics_saves(self, saves):
+        """Statistics at `saves` save times (before the first member joins)."""
+        _check(load().gbfv_batch_set_statistics_saves(self.h, int(saves)))
 
     def stats_reset(self):
         _check(load().gbfv_batch_stats_reset(self.h))

@@ -132,14 +132,14 @@ class Runner:
         self.stats_interval = intervals.pop() if intervals else 0.0
         self.stats_saves = stats[0].number_of_saves if stats else 0
         self.stats_initial = bool(stats and stats[0].write_initial_timestep)
-        batch_ok = (self.fvm.writer is None and not self.fvm.functionals and self.stats_saves <= 1
+        batch_ok = (self.fvm.writer is None and not self.fvm.functionals
                     and not self.stats_initial and all(st.name == "meanvar" for st in stats)
                     and self.fvm.integrator in ("rungekutta2", "rungekutta3"))
         if engine == "auto":
             engine = "batch" if batch_ok else "serial"
         if engine == "batch" and not batch_ok:
-            raise ConfigError("the batch engine needs rungekutta2/3, mean/variance statistics at the end time only "
-                              "and no fvm writer; use the serial engine")
+            raise ConfigError("the batch engine needs rungekutta2/3, mean/variance statistics (no initial-time "
+                              "statistics) and no fvm writer or functionals; use the serial engine")
         self.engine = engine
         self.timesteps = 0
         self.wall_s = 0.0
@@ -228,12 +228,16 @@ class Runner:
         pool = wave * per + (16 << 20)
         b = lib.Batch(f.equation, f.flux, f.reconstruction, f.integrator, f.boundary, pool, wave, gamma=f.gamma,
                       cfl=f.cfl, precision=self.precision)
-        total = None
+        # statistics at each of the numberOfSaves save times, folded on the
+        # device as every member's save clamp stops it there
+        saves = max(1, self.stats_saves)
+        per_save = []
         try:
+            b.set_statistics_saves(saves)
             for i in range(0, len(self.samples), wave):
                 chunk = self.samples[i:i + wave]
                 slots = [b.add(f.dimension, f.lower, f.upper, self._prim(params[s]), group=0) for s in chunk]
-                b.advance(f.end_time, 1, 0)
+                b.advance(f.end_time, saves if self.stats_saves > 0 else 1, 0)
                 for sl in slots:
                     self.timesteps += b.member_time(sl)[1]
                     b.remove(sl)
@@ -241,13 +245,15 @@ class Runner:
             g = lib.ghost_cells(f.reconstruction)
             dim = f.dim
             total = int(np.prod([f.dimension[d] + 2 * g if d < dim else f.dimension[d] for d in range(3)]))
-            if self.samples:
-                n, m, q = b.stats_export(0, total)
-            else:
-                n, m, q = 0, np.zeros((nv, total)), np.zeros((nv, total))
+            for k in range(saves):
+                if self.samples:
+                    n, m, q = b.stats_export(0, total, save=k)
+                else:
+                    n, m, q = 0, np.zeros((nv, total)), np.zeros((nv, total))
+                per_save.append((n, m.reshape(-1), q.reshape(-1)))
         finally:
             b.close()
-        return [[(n, m.reshape(-1), q.reshape(-1))] for _ in self.uqc.stats]
+        return [list(per_save) for _ in self.uqc.stats]
 
     # -- output ------------------------------------------------------------
 

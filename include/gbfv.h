@@ -354,6 +354,15 @@ int gbfv_batch_stats_result(gbfv_batch* b, int group, double* mean_host, double*
 /* The raw Welford triple of one group (see gbfv_stats_export). */
 int gbfv_batch_stats_export(gbfv_batch* b, int group, double* mean_host, double* m2_host, long long* count);
 int gbfv_batch_stats_reset(gbfv_batch* b);
+/* Statistics at several save times (FixedIntervalStatistics with
+ * numberOfSaves = saves, alsuq/src/stats/FixedIntervalStatistics.cpp:33-86):
+ * set before the first member joins; each group then holds one accumulator
+ * per save k, into which a member is folded when its save clamp stops it at
+ * t = (k + 1) end_time / saves (advance with number_of_saves = saves). The
+ * functions above read the last save; _save reads save k. */
+int gbfv_batch_set_statistics_saves(gbfv_batch* b, int saves);
+int gbfv_batch_stats_export_save(gbfv_batch* b, int group, int save, double* mean_host, double* m2_host,
+                                 long long* count);
 
 /* Slots whose member has reached the end time of the last advance (up to
  * capacity written; *count = all of them), and the number of members. */

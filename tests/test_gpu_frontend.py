@@ -116,14 +116,17 @@ def test_alsuq_statistics_match_the_oracle(cuda_device, tmp_path, engine):
         np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-15)
 
 
-def test_alsuq_statistics_at_several_save_times(cuda_device, tmp_path):
+@pytest.mark.parametrize("engine", ["serial", "batch"])
+def test_alsuq_statistics_at_several_save_times(cuda_device, tmp_path, engine):
+    """Mean / variance at two save times: the serial engine's statistics
+    clamp, and the ensemble folding each member at its save clamp."""
     _copy_inputs(tmp_path, ["kh_uq.xml", "kh_global.py"])
     xml = str(tmp_path / "kh_uq.xml")
     text = open(xml).read().replace("<numberOfSaves>1</numberOfSaves>", "<numberOfSaves>2</numberOfSaves>")
     open(xml, "w").write(text)
     cfg = config.read_config(xml)
-    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path))
-    assert r.engine == "serial"
+    r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(tmp_path), engine=engine)
+    assert r.engine == engine
     results = r.run()
     assert len(results) == 2
     T = cfg.fvm.end_time

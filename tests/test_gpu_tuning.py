@@ -173,9 +173,9 @@ def _ensemble(precision, sizes, cand):
         b.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp64_df"])
 def test_ensemble_candidates_are_bit_identical(cuda_device, precision):
-    prec = PRECISIONS[precision]
+    prec = lib.FP64_DF if precision == "fp64_df" else PRECISIONS[precision]
     # 62: FP32 padded rows of 66 * 4 bytes break the TMA rule; that member
     # keeps per-thread loads inside a TMA candidate
     sizes = [64, 96, 40, 62] if precision == "fp32" else [64, 96, 40]
