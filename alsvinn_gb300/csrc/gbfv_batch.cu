@@ -110,24 +110,38 @@ __global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, 
 // statistics save a member is folded when it reaches end_time; with nsaves
 // saves (FixedIntervalStatistics at (k + 1) end_time / nsaves) it is folded
 // into accumulator (group, k) at each save k its clamp stopped it at.
-// list[i] = (member, accumulator, count after the fold).
+// list[i] = (member, accumulator, count after the fold). One warp: the lanes
+// read 32 members' flags at a time, lane 0 numbers the (few) folds in order.
 __global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* accs, int nacc, int nsaves, int4* list,
                                     int* nlist) {
+    const int lane = threadIdx.x;
     int m = 0;
-    for (int s = 0; s < M; ++s) {
-        const int done = st[s].just_done;
-        const int saved = st[s].just_saved;
-        st[s].just_done = 0;
-        st[s].just_saved = -1;
-        const int k = nsaves <= 1 ? (done ? 0 : -1) : (st[s].status == 0 ? saved : -1);
-        if (k < 0 || k >= nsaves) continue;
-        const int g = st[s].group;
-        const int a = g * nsaves + k;
-        if (g < 0 || a >= nacc || !accs[a].mean) continue;
-        accs[a].count += 1;
-        list[m++] = make_int4(s, a, (int)accs[a].count, 0);
+    for (int base = 0; base < M; base += 32) {
+        const int s = base + lane;
+        int a = -1;
+        if (s < M) {
+            const int done = st[s].just_done;
+            const int saved = st[s].just_saved;
+            if (done || saved >= 0) {
+                st[s].just_done = 0;
+                st[s].just_saved = -1;
+                const int k = nsaves <= 1 ? (done ? 0 : -1) : (st[s].status == 0 ? saved : -1);
+                const int g = st[s].group;
+                if (k >= 0 && k < nsaves && g >= 0 && g * nsaves + k < nacc) a = g * nsaves + k;
+            }
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, a >= 0);
+        while (mask) {
+            const int l = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int al = __shfl_sync(0xffffffffu, a, l);
+            if (lane == 0 && accs[al].mean) {
+                accs[al].count += 1;
+                list[m++] = make_int4(base + l, al, (int)accs[al].count, 0);
+            }
+        }
     }
-    *nlist = m;
+    if (lane == 0) *nlist = m;
 }
 
 template <class R>
@@ -352,8 +366,8 @@ int enqueue_batch_step(gbfv_batch* b) {
     if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
     batch_finish_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.in == 1 ? 1 : 0);
     if (!b->groups.empty()) {
-        batch_assign_kernel<<<1, 1, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->stats_saves,
-                                            b->d_list, b->d_nlist);
+        batch_assign_kernel<<<1, 32, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->stats_saves,
+                                             b->d_list, b->d_nlist);
         const long long cells = b->stats_cells;
         unsigned nb = (unsigned)std::min<long long>((cells + 255) / 256, 152 * 8);
         if (b->scheme.elem == 8)
