@@ -311,8 +311,9 @@ def run_gpu(args):
     achieved = alg_bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profile_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "%s<double,euler2,hll3,weno2,2D> tile %dx%d, %d threads" % (
-                    "stage_kernel_tma" if stage_kernel["tma"] else "stage_kernel", stage_kernel["tile"][0],
+                "kernel": "%s<double,euler2,hll3,weno2,2D>%s tile %dx%d, %d threads" % (
+                    "stage_kernel_tma" if stage_kernel["tma"] else "stage_kernel",
+                    " (double-float arithmetic)" if args.precision == "fp64-df" else "", stage_kernel["tile"][0],
                     stage_kernel["tile"][1], stage_kernel["threads"]), "launch_ms": per_launch_ms,
                 "alg_bytes_per_launch": alg_bytes_per_launch,
                 "note": "FP64 arithmetic on GB300 issues at ~1/64 of the FP32 rate; this step is FP64-compute "
@@ -322,6 +323,10 @@ def run_gpu(args):
                               "source": "ncu sm__pipe_fp64_cycles_active and DADD+DFMA+DMUL thread "
                                         "instructions per cycle over the 2 per SM per cycle peak "
                                         "(profiles/stage_kernel_tma_kh1024_fp64.md)"}}
+    if args.precision != "fp64":
+        # the traffic and FP64-pipe figures come from the FP64 kernel's capture
+        roofline["traffic"] = None
+        roofline["fp64_pipe"] = None
     clk = clocks.summary()
     line = None
     if rank == 0:
@@ -331,7 +336,7 @@ def run_gpu(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded KH interface perturbation, sample = rank)",
                 "config": {"workload": WORKLOAD, "grid": [N, N], "equation": "euler2", "reconstruction": "weno2",
-                           "flux": "hll3", "integrator": "rungekutta3", "precision": "fp64",
+                           "flux": "hll3", "integrator": "rungekutta3", "precision": args.precision,
                            "l2": "flushed before every timed step (512 MiB memset, outside the events)",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "stage_kernel": stage_kernel},
