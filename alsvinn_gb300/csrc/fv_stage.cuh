@@ -415,6 +415,25 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     const int mode = A.mode;
     const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
 
+    // The combination at the end reads U0 of the thread's cells from global
+    // memory (and, with per-thread staging of another type, the stage input):
+    // start those lines towards L1 now so they arrive during the compute.
+    if (mode != MODE_L) {
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const int cell = tid + j * NTH;
+            if (cell >= NT) continue;
+            const int ix = org[0] + cell % TX, iy = org[1] + (cell / TX) % TY, iz = org[2] + cell / (TX * TY);
+            if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) continue;
+            const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                asm volatile("prefetch.global.L1 [%0];\n" ::"l"(u0 + k * total + own));
+                if constexpr (!kSame) asm volatile("prefetch.global.L1 [%0];\n" ::"l"(in + k * total + own));
+            }
+        }
+    }
+
     // 2. flux difference per direction, per owned cell
     C acc[CPT * NV];
 #pragma unroll
