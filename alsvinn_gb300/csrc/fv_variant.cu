@@ -194,14 +194,14 @@ static int launch_check(const CheckArgs& a, cudaStream_t s) {
 }
 
 #if FV_PART == 0
-// The default candidate of a scheme: the variant's tile shape, plain loads,
-// compiled for three resident CTAs per SM at 256 threads (an 80-register
-// cap; the uncapped FP64 kernels used up to 95 registers, two CTAs per SM).
+// The default candidate of a scheme: the variant's tile shape, plain loads;
+// in 2D compiled for three resident CTAs per SM (an 80-register cap: the
+// uncapped FP64 kernels used up to 95 registers, two CTAs per SM). The 3D
+// kernels stay uncapped: at 80 registers they spill hundreds of bytes.
 template <int FLUX, int RC, int DIM>
 static void reg_one(Registry& R) {
     using TS = TileShape<DIM, FV_VARIANT>;
-    Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (TS::THREADS >= 256 ? 3 : 1)>::add(R, FLUX,
-                                                                                                        RC);
+    Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>::add(R, FLUX, RC);
 }
 
 // Every reconstruction for one flux in one dimension. The double-float
