@@ -256,12 +256,19 @@ struct gbfv_solver {
     CUtensorMap tm[3];
     bool tm_ok = false;
     std::vector<double> tune_ms;  // the autotuner's MODE_L time per candidate (-1: not eligible)
+    // kGraphSteps time steps captured as one CUDA graph, replayed for the
+    // long stretches of an advance (valid for graph_params and graph_cand)
+    cudaGraphExec_t step_graph = nullptr;
+    StepParams graph_params;
+    int graph_cand = -2;
+    long long graph_launches = 0;  // kernels in one replay
 };
 
 static size_t state_bytes(const gbfv_solver* s) { return (size_t)s->nvar * s->G.total * s->elem; }
 
 static void release(gbfv_solver* s) {
     if (!s) return;
+    if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
     for (auto& e : s->events) {
         cudaEventDestroy(e.first);
         cudaEventDestroy(e.second);
@@ -603,6 +610,54 @@ static int enqueue_step(gbfv_solver* s, const StepParams& P) {
 
 static int tune(gbfv_solver* s, bool force);
 
+constexpr int kGraphSteps = 16;
+
+static bool same_params(const StepParams& a, const StepParams& b) {
+    return a.cfl == b.cfl && a.cell_lengths[0] == b.cell_lengths[0] && a.cell_lengths[1] == b.cell_lengths[1] &&
+           a.cell_lengths[2] == b.cell_lengths[2] && a.end_time == b.end_time && a.time_interval == b.time_interval &&
+           a.dim == b.dim && a.time_interval2 == b.time_interval2 && a.stop_at_save == b.stop_at_save;
+}
+
+// Enqueues n time steps: groups of kGraphSteps replay one captured graph
+// (one launch instead of five per step; steps past the end of the advance
+// return at once, as in the direct path), the rest are launched directly.
+// Profiling keeps the direct path (per-launch events).
+static int enqueue_steps(gbfv_solver* s, const StepParams& P, int n) {
+    if (!s->profiling && n >= kGraphSteps) {
+        if (!s->step_graph || !same_params(s->graph_params, P) || s->graph_cand != s->cand) {
+            if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
+            s->step_graph = nullptr;
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            const long long before = s->launches;
+            int r = GBFV_OK;
+            for (int i = 0; i < kGraphSteps && !r; ++i) r = enqueue_step(s, P);
+            const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+            s->graph_launches = s->launches - before;
+            s->launches = before;
+            if (r) {
+                if (g) cudaGraphDestroy(g);
+                return r;
+            }
+            if (ce != cudaSuccess) return fail(GBFV_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(ce));
+            const cudaError_t ie = cudaGraphInstantiate(&s->step_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return fail(GBFV_ERR_CUDA, std::string("step graph: ") + cudaGetErrorString(ie));
+            s->graph_params = P;
+            s->graph_cand = s->cand;
+        }
+        for (; n >= kGraphSteps; n -= kGraphSteps) {
+            CUDA_TRY(cudaGraphLaunch(s->step_graph, s->stream));
+            s->launches += s->graph_launches;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const int r = enqueue_step(s, P);
+        if (r) return r;
+    }
+    return GBFV_OK;
+}
+
 static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
     if (s->cand < 0 && !s->pinned) {
         const int r = tune(s, false);
@@ -613,10 +668,8 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
     s->launches += 1;
     int chunk = 1;
     for (;;) {
-        for (int i = 0; i < chunk; ++i) {
-            int r = enqueue_step(s, P);
-            if (r) return r;
-        }
+        const int r = enqueue_steps(s, P, chunk);
+        if (r) return r;
         CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         if (s->st_host->done) break;
