@@ -193,3 +193,30 @@ def test_ensemble_candidates_are_bit_identical(cuda_device, precision):
         for (tg, sg), (tr, sr) in zip(got, ref):
             assert tg == tr, (i, cands[i])
             assert np.array_equal(sg, sr), (i, cands[i])
+
+
+@pytest.mark.parametrize("case,integ", [("kh2d", None), ("burgers1d_rk2", None), ("sod1d", "forwardeuler")])
+def test_step_graph_replay_matches_direct_launches(cuda_device, case, integ):
+    """Advances of 16 steps and more replay a captured graph of 16 steps;
+    with profiling on, every kernel is launched directly. Both must give
+    the same bits, the same time and step count, whether the advance stops
+    on a step limit or inside a replayed group at its end time."""
+    eq, flux, integ0, bc, n, lo, hi, prim = CASES[case]
+    integ = integ or integ0
+    out = []
+    for direct in (False, True):
+        s = lib.Solver(eq, flux, "weno2", integ, bc, n, lo, hi, cfl=0.4, precision=lib.FP64)
+        try:
+            s.set_primitive(np.asarray(prim(n), dtype=np.float64).reshape(s.nvar, -1))
+            s.profile(direct)
+            s.advance(1e9, 0, 100)
+            t1, steps1, _ = s.time()
+            assert steps1 == 100
+            # an end time 37.5 steps further on: the advance ends inside a group
+            s.advance(t1 + 37.5 * (t1 / steps1), 0, 0)
+            out.append((s.get_state(), s.time()[:2], t1))
+        finally:
+            s.close()
+    (a, ta, t1a), (b, tb, t1b) = out
+    assert t1a == t1b and ta == tb
+    assert np.array_equal(a, b)
