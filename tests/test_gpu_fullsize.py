@@ -1,0 +1,127 @@
+"""Parity at the full sizes of the benchmark workloads: Kelvin-Helmholtz on
+1024 x 1024 and Taylor-Green on 256^3, a few steps each against the oracle
+run on the same initial data (bit-identical for the exact variant), plus
+size-independent properties over longer runs: conservation of every
+conserved total on the periodic domain, and the same state whether a run is
+advanced in one call or in pieces.
+
+Tolerances as in the other parity tests: FP64 <= 1e-10 relative L1 per
+conserved variable, the double-float variant 1e-10 (1e-9 on Taylor-Green's
+z momentum, which starts at zero under a pressure of 100), FP32 state-scaled
+L1 <= 1e-4 against the FP64 oracle.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from alsvinn_gb300 import lib
+from conftest import interior, rel_l1
+from oracle import fvoracle
+
+pytestmark = pytest.mark.gpu
+
+KH = dict(equation="euler2", n=(1024, 1024, 1), lower=(0, 0, 0), upper=(1, 1, 0), cfl=0.4, steps=3, nv=4)
+TG = dict(equation="euler3", n=(256, 256, 256), lower=(0, 0, 0), upper=(2 * math.pi,) * 3, cfl=0.4, steps=2, nv=5)
+G = 2  # WENO2 ghost width
+
+
+def _prim(case):
+    if case is KH:
+        return lib.init_kelvin_helmholtz(1024, sample=0)
+    return lib.init_taylor_green(256)
+
+
+def _scaled_l1(a, b):
+    a = a.reshape(a.shape[0], -1)
+    b = b.reshape(b.shape[0], -1)
+    return np.abs(a - b).sum(axis=1) / np.abs(b[0]).sum()
+
+
+_ORACLE = {}
+
+
+def _oracle(name):
+    """The oracle's state after the case's steps (computed once per case)."""
+    if name not in _ORACLE:
+        case = KH if name == "kh1024" else TG
+        rc, U, t, steps = fvoracle.run(case["equation"], "hll3", "weno2", "rungekutta3", "periodic", case["n"],
+                                       case["lower"], case["upper"], 1.4, case["cfl"], 1e9, 0, case["steps"],
+                                       _prim(case), G, case["nv"])
+        assert rc == 0 and steps == case["steps"]
+        _ORACLE.clear()  # one full-size reference state held at a time
+        _ORACLE[name] = (U, t)
+    return _ORACLE[name]
+
+
+def _solver(case, precision):
+    s = lib.Solver(case["equation"], "hll3", "weno2", "rungekutta3", "periodic", case["n"], case["lower"],
+                   case["upper"], cfl=case["cfl"], precision=precision)
+    s.set_primitive(_prim(case))
+    return s
+
+
+@pytest.mark.parametrize("precision", ["fp64_exact", "fp64", "fp64_df", "fp32"])
+@pytest.mark.parametrize("name", ["kh1024", "tg256"])
+def test_full_size_steps_match_oracle(cuda_device, name, precision):
+    case = KH if name == "kh1024" else TG
+    prec = {"fp64_exact": lib.FP64_EXACT, "fp64": lib.FP64, "fp64_df": lib.FP64_DF, "fp32": lib.FP32}[precision]
+    ref, ref_t = _oracle(name)
+    s = _solver(case, prec)
+    try:
+        s.advance(1e9, 0, case["steps"])
+        t, steps, _ = s.time()
+        U = s.get_state()
+    finally:
+        s.close()
+    assert steps == case["steps"]
+    if prec == lib.FP64_EXACT:
+        assert t == ref_t
+        assert np.array_equal(U, ref)
+        return
+    a, b = interior(U, case["n"], G), interior(ref, case["n"], G)
+    if prec == lib.FP32:
+        err = _scaled_l1(a, b)
+        assert (err <= 1e-4).all(), err
+    else:
+        assert abs(t - ref_t) <= 1e-12 * ref_t
+        tol = 1e-9 if (prec == lib.FP64_DF and name == "tg256") else 1e-10
+        err = rel_l1(a, b)
+        assert (err <= tol).all(), err
+
+
+@pytest.mark.parametrize("precision,tol", [(lib.FP64, 1e-12), (lib.FP64_DF, 1e-12), (lib.FP32, 1e-5)])
+def test_full_size_kh_conserves_totals(cuda_device, precision, tol):
+    """On the periodic domain every face flux enters its two cells with
+    opposite signs, so the totals of density, momentum and energy stay at
+    their initial values up to the rounding of the per-cell updates; the
+    change per variable is measured against the total mass."""
+    s = _solver(KH, precision)
+    try:
+        U0 = interior(s.get_state(), KH["n"], G).reshape(4, -1)
+        s.advance(1e9, 0, 40)
+        U1 = interior(s.get_state(), KH["n"], G).reshape(4, -1)
+    finally:
+        s.close()
+    mass = np.abs(U0[0]).sum()
+    change = np.abs(U1.sum(axis=1) - U0.sum(axis=1)) / mass
+    assert (change <= tol).all(), change
+    assert not np.array_equal(U0, U1)
+
+
+def test_full_size_kh_pieces_equal_one_advance(cuda_device):
+    """40 steps in one advance, and as 1 + 16 + 23 steps (direct launches,
+    one replayed group, a group and a remainder): the same bits."""
+    out = []
+    for pieces in ((40,), (1, 16, 23)):
+        s = _solver(KH, lib.FP64)
+        try:
+            for p in pieces:
+                s.advance(1e9, 0, p)
+            t, steps, _ = s.time()
+            assert steps == 40
+            out.append((s.get_state(), t))
+        finally:
+            s.close()
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][0], out[1][0])
