@@ -416,9 +416,12 @@ long long running_cells(const gbfv_batch* b) {
 }
 
 // The ensemble autotuner: with the step states of the current advance on the
-// device (after the begin kernel), times MODE_L launches of every candidate
-// over the running members (out = each member's L buffer, wave speeds into a
-// copy of the step states: no effect on the run) and keeps the fastest. The
+// device (after the begin kernel), times the stage launches of every
+// candidate over the running members and keeps the fastest: MODE_L (out =
+// each member's L buffer) and, for SSP-RK3, the first combination stage
+// (out = each member's V buffer, which every step rewrites before reading),
+// scored as one step's L + 2 x stage-1 launches; wave speeds and step
+// updates go into a copy of the step states, so the run is unaffected. The
 // choice is cached per scheme for the process; ensembles below 2^22 running
 // cells keep their current candidate and are tuned at a later advance (small
 // ensembles are launch-latency bound and time every candidate alike).
@@ -464,19 +467,27 @@ int tune_batch(gbfv_batch* b, bool force) {
         const BatchLauncher launch = current(b).batch;
         cudaError_t e = cudaMemcpyAsync(b->d_tune_states, b->d_states, M * sizeof(StepState),
                                         cudaMemcpyDeviceToDevice, b->stream);
-        int r = e == cudaSuccess ? launch(a, 0, b->stream) : (int)e;  // warm-up
-        if (!r) r = (int)cudaEventRecord(e0, b->stream);
-        for (int k = 0; k < kTimed && !r; ++k) r = launch(a, 0, b->stream);
-        if (!r) r = (int)cudaEventRecord(e1, b->stream);
-        if (!r) r = (int)cudaEventSynchronize(e1);
-        float ms = 0;
-        if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+        int r = e == cudaSuccess ? 0 : (int)e;
+        const int nmodes = p.in == 2 ? 2 : 1;
+        double step_ms = 0;
+        for (int m = 0; m < nmodes && !r; ++m) {
+            a.mode = m == 0 ? MODE_L : MODE_RK3_S1;
+            r = launch(a, 0, b->stream);  // warm-up
+            if (!r) r = (int)cudaEventRecord(e0, b->stream);
+            for (int k = 0; k < kTimed && !r; ++k) r = launch(a, 0, b->stream);
+            if (!r) r = (int)cudaEventRecord(e1, b->stream);
+            if (!r) r = (int)cudaEventSynchronize(e1);
+            float ms = 0;
+            if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+            step_ms += (m == 0 ? 1.0 : 2.0) * ms / kTimed;
+            b->launches += 1 + kTimed;
+        }
         if (r) {
             err = bfail(GBFV_ERR_CUDA, std::string("ensemble autotuning launch: ") + cudaGetErrorString((cudaError_t)r));
             break;
         }
-        b->launches += 1 + kTimed;
-        b->tune_ms[i] = ms / kTimed;
+        // per stage launch of one step
+        b->tune_ms[i] = step_ms / (nmodes == 2 ? 3.0 : 1.0);
         if (i == 0 || b->tune_ms[i] < best_ms) {
             best_ms = b->tune_ms[i];
             best = i;

@@ -416,7 +416,8 @@ def run_uq(args):
     stage_kernel = {"candidate": cand, "tile": list(cands[cand][0]), "threads": cands[cand][1],
                     "tma": cands[cand][2], "members_staged_by_tma": tma_members,
                     "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
-                                               for c, m in zip(cands, tune_ms)]}
+                                               for c, m in zip(cands, tune_ms)],
+                    "autotune_score": "mean stage launch of one RK3 step over all members: (MODE_L + 2 x stage 1) / 3"}
 
     # plain FP64, one solve at a time, each size
     plain_step_ms = {}
