@@ -747,21 +747,31 @@ static int tune(gbfv_solver* s, bool force) {
     int err = GBFV_OK;
     for (int i = 0; i < n && err == GBFV_OK; ++i) {
         if (!try_candidate(s, i)) continue;  // not eligible (TMA rules)
-        const StageArgs a = stage_args(s, s->st_op, s->U, s->U, nullptr, s->L, MODE_L, 0);
         cudaError_t e = cudaMemcpyAsync(s->st_op, &z, sizeof z, cudaMemcpyHostToDevice, s->stream);
-        int r = e == cudaSuccess ? launch_candidate(s, c[i], a) : (int)e;  // warm-up
-        if (!r) r = (int)cudaEventRecord(e0, s->stream);
-        for (int k = 0; k < kTimed && !r; ++k) r = launch_candidate(s, c[i], a);
-        if (!r) r = (int)cudaEventRecord(e1, s->stream);
-        if (!r) r = (int)cudaEventSynchronize(e1);
-        float ms = 0;
-        if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+        int r = e == cudaSuccess ? 0 : (int)e;
+        // SSP-RK3: one step is MODE_L plus two combination stages, timed as
+        // L + 2 x stage 1 (stage 1 writes the V scratch; dt = 0 in st_op)
+        const int nmodes = s->in == IN_RK3 ? 2 : 1;
+        double step_ms = 0;
+        for (int m = 0; m < nmodes && !r; ++m) {
+            const StageArgs a = m == 0 ? stage_args(s, s->st_op, s->U, s->U, nullptr, s->L, MODE_L, 0)
+                                       : stage_args(s, s->st_op, s->U, s->U, s->L, s->V, MODE_RK3_S1, 0);
+            r = launch_candidate(s, c[i], a);  // warm-up
+            if (!r) r = (int)cudaEventRecord(e0, s->stream);
+            for (int k = 0; k < kTimed && !r; ++k) r = launch_candidate(s, c[i], a);
+            if (!r) r = (int)cudaEventRecord(e1, s->stream);
+            if (!r) r = (int)cudaEventSynchronize(e1);
+            float ms = 0;
+            if (!r) r = (int)cudaEventElapsedTime(&ms, e0, e1);
+            step_ms += (m == 0 ? 1.0 : 2.0) * ms / kTimed;
+            s->launches += 1 + kTimed;
+        }
         if (r) {
             err = fail(GBFV_ERR_CUDA, std::string("autotuning launch: ") + cudaGetErrorString((cudaError_t)r));
             break;
         }
-        s->launches += 1 + kTimed;
-        s->tune_ms[i] = ms / kTimed;
+        // per stage launch of one step
+        s->tune_ms[i] = step_ms / (nmodes == 2 ? 3.0 : 1.0);
         if (i == 0 || s->tune_ms[i] < best_ms) {
             best_ms = s->tune_ms[i];
             best = i;

@@ -411,7 +411,8 @@ class Solver:
         return i.value
 
     def autotune(self):
-        """Runs the autotuner now: (chosen index, [ms per MODE_L launch or -1])."""
+        """Runs the autotuner now: (chosen index, [mean ms per stage launch of
+        one step, or -1 where not eligible])."""
         n = len(self.candidates())
         ms = (ctypes.c_double * max(n, 1))()
         chosen = ctypes.c_int()

@@ -162,8 +162,9 @@ int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt);
  * (t_x * element size) that are multiples of 16 bytes.
  *   gbfv_select_candidate: pin candidate idx (-1: back to the autotuner);
  *     GBFV_ERR_UNSUPPORTED when the grid cannot be staged by TMA.
- *   gbfv_autotune: tune now; ms[i] = the candidate's time per MODE_L launch
- *     (-1: not eligible), *chosen = the candidate kept.
+ *   gbfv_autotune: tune now; ms[i] = the candidate's mean time per stage
+ *     launch of one step (SSP-RK3: (MODE_L + 2 x stage 1) / 3; otherwise
+ *     MODE_L; -1: not eligible), *chosen = the candidate kept.
  *   gbfv_current_candidate: the candidate in use (-1: not chosen yet). */
 int gbfv_candidate_count(gbfv_solver* s, int* count);
 int gbfv_candidate_info(gbfv_solver* s, int idx, int tile[3], int* threads, int* tma);
@@ -382,8 +383,10 @@ int gbfv_batch_stream(gbfv_batch* b, void** stream);
  *   gbfv_batch_select_candidate: pin candidate idx (-1: back to the autotuner).
  *   gbfv_batch_current_candidate: the candidate in use; *member_tma = members
  *     staged by TMA.
- *   gbfv_batch_autotune_result: per candidate the time of one MODE_L launch
- *     over the running members when the autotuner ran (-1: not timed). */
+ *   gbfv_batch_autotune_result: per candidate the mean time per stage
+ *     launch of one step over the running members (SSP-RK3: (MODE_L + 2 x
+ *     stage 1) / 3; otherwise MODE_L) when the autotuner ran (-1: not
+ *     timed). */
 int gbfv_batch_select_candidate(gbfv_batch* b, int idx);
 int gbfv_batch_current_candidate(gbfv_batch* b, int* idx, int* member_tma);
 int gbfv_batch_autotune_result(gbfv_batch* b, double* ms, int capacity);

@@ -151,6 +151,27 @@ def test_autotuner_times_every_eligible_candidate(cuda_device):
         s.close()
 
 
+@pytest.mark.parametrize("precision", [lib.FP64, lib.FP32])
+def test_autotuning_leaves_the_solve_untouched(cuda_device, precision):
+    """The tuner's launches write only scratch (L, V, a scratch step state):
+    tuning first and then stepping equals stepping with the chosen
+    candidate pinned from the start."""
+    s = _solver("kh2d", precision)
+    try:
+        chosen, _ = s.autotune()
+        s.advance(1e9, 0, STEPS)
+        tuned = s.get_state()
+    finally:
+        s.close()
+    s = _solver("kh2d", precision)
+    try:
+        s.select_candidate(chosen)
+        s.advance(1e9, 0, STEPS)
+        assert np.array_equal(s.get_state(), tuned)
+    finally:
+        s.close()
+
+
 def _ensemble(precision, sizes, cand):
     b = lib.Batch("euler2", "hll3", "weno2", "rungekutta3", "periodic", 256 << 20, len(sizes), cfl=0.4,
                   precision=precision)
