@@ -466,28 +466,25 @@ int gbfv_state_device(gbfv_solver* s, void** dev) {
     return GBFV_OK;
 }
 
-// Primitive -> conserved for interior cells, then the ghost fill: the values
-// Simulator::setInitialValue produces (conversion CPUCellComputer::
-// computeFromPrimitive with Euler::computeConserved, Euler.hpp:236-245).
-int gbfv_set_primitive(gbfv_solver* s, const double* prim) {
-    if (!s || !prim) return fail(GBFV_ERR_ARGUMENT, "null argument");
-    const Grid& G = s->G;
+// Primitive -> conserved for the interior cells of a padded array (ghosts
+// untouched): CPUCellComputer::computeFromPrimitive with
+// Euler::computeConserved (Euler.hpp:236-245) in the reference's operand
+// order; Burgers copies u.
+static void prim_to_cons(int eq, double gamma, const Grid& G, const double* prim, double* cons) {
     const long long total = G.total;
     const long long cells = (long long)G.n[0] * G.n[1] * G.n[2];
-    std::vector<double> cons((size_t)s->nvar * total, 0.0);
-    const int nsd = s->eq == EQ_BURGERS ? 1 : s->eq;
-    const double gamma = s->gamma;
+    const int nsd = eq == EQ_BURGERS ? 1 : eq;
     for (int z = 0; z < G.n[2]; ++z)
         for (int y = 0; y < G.n[1]; ++y)
             for (int x = 0; x < G.n[0]; ++x) {
                 const long long ic = ((long long)z * G.n[1] + y) * G.n[0] + x;
                 const long long ip = ((long long)(z + G.g[2]) * G.t[1] + (y + G.g[1])) * G.t[0] + (x + G.g[0]);
-                if (s->eq == EQ_BURGERS) {
+                if (eq == EQ_BURGERS) {
                     cons[ip] = prim[ic];
                     continue;
                 }
                 const double rho = prim[ic];
-                double u[3];
+                double u[3] = {0.0, 0.0, 0.0};
                 for (int k = 0; k < nsd; ++k) u[k] = prim[(1 + k) * cells + ic];
                 const double p = prim[(1 + nsd) * cells + ic];
                 double dot = u[0] * u[0];
@@ -496,6 +493,15 @@ int gbfv_set_primitive(gbfv_solver* s, const double* prim) {
                 for (int k = 0; k < nsd; ++k) cons[(1 + k) * total + ip] = u[k] * rho;
                 cons[(1 + nsd) * total + ip] = p / (gamma - 1) + 0.5 * rho * dot;
             }
+}
+
+// Primitive -> conserved for interior cells, then the ghost fill: the values
+// Simulator::setInitialValue produces (conversion CPUCellComputer::
+// computeFromPrimitive with Euler::computeConserved, Euler.hpp:236-245).
+int gbfv_set_primitive(gbfv_solver* s, const double* prim) {
+    if (!s || !prim) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    std::vector<double> cons((size_t)s->nvar * s->G.total, 0.0);
+    prim_to_cons(s->eq, s->gamma, s->G, prim, cons.data());
     int r = upload(s, cons.data());
     if (r) return r;
     r = launch_boundary(s, s->U);
@@ -1124,29 +1130,7 @@ int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* 
 // Host primitive -> conserved conversion into a padded array (interior cells;
 // ghosts left at zero), as gbfv_set_primitive does.
 int gbfv_internal_prim_to_cons(const GbfvPlan& p, const double* prim, double* cons) {
-    const Grid& G = p.G;
-    const long long total = G.total;
-    const long long cells = (long long)G.n[0] * G.n[1] * G.n[2];
-    const int nsd = p.eq == EQ_BURGERS ? 1 : p.eq;
-    for (int z = 0; z < G.n[2]; ++z)
-        for (int y = 0; y < G.n[1]; ++y)
-            for (int x = 0; x < G.n[0]; ++x) {
-                const long long ic = ((long long)z * G.n[1] + y) * G.n[0] + x;
-                const long long ip = ((long long)(z + G.g[2]) * G.t[1] + (y + G.g[1])) * G.t[0] + (x + G.g[0]);
-                if (p.eq == EQ_BURGERS) {
-                    cons[ip] = prim[ic];
-                    continue;
-                }
-                const double rho = prim[ic];
-                double u[3];
-                for (int k = 0; k < nsd; ++k) u[k] = prim[(1 + k) * cells + ic];
-                const double pr = prim[(1 + nsd) * cells + ic];
-                double dot = u[0] * u[0];
-                for (int k = 1; k < nsd; ++k) dot = dot + u[k] * u[k];
-                cons[ip] = rho;
-                for (int k = 0; k < nsd; ++k) cons[(1 + k) * total + ip] = u[k] * rho;
-                cons[(1 + nsd) * total + ip] = pr / (p.gamma - 1) + 0.5 * rho * dot;
-            }
+    prim_to_cons(p.eq, p.gamma, p.G, prim, cons);
     return GBFV_OK;
 }
 

@@ -101,7 +101,7 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
     std::vector<double> prim;
     for (;;) {
         // admission: arrived requests of this kind, in arrival order, first fit
-        bool any_pending = false, any_running = false;
+        bool any_pending = false;
         double next_arrival = 1e300;
         {
             std::vector<int> order;
@@ -110,7 +110,6 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
                 for (auto& q : S->reqs) {
                     if (q.r.kind != kind) continue;
                     if (q.state == 0) order.push_back(q.id);
-                    if (q.state == 1) any_running = true;
                 }
             }
             std::sort(order.begin(), order.end(), [&](int a, int b) {
@@ -164,7 +163,6 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
                 q.state = 1;
                 q.slot = slot;
                 q.admit_s = since(S->start);
-                any_running = true;
             }
         }
         int active = 0;
