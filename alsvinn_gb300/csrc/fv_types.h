@@ -32,6 +32,37 @@ struct StepState {
     int just_saved;                 // ensemble: save index reached in the step just finished (-1: none)
 };
 
+// The step's dt (Integrator::computeTimestep, alsfvm/src/integrator/
+// Integrator.cpp:20-46: cfl over the sum of wave speed / cell length over the
+// active directions) clamped to the next save time of up to two fixed
+// intervals (FixedIntervalWriter::adjustTimestep, alsfvm/src/io/
+// FixedIntervalWriter.cpp:45-53; FixedIntervalStatistics::adjustTimestep,
+// alsuq/src/stats/FixedIntervalStatistics.cpp:33-41); stores dt and dt / dx.x.
+__device__ __forceinline__ void set_step_dt(StepState& S, int dim, const double* cell_lengths, double cfl,
+                                            double interval, double interval2) {
+    double ws[3];
+    for (int d = 0; d < 3; ++d) ws[d] = d < dim ? __longlong_as_double((long long)S.ws_bits[d]) : 0.0;
+    double waveSpeedTotal = 0;
+    for (int d = 0; d < 3; ++d) {
+        if (cell_lengths[d] == 0) continue;
+        waveSpeedTotal += ws[d] / cell_lengths[d];
+    }
+    double dt = cfl / waveSpeedTotal;
+    if (interval > 0) {
+        const double nextSaveTime = (double)S.number_saved * interval + 0.0;
+        const double lim = nextSaveTime - S.t;
+        dt = lim < dt ? lim : dt;
+    }
+    if (interval2 > 0) {
+        const double nextSaveTime = (double)S.number_saved2 * interval2;
+        const double lim = nextSaveTime - S.t;
+        dt = lim < dt ? lim : dt;
+    }
+    S.dt = dt;
+    S.scale = dt / cell_lengths[0];
+    S.scale_f = (float)S.scale;
+}
+
 struct StepParams {
     double cfl;
     double cell_lengths[3];

@@ -62,28 +62,7 @@ const StageCandidate* candidates(int var, int eq, int fl, int rc, int dim, int* 
 // FixedIntervalWriter::adjustTimestep, alsfvm/src/io/FixedIntervalWriter.cpp:45-53).
 __global__ void dt_kernel(StepState* st, StepParams P) {
     if (st->done) return;
-    double ws[3];
-    for (int d = 0; d < 3; ++d) ws[d] = d < P.dim ? __longlong_as_double((long long)st->ws_bits[d]) : 0.0;
-    double waveSpeedTotal = 0;
-    for (int d = 0; d < 3; ++d) {
-        if (P.cell_lengths[d] == 0) continue;
-        waveSpeedTotal += ws[d] / P.cell_lengths[d];
-    }
-    double dt = P.cfl / waveSpeedTotal;
-    if (P.time_interval > 0) {
-        const double nextSaveTime = (double)st->number_saved * P.time_interval + 0.0;
-        const double lim = nextSaveTime - st->t;
-        dt = lim < dt ? lim : dt;
-    }
-    // FixedIntervalStatistics::adjustTimestep (alsuq/src/stats/FixedIntervalStatistics.cpp:33-41)
-    if (P.time_interval2 > 0) {
-        const double nextSaveTime = (double)st->number_saved2 * P.time_interval2;
-        const double lim = nextSaveTime - st->t;
-        dt = lim < dt ? lim : dt;
-    }
-    st->dt = dt;
-    st->scale = dt / P.cell_lengths[0];
-    st->scale_f = (float)st->scale;
+    set_step_dt(*st, P.dim, P.cell_lengths, P.cfl, P.time_interval, P.time_interval2);
 }
 
 // t += dt (TimestepInformation::incrementTime), the writer's save counter, and

@@ -50,24 +50,7 @@ struct GroupAcc {
 __global__ void batch_dt_kernel(StepState* st, const MemberParam* mp, int M, double cfl) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= M || !mp[s].active || st[s].done) return;
-    StepState& S = st[s];
-    const MemberParam& P = mp[s];
-    double ws[3];
-    for (int d = 0; d < 3; ++d) ws[d] = d < P.dim ? __longlong_as_double((long long)S.ws_bits[d]) : 0.0;
-    double waveSpeedTotal = 0;
-    for (int d = 0; d < 3; ++d) {
-        if (P.cell_lengths[d] == 0) continue;
-        waveSpeedTotal += ws[d] / P.cell_lengths[d];
-    }
-    double dt = cfl / waveSpeedTotal;
-    if (P.time_interval > 0) {
-        const double nextSaveTime = (double)S.number_saved * P.time_interval + 0.0;
-        const double lim = nextSaveTime - S.t;
-        dt = lim < dt ? lim : dt;
-    }
-    S.dt = dt;
-    S.scale = dt / P.cell_lengths[0];
-    S.scale_f = (float)S.scale;
+    set_step_dt(st[s], mp[s].dim, mp[s].cell_lengths, cfl, mp[s].time_interval, 0.0);
 }
 
 __global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M, int alternate) {
