@@ -77,8 +77,10 @@ struct StepParams {
 // dimension and arithmetic variant (0 fp64, 1 fp64 exact, 2 fp32, 3 fp64 state
 // with double-float arithmetic). A tile of T cells per direction needs
 // T_d + 2 reconstructions and T_d + 1 face fluxes along each direction d
-// (times the other extents). The FP64 and FP32 kernels use 32 x 8 tiles, one
-// thread per cell; the double-float kernel, bound by barrier waits, uses a
+// (times the other extents). These are the default configurations (candidate
+// 0; the autotuner's other candidates are registered in fv_variant.cu): the
+// FP64 and FP32 kernels use 32 x 8 tiles, one thread per cell; the
+// double-float kernel, bound by barrier waits, uses a
 // 16 x 12 tile on 256 threads, which keeps each reconstruction and flux phase
 // within one pass of the threads (a second, nearly empty pass leaves most
 // warps waiting at the next barrier). Threads past the tile's cells join the
