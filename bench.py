@@ -81,7 +81,9 @@ def profile_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples every 200 ms over the timed region:
+    sampling is running before the region starts and takes one more sample
+    after it ends, so even a region shorter than the interval is bracketed."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -101,10 +103,28 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # sampling running before the timed region starts, and one more
+        # sample after it ends: a short region is bracketed by samples
+        self._wait_samples(1, 3.0)
+        self.before = self._samples()
         return self
+
+    def _samples(self):
+        try:
+            with open(self.path) as f:
+                return sum(1 for line in f if line.strip())
+        except OSError:
+            return 0
+
+    def _wait_samples(self, n, timeout):
+        t0 = time.time()
+        while (self.proc and self.proc.poll() is None and self._samples() < n
+               and time.time() - t0 < timeout):
+            time.sleep(0.02)
 
     def __exit__(self, *exc):
         if self.proc:
+            self._wait_samples(self.before + 1, 1.0)
             self.proc.terminate()
             try:
                 self.proc.wait(5)
