@@ -59,6 +59,7 @@ def _units():
     units.append(("gbfv_structure.cu", "gbfv_structure.o", []))
     units.append(("gbfv_functional.cu", "gbfv_functional.o", ["-fmad=false"]))
     units.append(("gbfv_noalloc.cu", "gbfv_noalloc.o", []))
+    units.append(("gbfv_memory.cu", "gbfv_memory.o", ["-fmad=false"]))
     units.append(("gbfv_batch.cu", "gbfv_batch.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_init.cpp", "gbfv_init.o", ["-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_serve.cpp", "gbfv_serve.o", []))
@@ -115,12 +116,19 @@ def build_oracle():
 
 
 def build_reference_oracle(ref_root=None):
-    """Compiles the reference's CPU path from its sources, where they exist."""
-    ref_root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(ref_root, "alsfvm", "src")):
+    """Compiles the reference's CPU path from its sources, where they exist:
+    REF_ROOT in the environment, else the location the recipe
+    (oracle/refbuild/Makefile) names."""
+    refbuild = os.path.join(ORACLE_DIR, "refbuild")
+    ref_root = ref_root or os.environ.get("REF_ROOT")
+    if not ref_root:
+        try:
+            ref_root = _run(["make", "-s", "--no-print-directory", "-C", refbuild, "print-ref"]).strip()
+        except (OSError, RuntimeError):
+            return None
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "alsfvm", "src")):
         return None
-    _run(["make", "-s", "-C", os.path.join(ORACLE_DIR, "refbuild"), "-j%d" % (os.cpu_count() or 4),
-          "REF=" + ref_root])
+    _run(["make", "-s", "-C", refbuild, "-j%d" % (os.cpu_count() or 4), "REF=" + ref_root])
     return os.path.join(ORACLE_DIR, "_ref", "libalsref.so")
 
 

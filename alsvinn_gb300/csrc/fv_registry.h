@@ -28,6 +28,9 @@ typedef int (*ApplyLauncher)(const StageArgs& a, cudaStream_t s);
 
 typedef int (*ReconLauncher)(const ReconArgs& a, cudaStream_t s);
 
+// The operator on a region of cells (a.rlo, a.rhi, a.vin, a.vout; MODE_L).
+typedef int (*RegionLauncher)(const StageArgs& a, cudaStream_t s);
+
 typedef int (*CheckLauncher)(const CheckArgs& a, cudaStream_t s);
 
 // Persistent ensemble stage launch: grid = ctas (0: one wave of resident CTAs).
@@ -54,6 +57,7 @@ struct Registry {
     // [variant][equation][flux][recon][dim-1][candidate]
     StageCandidate cand[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3][kMaxCandidates];
     int ncand[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
+    RegionLauncher region[NUM_VARIANTS][NUM_EQ][NUM_FLUX][NUM_RECON][3];
     ApplyLauncher apply[NUM_VARIANTS][NUM_EQ];
     ReconLauncher recon[NUM_VARIANTS][NUM_EQ][NUM_RECON];
     CheckLauncher check[NUM_VARIANTS][NUM_EQ];

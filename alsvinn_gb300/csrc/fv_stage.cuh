@@ -162,9 +162,12 @@ template <int NT, int NTH> struct CellsPerThread {
 
 
 // One direction D of the tile: reconstruct, face fluxes, accumulate into acc.
+// A face counts towards the wave-speed maximum when its cells along D lie
+// in [0, hi[D]] (faces 0 .. n of the grid, or of a region's cells) and the
+// other coordinates below hi.
 template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, int D>
 __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc, int tid,
-                                               const int* org, const Grid& G, R gamma, R& wsmax) {
+                                               const int* org, const int* hi, R gamma, R& wsmax) {
     using Ph = Physics<R, EQ, FLUX>;
     constexpr int NV = Ph::NV;
     using SL = SmemLayout<R, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
@@ -247,10 +250,10 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         if (D == 0) { c[1] = p; c[2] = q; }
         else if (D == 1) { c[0] = p; c[2] = q; }
         else { c[0] = p; c[1] = q; }
-        bool valid = org[D] + c[D] <= G.n[D];
+        bool valid = org[D] + c[D] <= hi[D];
 #pragma unroll
         for (int d = 0; d < 3; ++d)
-            if (d != D) valid = valid && (org[d] + c[d] < G.n[d]);
+            if (d != D) valid = valid && (org[d] + c[d] < hi[d]);
         if (valid) wsmax = fmax_(wsmax, w);
     }
     __syncthreads();
@@ -291,7 +294,8 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
 // and runs in R.
 // Phase 1 of a tile: the tile plus its halo of g cells per active dimension
 // into su, the stage-1 modes forming U1 = L0 c + U0 on the way.
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+// REGION: the region kernel's load, one input array per variable (A.vin).
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R, bool REGION = false>
 __device__ __forceinline__ void stage_tile_load(const StageArgs& A, const int* org, C* su) {
     constexpr int NV = Physics<C, EQ, FLUX>::NV;
     using SL = SmemLayout<C, NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
@@ -308,14 +312,19 @@ __device__ __forceinline__ void stage_tile_load(const StageArgs& A, const int* o
         const int px = org[0] + hx, py = org[1] + hy, pz = org[2] + hz;
         if (px < Gd.t[0] && py < Gd.t[1] && pz < Gd.t[2]) {
             const long long gi = gidx(Gd, px, py, pz);
+            if constexpr (REGION) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                // U1 = L0 * c + U0 (the reference's *= then +=), formed in R:
-                // the ENO stencil choices compare differences of these values
-                const R v = (mode == MODE_RK3_S1 || mode == MODE_RK2_S1)
-                                ? madd(l0[k * total + gi], scale, in[k * total + gi])
-                                : in[k * total + gi];
-                su[k * SL::HALO + w] = C(v);
+                for (int k = 0; k < NV; ++k) su[k * SL::HALO + w] = C(reinterpret_cast<const R*>(A.vin[k])[gi]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    // U1 = L0 * c + U0 (the reference's *= then +=), formed in R:
+                    // the ENO stencil choices compare differences of these values
+                    const R v = (mode == MODE_RK3_S1 || mode == MODE_RK2_S1)
+                                    ? madd(l0[k * total + gi], scale, in[k * total + gi])
+                                    : in[k * total + gi];
+                    su[k * SL::HALO + w] = C(v);
+                }
             }
         } else {
 #pragma unroll
@@ -391,7 +400,10 @@ __device__ __forceinline__ void stage_tile_prefetch_finish(const StageArgs& A, R
 
 // Phases 2-4 of a tile whose halo is in su; work holds the per-direction
 // line buffers (reconstructed face values and face fluxes).
-template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+// REGION: the region kernel (MODE_L over the cells [A.rlo, A.rhi), faces
+// and stores limited to them, one output array per variable, no ghost
+// images written).
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R, bool REGION = false>
 __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int* org, const C* su, C* work,
                                                    C* wred) {
     using Ph = Physics<C, EQ, FLUX>;
@@ -414,6 +426,7 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     const long long total = Gd.total;
     const int mode = A.mode;
     const R scale = uniform_value<R>(A.st->scale, A.st->scale_f);
+    const int* hi = REGION ? A.rhi : Gd.n;  // cells and faces at or past hi are not this launch's
 
     // The combination at the end reads U0 of the thread's cells from global
     // memory (and, with per-thread staging of another type, the stage input):
@@ -442,11 +455,11 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     // conversion per thread gives the same double as converting every face)
     C wsd[3] = {C(0), C(0), C(0)};
     const C gamma = uniform_value<C>(A.gamma, A.gamma_f);
-    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[0]);
+    tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 0>(su, rl, rr, acc, tid, org, hi, gamma, wsd[0]);
     if constexpr (DIM > 1)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[1]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 1>(su, rl, rr, acc, tid, org, hi, gamma, wsd[1]);
     if constexpr (DIM > 2)
-        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 2>(su, rl, rr, acc, tid, org, Gd, gamma, wsd[2]);
+        tile_direction<C, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, 2>(su, rl, rr, acc, tid, org, hi, gamma, wsd[2]);
 
     // 3. wave speeds (stage 0 only): warp max, CTA max, one atomic per direction
     if (mode == MODE_L) {
@@ -475,9 +488,13 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     if (cell >= NT) continue;
     const int cx = cell % TX, cy = (cell / TX) % TY, cz = cell / (TX * TY);
     const int ix = org[0] + cx, iy = org[1] + cy, iz = org[2] + cz;
-    if (ix >= Gd.n[0] || iy >= Gd.n[1] || iz >= Gd.n[2]) continue;
+    if (ix >= hi[0] || iy >= hi[1] || iz >= hi[2]) continue;
     const int sidx = ((cz + SL::GZ) * SL::HY + (cy + SL::GY)) * SL::HX + (cx + SL::GX);
     const long long own = gidx(Gd, ix + Gd.g[0], iy + Gd.g[1], iz + Gd.g[2]);
+    if constexpr (REGION) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) reinterpret_cast<R*>(A.vout[k])[own] = (R)acc[j * NV + k];
+    } else {
     R res[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -512,6 +529,7 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
         if (atomicCAS(&A.st->status, 0, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
+    }
     }
 }
 
@@ -579,6 +597,25 @@ __global__ void __launch_bounds__(NTH, MINB) stage_kernel(StageArgs A) {
     if (A.st->done) return;
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
     stage_tile<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C>(A, org, align_smem(smem_raw), wred);
+}
+
+// The operator on a region of the grid (NumericalFlux::computeFlux with start
+// / end, alsfvm/src/numflux/NumericalFluxCPU.cpp:167-221): the default tile
+// with per-thread loads, tiles starting at the region's first cell, MODE_L
+// into A.vout; the wave speeds of the region's faces into A.st.
+template <class R, int EQ, int FLUX, int RC, int DIM, int TX, int TY, int TZ, int NTH, class C = R>
+__global__ void __launch_bounds__(NTH, 1) region_kernel(StageArgs A) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned char wred_raw[(NTH / 32) * 3 * sizeof(C)];
+    C* wred = reinterpret_cast<C*>(wred_raw);
+    const int org[3] = {A.rlo[0] + (int)blockIdx.x * TX, A.rlo[1] + (int)blockIdx.y * TY,
+                        A.rlo[2] + (int)blockIdx.z * TZ};
+    using SL = SmemLayout<C, Physics<C, EQ, FLUX>::NV, ReconTraits<RC>::ghosts, DIM, TX, TY, TZ>;
+    unsigned char* base = align_smem(smem_raw);
+    C* su = reinterpret_cast<C*>(base);
+    stage_tile_load<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C, true>(A, org, su);
+    stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, C, true>(A, org, su,
+                                                                       reinterpret_cast<C*>(base + SL::halo_bytes), wred);
 }
 
 // The single-grid stage with the tile + halo staged by TMA (storage type =

@@ -194,6 +194,13 @@ struct StageArgs {
     int mode;
     int periodic;
     int check;        // run the constraint check on the output
+    // region calls of the operator (region_kernel, MODE_L only): the cells
+    // [rlo, rhi) in interior coordinates, read from and written to one
+    // array per variable
+    int rlo[3];
+    int rhi[3];
+    const void* vin[5];
+    void* vout[5];
 };
 
 // Reconstruction of one direction over the reference's cell range
@@ -206,6 +213,8 @@ struct ReconArgs {
     Grid G;
     int dir;
     double gamma;  // for reconstructions in primitive variables
+    int start[3];  // offsets of the cell range's lower / upper ends (the
+    int end[3];    // reference's start / end; 0: the whole range)
 };
 
 // Constraint check over every padded cell (ghosts included, as the reference

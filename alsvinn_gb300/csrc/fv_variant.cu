@@ -87,6 +87,22 @@ struct Cand {
         return (int)cudaGetLastError();
     }
 
+    // the region kernel (operator on part of the grid): per-thread loads
+    static int launch_region(const StageArgs& a, cudaStream_t s) {
+        static_assert(!TMA, "the region kernel stages its halo with per-thread loads");
+        const dim3 grid((a.rhi[0] - a.rlo[0] + TX - 1) / TX, (a.rhi[1] - a.rlo[1] + TY - 1) / TY,
+                        (a.rhi[2] - a.rlo[2] + TZ - 1) / TZ);
+        auto k = region_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute>;
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SL::bytes);
+            if (e != cudaSuccess) return (int)e;
+            configured = 1;
+        }
+        k<<<grid, NTH, SL::bytes, s>>>(a);
+        return (int)cudaGetLastError();
+    }
+
     static int launch_batch(const BatchArgs& a, int ctas, cudaStream_t s) {
         auto k = batch_stage_kernel<Real, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, Compute, TMA>;
         static int resident = 0;
@@ -141,10 +157,11 @@ __global__ void recon_kernel(ReconArgs A) {
     const int d = A.dir;
     int lo[3], hi[3];
     for (int k = 0; k < 3; ++k) {
-        // "none" copies every cell (NoReconstruction.cpp:52-64)
-        lo[k] = RC == RC_NONE ? 0 : G.g[k] - (k == d);
-        hi[k] = RC == RC_NONE ? G.t[k] : G.t[k] - G.g[k] + (k == d);
+        // "none" copies every cell and ignores the range (NoReconstruction.cpp:52-64)
+        lo[k] = RC == RC_NONE ? 0 : G.g[k] - (k == d) + A.start[k];
+        hi[k] = RC == RC_NONE ? G.t[k] : G.t[k] - G.g[k] + (k == d) + A.end[k];
     }
+    if (hi[0] <= lo[0] || hi[1] <= lo[1] || hi[2] <= lo[2]) return;
     const long long ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ex * ey * ez) return;
@@ -168,8 +185,11 @@ template <int EQ, int RC>
 static int launch_recon(const ReconArgs& a, cudaStream_t s) {
     constexpr int NV = EQ == 0 ? 1 : EQ + 2;
     long long cnt = 1;
-    for (int k = 0; k < 3; ++k)
-        cnt *= RC == RC_NONE ? a.G.t[k] : (a.G.t[k] - 2 * a.G.g[k] + 2 * (k == a.dir));
+    for (int k = 0; k < 3; ++k) {
+        const long long e = RC == RC_NONE ? a.G.t[k] : (a.G.t[k] - 2 * a.G.g[k] + 2 * (k == a.dir) + a.end[k] - a.start[k]);
+        cnt *= e > 0 ? e : 0;
+    }
+    if (cnt == 0) return (int)cudaGetLastError();
     const int bs = 256;
     recon_kernel<NV, RC><<<(unsigned)((cnt + bs - 1) / bs), bs, 0, s>>>(a);
     return (int)cudaGetLastError();
@@ -201,7 +221,9 @@ static int launch_check(const CheckArgs& a, cudaStream_t s) {
 template <int FLUX, int RC, int DIM>
 static void reg_one(Registry& R) {
     using TS = TileShape<DIM, FV_VARIANT>;
-    Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>::add(R, FLUX, RC);
+    using C0 = Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>;
+    C0::add(R, FLUX, RC);
+    R.region[FV_VARIANT][FV_EQ][FLUX][RC][DIM - 1] = &C0::launch_region;
 }
 
 // Every reconstruction for one flux in one dimension. The double-float

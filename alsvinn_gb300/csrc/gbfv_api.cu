@@ -235,6 +235,7 @@ struct gbfv_solver {
     CUtensorMap tm[3];
     bool tm_ok = false;
     std::vector<double> tune_ms;  // the autotuner's MODE_L time per candidate (-1: not eligible)
+    void* op_block = nullptr;     // scratch of the per-variable operator calls (allocated at first use)
     // kGraphSteps time steps captured as one CUDA graph, replayed for the
     // long stretches of an advance (valid for graph_params and graph_cand)
     cudaGraphExec_t step_graph = nullptr;
@@ -262,6 +263,7 @@ static void release(gbfv_solver* s) {
     if (s->st_host) cudaFreeHost(s->st_host);
     if (s->flag_host) cudaFreeHost(s->flag_host);
     if (s->staging) cudaFreeHost(s->staging);
+    if (s->op_block) cudaFree(s->op_block);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -491,6 +493,7 @@ int gbfv_set_primitive(gbfv_solver* s, const double* prim) {
 static StageArgs stage_args(gbfv_solver* s, StepState* st, const void* in, const void* u0, const void* l0,
                             void* out, int mode, int check) {
     StageArgs a;
+    std::memset(&a, 0, sizeof a);
     a.in = in;
     a.u0 = u0;
     a.l0 = l0;
@@ -930,6 +933,7 @@ int gbfv_reconstruct(gbfv_solver* s, int direction, const void* U, void* left, v
     if (!s || !U || !left || !right) return fail(GBFV_ERR_ARGUMENT, "null argument");
     if (direction < 0 || direction >= s->G.dim) return fail(GBFV_ERR_ARGUMENT, "bad direction");
     ReconArgs a;
+    std::memset(&a, 0, sizeof a);
     a.in = U;
     a.left = left;
     a.right = right;
@@ -963,6 +967,337 @@ int gbfv_obeys_constraints(gbfv_solver* s, const void* U, int* ok) {
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     *ok = *s->flag_host;
     return GBFV_OK;
+}
+
+// ------------------------------------- operator level, one array per variable
+
+// The arrays of one volume are a padded block (variable k at base + k * total
+// elements) or nvar separate allocations, as the reference's Volume holds
+// them (one Memory per variable).
+static bool contiguous(const gbfv_solver* s, const void* const* vars) {
+    const char* b = (const char*)vars[0];
+    for (int k = 1; k < s->nvar; ++k)
+        if ((const char*)vars[k] != b + (size_t)k * s->G.total * s->elem) return false;
+    return true;
+}
+
+static bool all_set(const gbfv_solver* s, const void* const* vars) {
+    if (!vars) return false;
+    for (int k = 0; k < s->nvar; ++k)
+        if (!vars[k]) return false;
+    return true;
+}
+
+// Scratch block of the solver for the gather / scatter of separate arrays
+// (allocated at its first use; the step buffers V and L serve as the others).
+static int op_scratch(gbfv_solver* s, void** p) {
+    if (!s->op_block) {
+        cudaError_t e = cudaMalloc(&s->op_block, state_bytes(s));
+        if (e != cudaSuccess) {
+            s->op_block = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? GBFV_ERR_MEMORY : GBFV_ERR_CUDA,
+                        std::string("operator scratch: ") + cudaGetErrorString(e));
+        }
+    }
+    *p = s->op_block;
+    return GBFV_OK;
+}
+
+static int gather(gbfv_solver* s, const void* const* vars, void* block, cudaStream_t q) {
+    const size_t bytes = (size_t)s->G.total * s->elem;
+    for (int k = 0; k < s->nvar; ++k)
+        CUDA_TRY(cudaMemcpyAsync((char*)block + k * bytes, vars[k], bytes, cudaMemcpyDeviceToDevice, q));
+    return GBFV_OK;
+}
+
+static int scatter(gbfv_solver* s, const void* block, void* const* vars, cudaStream_t q) {
+    const size_t bytes = (size_t)s->G.total * s->elem;
+    for (int k = 0; k < s->nvar; ++k)
+        CUDA_TRY(cudaMemcpyAsync(vars[k], (const char*)block + k * bytes, bytes, cudaMemcpyDeviceToDevice, q));
+    return GBFV_OK;
+}
+
+int gbfv_compute_flux_region(gbfv_solver* s, const void* const* state_vars, void* const* out_vars, double ws[3],
+                             const int start[3], const int end[3], void* stream) {
+    if (!s || !all_set(s, state_vars) || !all_set(s, (const void* const*)out_vars))
+        return fail(GBFV_ERR_ARGUMENT, "gbfv_compute_flux_region: null argument");
+    int lo[3], hi[3];
+    bool empty = false;
+    for (int d = 0; d < 3; ++d) {
+        const int a = start ? start[d] : 0, b = end ? end[d] : 0;
+        if (d >= s->G.dim) {
+            if (a != 0 || b != 0) return fail(GBFV_ERR_ARGUMENT, "start / end of an inactive dimension must be 0");
+            lo[d] = 0;
+            hi[d] = 1;
+            continue;
+        }
+        lo[d] = a;
+        hi[d] = s->G.n[d] + b;
+        if (lo[d] < 0 || hi[d] > s->G.n[d])
+            return fail(GBFV_ERR_ARGUMENT, "gbfv_compute_flux_region: the region leaves the interior");
+        if (hi[d] <= lo[d]) empty = true;
+    }
+    if (ws)
+        for (int d = 0; d < 3; ++d) ws[d] = 0.0;
+    if (empty) return GBFV_OK;
+    const RegionLauncher launch = registry().region[s->var][s->eq][s->fl][s->rc][s->G.dim - 1];
+    if (!launch) return fail(GBFV_ERR_UNSUPPORTED, "no region kernel for this scheme");
+    cudaStream_t q = stream ? (cudaStream_t)stream : s->stream;
+    CUDA_TRY(cudaMemsetAsync(s->st_op, 0, sizeof(StepState), q));
+    StageArgs a = stage_args(s, s->st_op, state_vars[0], nullptr, nullptr, out_vars[0], MODE_L, 0);
+    for (int d = 0; d < 3; ++d) {
+        a.rlo[d] = lo[d];
+        a.rhi[d] = hi[d];
+    }
+    for (int k = 0; k < s->nvar; ++k) {
+        a.vin[k] = state_vars[k];
+        a.vout[k] = out_vars[k];
+    }
+    LAUNCH_TRY(launch(a, q));
+    s->launches += 1;
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st_op, sizeof(StepState), cudaMemcpyDeviceToHost, q));
+    CUDA_TRY(cudaStreamSynchronize(q));
+    if (ws)
+        for (int d = 0; d < s->G.dim; ++d) {
+            unsigned long long b = s->st_host->ws_bits[d];
+            std::memcpy(&ws[d], &b, sizeof(double));
+        }
+    return GBFV_OK;
+}
+
+int gbfv_reconstruct_vars(gbfv_solver* s, int direction, const void* const* state_vars, void* const* left_vars,
+                          void* const* right_vars, const int start[3], const int end[3], void* stream) {
+    if (!s || !all_set(s, state_vars) || !all_set(s, (const void* const*)left_vars) ||
+        !all_set(s, (const void* const*)right_vars))
+        return fail(GBFV_ERR_ARGUMENT, "gbfv_reconstruct_vars: null argument");
+    if (direction < 0 || direction >= s->G.dim) return fail(GBFV_ERR_ARGUMENT, "bad direction");
+    cudaStream_t q = stream ? (cudaStream_t)stream : s->stream;
+    ReconArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.G = s->G;
+    a.dir = direction;
+    a.gamma = s->gamma;
+    for (int d = 0; d < 3; ++d) {
+        a.start[d] = d < s->G.dim && start ? start[d] : 0;
+        a.end[d] = d < s->G.dim && end ? end[d] : 0;
+    }
+    const bool c = contiguous(s, state_vars) && contiguous(s, (const void* const*)left_vars) &&
+                   contiguous(s, (const void* const*)right_vars);
+    void* blk = nullptr;
+    if (c) {
+        a.in = state_vars[0];
+        a.left = left_vars[0];
+        a.right = right_vars[0];
+    } else {
+        // separate arrays: through the solver's step buffers and scratch (the
+        // outputs are gathered too, so cells outside the range keep their values)
+        int r = op_scratch(s, &blk);
+        if (!r) r = gather(s, state_vars, blk, q);
+        if (!r) r = gather(s, (const void* const*)left_vars, s->V, q);
+        if (!r) r = gather(s, (const void* const*)right_vars, s->L, q);
+        if (r) return r;
+        a.in = blk;
+        a.left = s->V;
+        a.right = s->L;
+    }
+    LAUNCH_TRY(registry().recon[s->var][s->eq][s->rc](a, q));
+    s->launches += 1;
+    if (!c) {
+        int r = scatter(s, s->V, left_vars, q);
+        if (!r) r = scatter(s, s->L, right_vars, q);
+        if (r) return r;
+    }
+    CUDA_TRY(cudaStreamSynchronize(q));
+    return GBFV_OK;
+}
+
+int gbfv_apply_boundary_vars(gbfv_solver* s, void* const* vars, void* stream) {
+    if (!s || !all_set(s, (const void* const*)vars)) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    cudaStream_t q = stream ? (cudaStream_t)stream : s->stream;
+    const bool c = contiguous(s, (const void* const*)vars);
+    void* blk = vars[0];
+    if (!c) {
+        int r = op_scratch(s, &blk);
+        if (!r) r = gather(s, (const void* const*)vars, blk, q);
+        if (r) return r;
+    }
+    cudaStream_t own = s->stream;
+    s->stream = q;
+    int r = launch_boundary(s, blk);
+    s->stream = own;
+    if (r) return r;
+    s->launches += 1;
+    if (!c) {
+        r = scatter(s, blk, vars, q);
+        if (r) return r;
+    }
+    CUDA_TRY(cudaStreamSynchronize(q));
+    return GBFV_OK;
+}
+
+int gbfv_obeys_constraints_vars(gbfv_solver* s, const void* const* vars, int* ok, void* stream) {
+    if (!s || !ok || !all_set(s, vars)) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    cudaStream_t q = stream ? (cudaStream_t)stream : s->stream;
+    const void* blk = vars[0];
+    if (!contiguous(s, vars)) {
+        void* b = nullptr;
+        int r = op_scratch(s, &b);
+        if (!r) r = gather(s, vars, b, q);
+        if (r) return r;
+        blk = b;
+    }
+    *s->flag_host = 1;
+    CUDA_TRY(cudaMemcpyAsync(s->flag, s->flag_host, sizeof(int), cudaMemcpyHostToDevice, q));
+    CheckArgs a;
+    a.in = blk;
+    a.flag = s->flag;
+    a.G = s->G;
+    a.gamma = s->gamma;
+    LAUNCH_TRY(registry().check[s->var][s->eq](a, q));
+    s->launches += 1;
+    CUDA_TRY(cudaMemcpyAsync(s->flag_host, s->flag, sizeof(int), cudaMemcpyDeviceToHost, q));
+    CUDA_TRY(cudaStreamSynchronize(q));
+    *ok = *s->flag_host;
+    return GBFV_OK;
+}
+
+}  // extern "C"
+
+// Per-cell maps of CellComputer over every cell of a volume (ghosts
+// included), one array per variable, in the element type R of the solver.
+struct VarPtrs {
+    const void* in[5];
+    void* out[5];
+};
+
+// computeFromPrimitive: Euler::computeConserved (alsfvm/include/alsfvm/
+// equation/euler/Euler.hpp:236-245) in its operand order; Burgers copies u.
+template <class R>
+__global__ void cells_prim_to_cons_kernel(VarPtrs v, long long total, int eq, R gamma) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    if (eq == EQ_BURGERS) {
+        ((R*)v.out[0])[i] = ((const R*)v.in[0])[i];
+        return;
+    }
+    const int nsd = eq;
+    const R rho = ((const R*)v.in[0])[i];
+    R u[3];
+    for (int k = 0; k < nsd; ++k) u[k] = ((const R*)v.in[1 + k])[i];
+    const R p = ((const R*)v.in[1 + nsd])[i];
+    R dot = u[0] * u[0];
+    for (int k = 1; k < nsd; ++k) dot = dot + u[k] * u[k];
+    ((R*)v.out[0])[i] = rho;
+    for (int k = 0; k < nsd; ++k) ((R*)v.out[1 + k])[i] = u[k] * rho;
+    ((R*)v.out[1 + nsd])[i] = p / (gamma - R(1)) + R(0.5) * rho * dot;
+}
+
+// computeExtraVariables: Euler::computeExtra (Euler.hpp:204-211): p, then u.
+template <class R>
+__global__ void cells_extra_kernel(VarPtrs v, long long total, int nsd, R gamma) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const R rho = ((const R*)v.in[0])[i];
+    R m[3];
+    for (int k = 0; k < nsd; ++k) m[k] = ((const R*)v.in[1 + k])[i];
+    const R E = ((const R*)v.in[1 + nsd])[i];
+    R dot = m[0] * m[0];
+    for (int k = 1; k < nsd; ++k) dot = dot + m[k] * m[k];
+    const R ie = E - R(0.5) * dot / rho;
+    ((R*)v.out[0])[i] = (gamma - R(1)) * ie;
+    for (int k = 0; k < nsd; ++k) ((R*)v.out[1 + k])[i] = m[k] / rho;
+}
+
+// computeMaxWaveSpeed in direction d: the maximum over cells of
+// |u_d| + sqrt(gamma p / rho) (Euler.hpp:251-258) or |u| (Burgers); cells
+// whose value is not a number are passed over, as std::max passes them.
+template <class R>
+__global__ void cells_wave_speed_kernel(VarPtrs v, long long total, int eq, int d, R gamma,
+                                        unsigned long long* bits) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double w = 0.0;
+    if (i < total) {
+        if (eq == EQ_BURGERS) {
+            w = (double)fabs(((const R*)v.in[0])[i]);
+        } else {
+            const int nsd = eq;
+            const R rho = ((const R*)v.in[0])[i];
+            R m[3];
+            for (int k = 0; k < nsd; ++k) m[k] = ((const R*)v.in[1 + k])[i];
+            const R E = ((const R*)v.in[1 + nsd])[i];
+            R dot = m[0] * m[0];
+            for (int k = 1; k < nsd; ++k) dot = dot + m[k] * m[k];
+            const R p = (gamma - R(1)) * (E - R(0.5) * dot / rho);
+            const R ud = d < nsd ? m[d] / rho : R(0);
+            w = (double)(fabs(ud) + sqrt(gamma * p / rho));
+        }
+        if (!(w >= 0.0)) w = 0.0;  // NaN
+    }
+    for (int off = 16; off > 0; off >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, off));
+    if ((threadIdx.x & 31) == 0 && w > 0.0) atomicMax(bits, (unsigned long long)__double_as_longlong(w));
+}
+
+static int cells_launch(gbfv_solver* s, int which, const void* const* in, void* const* out, int d, double* result,
+                        void* stream) {
+    cudaStream_t q = stream ? (cudaStream_t)stream : s->stream;
+    VarPtrs v;
+    std::memset(&v, 0, sizeof v);
+    const int nsd = s->eq == EQ_BURGERS ? 1 : s->eq;
+    const int nin = which == 0 ? s->nvar : s->nvar;
+    const int nout = which == 0 ? s->nvar : (which == 1 ? (s->eq == EQ_BURGERS ? 0 : nsd + 1) : 0);
+    for (int k = 0; k < nin; ++k) {
+        if (!in[k]) return fail(GBFV_ERR_ARGUMENT, "null variable array");
+        v.in[k] = in[k];
+    }
+    for (int k = 0; k < nout; ++k) {
+        if (!out || !out[k]) return fail(GBFV_ERR_ARGUMENT, "null variable array");
+        v.out[k] = out[k];
+    }
+    const long long total = s->G.total;
+    const int bs = 256;
+    const unsigned nb = (unsigned)((total + bs - 1) / bs);
+    if (which == 0) {
+        if (s->elem == 8) cells_prim_to_cons_kernel<double><<<nb, bs, 0, q>>>(v, total, s->eq, s->gamma);
+        else cells_prim_to_cons_kernel<float><<<nb, bs, 0, q>>>(v, total, s->eq, (float)s->gamma);
+    } else if (which == 1) {
+        if (nout == 0) return GBFV_OK;  // Burgers has no extra variables
+        if (s->elem == 8) cells_extra_kernel<double><<<nb, bs, 0, q>>>(v, total, nsd, s->gamma);
+        else cells_extra_kernel<float><<<nb, bs, 0, q>>>(v, total, nsd, (float)s->gamma);
+    } else {
+        CUDA_TRY(cudaMemsetAsync(s->st_op, 0, sizeof(StepState), q));
+        unsigned long long* bits = &s->st_op->ws_bits[0];
+        if (s->elem == 8) cells_wave_speed_kernel<double><<<nb, bs, 0, q>>>(v, total, s->eq, d, s->gamma, bits);
+        else cells_wave_speed_kernel<float><<<nb, bs, 0, q>>>(v, total, s->eq, d, (float)s->gamma, bits);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st_op, sizeof(StepState), cudaMemcpyDeviceToHost, q));
+    }
+    CUDA_TRY(cudaGetLastError());
+    s->launches += 1;
+    CUDA_TRY(cudaStreamSynchronize(q));
+    if (which == 2 && result) {
+        unsigned long long b = s->st_host->ws_bits[0];
+        std::memcpy(result, &b, sizeof(double));
+    }
+    return GBFV_OK;
+}
+
+extern "C" {
+
+int gbfv_prim_to_cons_vars(gbfv_solver* s, const void* const* prim_vars, void* const* cons_vars, void* stream) {
+    if (!s || !prim_vars || !cons_vars) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    return cells_launch(s, 0, prim_vars, cons_vars, 0, nullptr, stream);
+}
+
+int gbfv_extra_variables_vars(gbfv_solver* s, const void* const* cons_vars, void* const* extra_vars, void* stream) {
+    if (!s || !cons_vars) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    return cells_launch(s, 1, cons_vars, extra_vars, 0, nullptr, stream);
+}
+
+int gbfv_max_wave_speed_vars(gbfv_solver* s, const void* const* cons_vars, int direction, double* speed,
+                             void* stream) {
+    if (!s || !cons_vars || !speed || direction < 0 || direction > 2)
+        return fail(GBFV_ERR_ARGUMENT, "gbfv_max_wave_speed_vars: bad arguments");
+    return cells_launch(s, 2, cons_vars, nullptr, direction, speed, stream);
 }
 
 // ------------------------------------------------------- generator

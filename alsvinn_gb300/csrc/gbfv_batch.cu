@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <string>
 #include <vector>
@@ -35,6 +36,7 @@ namespace {
 struct MemberParam {
     double cell_lengths[3];
     double time_interval;  // save-time clamp interval (0: none)
+    double end_time;       // the member's own end time (+inf: the advance's)
     int dim;
     int active;
 };
@@ -82,11 +84,12 @@ __global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, 
         S.done = 1;
         return;
     }
-    S.end_time = end_time;
+    const double end = mp[s].end_time < end_time ? mp[s].end_time : end_time;
+    S.end_time = end;
     S.step_limit = max_steps > 0 ? S.steps + max_steps : -1;
     S.ws_bits[0] = S.ws_bits[1] = S.ws_bits[2] = 0ull;
     S.just_done = 0;
-    S.done = (!(S.t < end_time) || S.status != 0) ? 1 : 0;
+    S.done = (!(S.t < end) || S.status != 0) ? 1 : 0;
 }
 
 // Welford order: members to fold in this step, in member order. With one
@@ -192,6 +195,7 @@ struct gbfv_batch {
         BatchMember m;
         MemberParam p;
         int group = -1;
+        bool own_end = false;  // end time and save clamp set by gbfv_batch_set_member_end
     };
     std::vector<Host> members;
     BatchMember* d_members = nullptr;
@@ -276,7 +280,8 @@ int rebuild_tiles(gbfv_batch* b) {
     for (size_t s = 0; s < b->members.size(); ++s) {
         const auto& h = b->members[s];
         if (!h.active) continue;
-        if (b->h_states[s].done && b->h_states[s].t >= b->h_states[s].end_time) continue;
+        const StepState& S = b->h_states[s];
+        if (S.done && (S.t >= S.end_time || S.status != 0)) continue;  // finished or stopped by a failure
         for (int z = 0; z < h.m.G.n[2]; z += tz)
             for (int y = 0; y < h.m.G.n[1]; y += ty)
                 for (int x = 0; x < h.m.G.n[0]; x += tx) tiles.push_back(make_int4((int)s, x, y, z));
@@ -679,6 +684,8 @@ int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const d
     h.m.G = p.G;
     for (int k = 0; k < 3; ++k) h.p.cell_lengths[k] = p.cell_lengths[k];
     h.p.time_interval = 0;
+    h.p.end_time = std::numeric_limits<double>::infinity();
+    h.own_end = false;
     h.p.dim = p.G.dim;
     h.p.active = 1;
 
@@ -758,7 +765,8 @@ int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int 
     const int M = b->max_members;
     // save-time clamp per member (FixedIntervalStatistics / FixedIntervalWriter)
     for (int s = 0; s < M; ++s)
-        if (b->members[s].active) b->members[s].p.time_interval = number_of_saves > 0 ? end_time / number_of_saves : 0;
+        if (b->members[s].active && !b->members[s].own_end)
+            b->members[s].p.time_interval = number_of_saves > 0 ? end_time / number_of_saves : 0;
     int r = upload_members(b);
     if (r) return r;
     const unsigned mb = (unsigned)((M + 127) / 128);
@@ -830,6 +838,28 @@ int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int 
                      b->h_states[s].t, b->h_states[s].failed_step);
             return bfail(GBFV_ERR_CONSTRAINT, msg);
         }
+    return GBFV_OK;
+}
+
+int gbfv_batch_set_member_end(gbfv_batch* b, int slot, double end_time, int number_of_saves) {
+    if (!b || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_set_member_end: bad slot");
+    if (!(end_time > 0) || number_of_saves < 0)
+        return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_set_member_end: bad end time or number of saves");
+    auto& h = b->members[slot];
+    h.own_end = true;
+    h.p.end_time = end_time;
+    h.p.time_interval = number_of_saves > 0 ? end_time / number_of_saves : 0;
+    return upload_members(b);
+}
+
+int gbfv_batch_member_status(gbfv_batch* b, int slot, int* status, int* failed_step) {
+    if (!b || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "bad slot");
+    BCUDA(cudaMemcpyAsync(&b->h_states[slot], b->d_states + slot, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    if (status) *status = b->h_states[slot].status;
+    if (failed_step) *failed_step = b->h_states[slot].failed_step;
     return GBFV_OK;
 }
 

@@ -11,8 +11,11 @@
 // yet); it then runs inside the ensemble's persistent stage launches next to
 // whatever is already in flight, with its own dt, until its end time. Its
 // final state is folded into the FP64 Welford statistics of its (kind, grid)
-// group and it leaves the ensemble, freeing its slot and memory. The reference
-// has no counterpart (alsuq runs a fixed sample list, alsuq/src/run/Runner.cpp:39-90).
+// group and it leaves the ensemble, freeing its slot and memory. Every request
+// has its own end time (the ensemble stops each member at its own end). A
+// request whose state breaks the constraint check stops alone: it is marked
+// failed and leaves, while the others run on. The reference has no
+// counterpart (alsuq runs a fixed sample list, alsuq/src/run/Runner.cpp:39-90).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -40,12 +43,13 @@ struct Req {
     double admit_s = 0, finish_s = 0;
     long long steps = 0;
     std::vector<double> final_state;
+    std::vector<double> initial;  // caller's primitive initial data (empty: the kind's family)
 };
 
 struct Kind {
     gbfv_batch* batch = nullptr;
     int dim = 1;
-    std::map<int, int> group_of_n;  // grid size -> statistics group
+    std::map<std::pair<int, double>, int> group_of;  // (grid size, end time) -> statistics group
 };
 
 }  // namespace
@@ -60,6 +64,7 @@ struct gbfv_server {
     std::string error;
     int error_code = 0;
     long long completed = 0;
+    long long failed = 0;
 };
 
 namespace {
@@ -78,7 +83,12 @@ int grid_of(const gbfv_request& r, int n3[3], double lo[3], double hi[3]) {
     return 0;
 }
 
-int initial_data(const gbfv_request& r, std::vector<double>& prim) {
+int initial_data(const Req& q, std::vector<double>& prim) {
+    const gbfv_request& r = q.r;
+    if (!q.initial.empty()) {
+        prim = q.initial;
+        return GBFV_OK;
+    }
     int n3[3];
     double lo[3], hi[3];
     grid_of(r, n3, lo, hi);
@@ -135,7 +145,7 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
                     any_pending = true;  // waits for memory / a slot
                     continue;
                 }
-                if (initial_data(q.r, prim)) {
+                if (initial_data(q, prim)) {
                     std::lock_guard<std::mutex> g(S->mu);
                     q.state = 3;
                     continue;
@@ -143,12 +153,18 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
                 int group;
                 {
                     std::lock_guard<std::mutex> g(S->mu);
-                    auto it = K.group_of_n.find(q.r.n);
-                    if (it == K.group_of_n.end()) it = K.group_of_n.emplace(q.r.n, (int)K.group_of_n.size()).first;
+                    const auto key = std::make_pair(q.r.n, q.r.end_time);
+                    auto it = K.group_of.find(key);
+                    if (it == K.group_of.end()) it = K.group_of.emplace(key, (int)K.group_of.size()).first;
                     group = it->second;
                 }
                 int slot = -1;
-                const int rc = gbfv_batch_add(K.batch, n3, lo, hi, prim.data(), group, &slot);
+                int rc = gbfv_batch_add(K.batch, n3, lo, hi, prim.data(), group, &slot);
+                // the request's own end time; one save clamp lands it exactly there
+                if (rc == GBFV_OK) {
+                    rc = gbfv_batch_set_member_end(K.batch, slot, q.r.end_time, 1);
+                    if (rc) gbfv_batch_remove(K.batch, slot);
+                }
                 std::lock_guard<std::mutex> g(S->mu);
                 if (rc == GBFV_ERR_MEMORY) {
                     any_pending = true;
@@ -180,7 +196,31 @@ void drive(gbfv_server* S, int kind, int steps_per_chunk) {
             for (auto& q : S->reqs)
                 if (q.r.kind == kind && q.state == 1) end_time = std::max(end_time, q.r.end_time);
         }
-        int rc = gbfv_batch_advance(K.batch, end_time, 1, steps_per_chunk);
+        int rc = gbfv_batch_advance(K.batch, end_time, 0, steps_per_chunk);
+        if (rc == GBFV_ERR_CONSTRAINT) {
+            // members whose state broke the constraints stopped alone: those
+            // requests fail and leave; the rest of the chunk ran as usual
+            std::vector<Req*> running;
+            {
+                std::lock_guard<std::mutex> g(S->mu);
+                for (auto& q : S->reqs)
+                    if (q.r.kind == kind && q.state == 1) running.push_back(&q);
+            }
+            const double t_fail = since(S->start);
+            for (Req* q : running) {
+                int status = 0, failed_step = 0;
+                if (gbfv_batch_member_status(K.batch, q->slot, &status, &failed_step) || status == 0) continue;
+                long long steps = 0;
+                gbfv_batch_member_time(K.batch, q->slot, nullptr, &steps);
+                gbfv_batch_remove(K.batch, q->slot);
+                std::lock_guard<std::mutex> g(S->mu);
+                q->state = 3;
+                q->finish_s = t_fail;
+                q->steps = steps;
+                S->failed += 1;
+            }
+            rc = GBFV_OK;
+        }
         if (rc) {
             std::lock_guard<std::mutex> g(S->mu);
             S->error = gbfv_last_error();
@@ -284,13 +324,15 @@ int gbfv_server_submit(gbfv_server* S, const gbfv_request* r, int* id) {
     if (!S || !r || !id) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "null argument");
     if (r->kind != GBFV_REQUEST_BURGERS && r->kind != GBFV_REQUEST_KELVIN_HELMHOLTZ)
         return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "unknown request kind");
-    if (r->n < 8 || r->end_time <= 0) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "bad request grid or end time");
+    if (r->n < 8 || !(r->end_time > 0)) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "bad request grid or end time");
     std::lock_guard<std::mutex> g(S->mu);
-    for (const auto& x : S->reqs)
-        if (x.r.kind == r->kind && x.r.end_time != r->end_time)
-            return gbfv_internal_fail(GBFV_ERR_UNSUPPORTED, "requests of one kind share one end time");
     Req q;
     q.r = *r;
+    if (r->initial_primitive) {
+        const size_t cells = r->kind == GBFV_REQUEST_BURGERS ? (size_t)r->n : (size_t)4 * r->n * r->n;
+        q.initial.assign(r->initial_primitive, r->initial_primitive + cells);
+    }
+    q.r.initial_primitive = nullptr;
     q.id = (int)S->reqs.size();
     S->reqs.push_back(q);
     *id = q.id;
@@ -334,11 +376,26 @@ int gbfv_server_final_state(gbfv_server* S, int id, double* state_host, long lon
     return GBFV_OK;
 }
 
+int gbfv_server_stats_at(gbfv_server* S, int kind, int n, double end_time, double* mean_host, double* var_host,
+                        long long* count) {
+    if (!S || (kind != 0 && kind != 1)) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "bad kind");
+    auto it = S->kinds[kind].group_of.find(std::make_pair(n, end_time));
+    if (it == S->kinds[kind].group_of.end())
+        return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "no request of this grid and end time");
+    return gbfv_batch_stats_result(S->kinds[kind].batch, it->second, mean_host, var_host, count);
+}
+
 int gbfv_server_stats(gbfv_server* S, int kind, int n, double* mean_host, double* var_host, long long* count) {
     if (!S || (kind != 0 && kind != 1)) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "bad kind");
-    auto it = S->kinds[kind].group_of_n.find(n);
-    if (it == S->kinds[kind].group_of_n.end()) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "no request of this grid");
-    return gbfv_batch_stats_result(S->kinds[kind].batch, it->second, mean_host, var_host, count);
+    const std::pair<int, double>* key = nullptr;
+    for (const auto& kv : S->kinds[kind].group_of) {
+        if (kv.first.first != n) continue;
+        if (key) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "requests of this grid have several end times: "
+                                                              "use gbfv_server_stats_at");
+        key = &kv.first;
+    }
+    if (!key) return gbfv_internal_fail(GBFV_ERR_ARGUMENT, "no request of this grid");
+    return gbfv_server_stats_at(S, kind, n, key->second, mean_host, var_host, count);
 }
 
 int gbfv_server_launches(gbfv_server* S, long long* launches) {

@@ -158,9 +158,87 @@ _SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "gbfv_init_burgers_sine": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_void_p]),
+    "gbfv_memory_op": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int,
+                                      ctypes.c_void_p]),
+    "gbfv_memory_op_scalar": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong,
+                                             ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_memory_make_zero": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_memory_add_linear_combination": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                                          ctypes.c_double, ctypes.c_void_p, ctypes.c_double,
+                                                          ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int,
+                                                          ctypes.c_void_p]),
+    "gbfv_memory_add_power": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_memory_subtract_power": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                                  ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p]),
+    "gbfv_memory_total_variation": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                                   ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "gbfv_compute_flux_region": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    "gbfv_reconstruct_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    "gbfv_apply_boundary_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_obeys_constraints_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                                   ctypes.c_void_p]),
+    "gbfv_prim_to_cons_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "gbfv_extra_variables_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_void_p]),
+    "gbfv_max_wave_speed_vars": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
 }
 
 NOALLOC_SCRATCH_BYTES = 32 << 20
+
+MEMORY_ADD, MEMORY_SUBTRACT, MEMORY_MULTIPLY, MEMORY_DIVIDE = 0, 1, 2, 3
+
+
+def _ptrs(ptrs):
+    """A C array of device pointers (one per variable)."""
+    return (ctypes.c_void_p * len(ptrs))(*[ctypes.c_void_p(int(p)) for p in ptrs])
+
+
+def memory_op(op, a_dev, b_dev, count, precision=0, stream=None):
+    """a op= b on device arrays (gbfv_memory_op)."""
+    _check(load().gbfv_memory_op(op, ctypes.c_void_p(a_dev), ctypes.c_void_p(b_dev), count, precision,
+                                 ctypes.c_void_p(stream)))
+
+
+def memory_op_scalar(op, a_dev, scalar, count, precision=0, stream=None):
+    _check(load().gbfv_memory_op_scalar(op, ctypes.c_void_p(a_dev), float(scalar), count, precision,
+                                        ctypes.c_void_p(stream)))
+
+
+def memory_make_zero(a_dev, count, precision=0, stream=None):
+    _check(load().gbfv_memory_make_zero(ctypes.c_void_p(a_dev), count, precision, ctypes.c_void_p(stream)))
+
+
+def memory_add_linear_combination(v1, a1, a2, v2, a3, v3, a4, v4, a5, v5, count, precision=0, stream=None):
+    vp = [ctypes.c_void_p(x) for x in (v1, v2, v3, v4, v5)]
+    _check(load().gbfv_memory_add_linear_combination(vp[0], a1, a2, vp[1], a3, vp[2], a4, vp[3], a5, vp[4], count,
+                                                     precision, ctypes.c_void_p(stream)))
+
+
+def memory_add_power(a_dev, b_dev, power, count, factor=1.0, precision=0, stream=None):
+    _check(load().gbfv_memory_add_power(ctypes.c_void_p(a_dev), ctypes.c_void_p(b_dev), power, factor, count,
+                                        precision, ctypes.c_void_p(stream)))
+
+
+def memory_subtract_power(a_dev, b_dev, power, count, precision=0, stream=None):
+    _check(load().gbfv_memory_subtract_power(ctypes.c_void_p(a_dev), ctypes.c_void_p(b_dev), power, count,
+                                             precision, ctypes.c_void_p(stream)))
+
+
+def memory_total_variation(a_dev, extents, p, direction, start, end, precision=0, stream=None):
+    r = ctypes.c_double()
+    _check(load().gbfv_memory_total_variation(ctypes.c_void_p(a_dev), _c_int3(*extents), int(p), int(direction),
+                                              _c_int3(*start), _c_int3(*end), precision, ctypes.byref(r),
+                                              ctypes.c_void_p(stream)))
+    return r.value
 
 
 def make_desc(equation, flux, reconstruction, integrator, boundary, n, lower, upper, gamma=1.4, cfl=0.475,
@@ -443,6 +521,40 @@ class Solver:
         _check(load().gbfv_obeys_constraints(self.h, ctypes.c_void_p(state_dev), ctypes.byref(ok)))
         return bool(ok.value)
 
+    # one device array per variable (a reference Volume's layout)
+    def compute_flux_region(self, state_vars, out_vars, start=(0, 0, 0), end=(0, 0, 0), stream=None):
+        ws = _c_double3()
+        _check(load().gbfv_compute_flux_region(self.h, _ptrs(state_vars), _ptrs(out_vars), ws, _c_int3(*start),
+                                               _c_int3(*end), ctypes.c_void_p(stream)))
+        return list(ws)
+
+    def reconstruct_vars(self, direction, state_vars, left_vars, right_vars, start=(0, 0, 0), end=(0, 0, 0),
+                         stream=None):
+        _check(load().gbfv_reconstruct_vars(self.h, direction, _ptrs(state_vars), _ptrs(left_vars),
+                                            _ptrs(right_vars), _c_int3(*start), _c_int3(*end),
+                                            ctypes.c_void_p(stream)))
+
+    def apply_boundary_vars(self, vars_, stream=None):
+        _check(load().gbfv_apply_boundary_vars(self.h, _ptrs(vars_), ctypes.c_void_p(stream)))
+
+    def obeys_constraints_vars(self, vars_, stream=None):
+        ok = ctypes.c_int()
+        _check(load().gbfv_obeys_constraints_vars(self.h, _ptrs(vars_), ctypes.byref(ok), ctypes.c_void_p(stream)))
+        return bool(ok.value)
+
+    def prim_to_cons_vars(self, prim_vars, cons_vars, stream=None):
+        _check(load().gbfv_prim_to_cons_vars(self.h, _ptrs(prim_vars), _ptrs(cons_vars), ctypes.c_void_p(stream)))
+
+    def extra_variables_vars(self, cons_vars, extra_vars, stream=None):
+        _check(load().gbfv_extra_variables_vars(self.h, _ptrs(cons_vars), _ptrs(extra_vars) if extra_vars else None,
+                                                ctypes.c_void_p(stream)))
+
+    def max_wave_speed_vars(self, cons_vars, direction, stream=None):
+        w = ctypes.c_double()
+        _check(load().gbfv_max_wave_speed_vars(self.h, _ptrs(cons_vars), direction, ctypes.byref(w),
+                                               ctypes.c_void_p(stream)))
+        return w.value
+
 
 class Stats:
     """Streaming FP64 mean / variance (gbfv_stats_*)."""
@@ -660,6 +772,17 @@ class Batch:
     def advance(self, end_time, number_of_saves=0, max_steps=0):
         _check(load().gbfv_batch_advance(self.h, end_time, number_of_saves, max_steps))
 
+    def set_member_end(self, slot, end_time, number_of_saves=1):
+        """The member's own end time (and save clamp)."""
+        _check(load().gbfv_batch_set_member_end(self.h, int(slot), float(end_time), int(number_of_saves)))
+
+    def member_status(self, slot):
+        """(status, failed step): 0 fine, 1 constraint check failed, 2 halo copy timed out."""
+        st = ctypes.c_int()
+        fs = ctypes.c_int()
+        _check(load().gbfv_batch_member_status(self.h, int(slot), ctypes.byref(st), ctypes.byref(fs)))
+        return st.value, fs.value
+
     def member_time(self, slot):
         t = ctypes.c_double()
         s = ctypes.c_longlong()
@@ -727,7 +850,7 @@ REQUEST_BURGERS, REQUEST_KELVIN_HELMHOLTZ = 0, 1
 class _Request(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("n", ctypes.c_int), ("end_time", ctypes.c_double),
                 ("phase", ctypes.c_double), ("sample", ctypes.c_int), ("arrival", ctypes.c_double),
-                ("keep", ctypes.c_int)]
+                ("keep", ctypes.c_int), ("initial_primitive", ctypes.c_void_p)]
 
 
 _SIGNATURES.update({
@@ -745,6 +868,11 @@ _SIGNATURES.update({
     "gbfv_server_final_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong]),
     "gbfv_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_server_stats_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "gbfv_batch_set_member_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+    "gbfv_batch_member_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int)]),
     "gbfv_server_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
 })
 
@@ -774,8 +902,14 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
-    def submit(self, kind, n, end_time, phase=0.0, sample=0, arrival=0.0, keep=False):
-        r = _Request(kind, n, end_time, phase, sample, arrival, 1 if keep else 0)
+    def submit(self, kind, n, end_time, phase=0.0, sample=0, arrival=0.0, keep=False, initial=None):
+        """Queues a request; `initial` (optional) is the caller's interior
+        primitive initial data (copied at submission)."""
+        buf = None
+        if initial is not None:
+            buf = np.ascontiguousarray(initial, dtype=np.float64)
+        r = _Request(kind, n, end_time, phase, sample, arrival, 1 if keep else 0,
+                     buf.ctypes.data if buf is not None else None)
         i = ctypes.c_int()
         _check(load().gbfv_server_submit(self.h, ctypes.byref(r), ctypes.byref(i)))
         return i.value
@@ -796,11 +930,15 @@ class Server:
         _check(load().gbfv_server_final_state(self.h, int(rid), _ptr(U), int(size)))
         return U
 
-    def stats(self, kind, n, size):
+    def stats(self, kind, n, size, end_time=None):
         m = np.zeros(size)
         v = np.zeros(size)
         c = ctypes.c_longlong()
-        _check(load().gbfv_server_stats(self.h, int(kind), int(n), _ptr(m), _ptr(v), ctypes.byref(c)))
+        if end_time is None:
+            _check(load().gbfv_server_stats(self.h, int(kind), int(n), _ptr(m), _ptr(v), ctypes.byref(c)))
+        else:
+            _check(load().gbfv_server_stats_at(self.h, int(kind), int(n), float(end_time), _ptr(m), _ptr(v),
+                                               ctypes.byref(c)))
         return m, v, c.value
 
     def launches(self):

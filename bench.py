@@ -45,8 +45,52 @@ FLUSH_BYTES = 512 << 20
 
 
 def kh_initial_primitives(n, sample=0):
+    """Product initial data (the library's C++ formula) for the GPU arm."""
     from alsvinn_gb300 import lib
     return lib.init_kelvin_helmholtz(n, sample=sample)
+
+
+def oracle_kh_primitives(n, sample=0):
+    """The same initial data for the CPU arms, without product code: the
+    oracle's generator draws and the Python formula of tests/workloads.py
+    (bit-identical to the library's, which the tests check)."""
+    import workloads
+    from oracle import fvoracle
+    return workloads.kh_prim(n, fvoracle.uniform(40, sample))
+
+
+def headline_config(precision):
+    """The workload description both arms print (the same dict in each)."""
+    return {"workload": WORKLOAD, "grid": [N, N], "domain": [[0, 1], [0, 1]], "boundary": "periodic",
+            "equation": "euler2", "gamma": 1.4, "reconstruction": "weno2", "flux": "hll3",
+            "integrator": "rungekutta3", "cfl": 0.4, "precision": precision,
+            "initial_data": "KH interface perturbation, generator sample = rank",
+            "l2": "state 33.8 MB < L2: flushed before every timed GPU step (512 MiB memset, outside the events)",
+            "parallelism": "independent replicas, one per rank"}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def time_oracle_kh(prim, steps, threads):
+    """The oracle's KH 1024^2 run of `steps` SSP-RK3 steps on `threads`
+    threads; returns (steps done, seconds of the step loop alone)."""
+    from oracle import fvoracle
+    fvoracle.set_threads(threads)
+    rc, _, _, done = fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0),
+                                  (1, 1, 0), 1.4, 0.4, 2.0, 0, steps, prim, 2, NVAR)
+    if rc != 0 or done != steps:
+        raise RuntimeError("oracle run failed")
+    return done, fvoracle.last_loop_seconds()
 
 
 def dist_env():
@@ -156,48 +200,45 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(steps):
-    """The oracle (reference CPU algorithm) on all host cores, bounded sample."""
-    from oracle import fvoracle
-    import workloads  # noqa: F401
-    prim = kh_initial_primitives(N)
+def cpu_baseline(steps, one_thread_steps=2):
+    """The oracle (the reference's CPU algorithm, restated) on every host core
+    over a bounded sample, plus a one-thread figure; step loop only."""
+    prim = oracle_kh_primitives(N)
     threads = os.cpu_count() or 1
-    fvoracle.set_threads(threads)
-    t0 = time.perf_counter()
-    rc, _, _, done = fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0),
-                                  (1, 1, 0), 1.4, 0.4, 2.0, 0, steps, prim, 2, NVAR)
-    dt = time.perf_counter() - t0
-    if rc != 0 or done != steps:
-        raise RuntimeError("oracle run failed")
-    return {"value": N * N * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": "KH 1024x1024 WENO2/HLL3/RK3 FP64, %d steps from t=0 on %d threads (incl. setup)"
-                      % (steps, threads)}
+    time_oracle_kh(prim, 1, threads)  # untimed: first touch, thread pool
+    done, sec = time_oracle_kh(prim, steps, threads)
+    done1, sec1 = time_oracle_kh(prim, one_thread_steps, 1)
+    return {"value": N * N * done / sec, "unit": METRIC, "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(), "one_thread_value": N * N * done1 / sec1,
+            "sample": "KH 1024x1024 WENO2/HLL3/SSP-RK3 FP64: %d steps on %d threads, %d steps on 1 thread, "
+                      "step loop only (initial data and allocation excluded)" % (done, threads, done1)}
 
 
 def run_reference(args):
+    """The reference's CPU path for the headline workload: the oracle port
+    (bit-identical to the reference's own CPU build wherever both ran) on all
+    host threads. Initial data come from the oracle's generator and the
+    Python formula; nothing of the GPU library is loaded."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from oracle import fvoracle
-    prim = kh_initial_primitives(N)
+    prim = oracle_kh_primitives(N)
     threads = os.cpu_count() or 1
-    fvoracle.set_threads(threads)
-    # warm-up steps are run untimed; then K single-step samples are timed
-    fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0), (1, 1, 0), 1.4,
-                 0.4, 2.0, 0, max(args.warmup, 1), prim, 2, NVAR)
-    t0 = time.perf_counter()
-    rc, _, _, done = fvoracle.run("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0),
-                                  (1, 1, 0), 1.4, 0.4, 2.0, 0, args.steps, prim, 2, NVAR)
-    dt = time.perf_counter() - t0
-    value = N * N * done / dt
+    time_oracle_kh(prim, max(args.warmup, 1), threads)  # warm-up run, untimed
+    done, sec = time_oracle_kh(prim, args.steps, threads)
+    done1, sec1 = time_oracle_kh(prim, 2, 1)
+    value = N * N * done / sec
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / max(done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded KH interface perturbation)",
-            "config": {"workload": WORKLOAD, "grid": [N, N], "parallelism": "host threads"},
+            "config": headline_config("fp64"),
+            "executor": "oracle port of the reference CPU path, %d host threads (%s)" % (threads, cpu_model()),
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": "%d SSP-RK3 steps of KH 1024x1024 from t=0 (incl. setup) on %d threads"
-                                       % (done, threads)},
+                             "cpu_model": cpu_model(), "one_thread_value": N * N * done1 / sec1,
+                             "sample": "%d SSP-RK3 steps of KH 1024x1024 after %d warm-up steps on %d threads; "
+                                       "%d steps on 1 thread; step loop only" % (done, max(args.warmup, 1),
+                                                                                 threads, done1)},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -355,142 +396,246 @@ def run_gpu(args):
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded KH interface perturbation, sample = rank)",
-                "config": {"workload": WORKLOAD, "grid": [N, N], "equation": "euler2", "reconstruction": "weno2",
-                           "flux": "hll3", "integrator": "rungekutta3", "precision": args.precision,
-                           "l2": "flushed before every timed step (512 MiB memset, outside the events)",
-                           "parallelism": "replicas" if world > 1 else "single GPU",
-                           "stage_kernel": stage_kernel},
+                "config": headline_config(args.precision), "stage_kernel": stage_kernel,
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clk,
                 "gpu_launches": int(launches1 - launches0), "fp64_df": df,
                 "sim": {"t": t_sim, "steps": steps_done}}
+        s.close()
+        # the batched UQ ensemble and the serving stream, measured to their
+        # end times (one GPU: these describe the single-device engines)
+        if world == 1 and args.headline_uq_samples > 0:
+            line["uq"] = measure_uq(args.headline_uq_samples, args.uq_plain, args.warmup)
+        if world == 1 and args.headline_serve_requests > 0:
+            line["serve"] = measure_serve(args.headline_serve_requests, args.serve_rate, args.serve_chunk,
+                                          args.serve_plain)
         print(json.dumps(line), flush=True)
-    s.close()
+    else:
+        s.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
-def run_uq(args):
-    """Batched UQ ensemble: `--uq-samples` Kelvin-Helmholtz samples, each with
-    its own seeded perturbation (generator sample = member index), grid sizes
-    drawn uniformly from {128^2, 256^2, 512^2} (log-uniform in size) with a
-    fixed seed, FP32 state, FP64 Welford statistics per grid size at T = 2.
-    The whole ensemble advances `--steps` time steps per timed region, each
-    member with its own dt. samples/s is extrapolated to T = 2 from the
-    measured ensemble cell-update rate and each size's initial dt; the plain
-    FP64 one-solve-at-a-time path is timed per size the same way and
-    extrapolated identically, so the ratio compares equal work."""
+UQ_SIZES = (128, 256, 512)
+UQ_SCHEME = ("euler2", "hll3", "weno2", "rungekutta3", "periodic")
+UQ_T = 2.0
+
+
+def uq_sizes(S):
+    """Grid sizes of the first S members of the 4096-member ensemble: drawn
+    uniformly from {128, 256, 512} (log-uniform in size) with a fixed seed."""
+    import numpy as np
+    rng = np.random.default_rng(20240611)
+    return rng.choice(UQ_SIZES, size=max(S, 4096))[:S]
+
+
+def measure_uq(S, plain_per_size, warmup, candidate=-1):
+    """Batched UQ ensemble: S Kelvin-Helmholtz members (generator sample =
+    member index, grids from uq_sizes), FP32 state, FP64 Welford mean /
+    variance per grid size, every member advanced from t = 0 to T = 2 in one
+    ensemble (one persistent launch per RK stage, one graph per step). The
+    timed region is the whole advance to T with the members resident in HBM;
+    samples/s = S / that time. The plain FP64 path solves members one at a
+    time to T = 2 as well (plain_per_size members of each grid size, the
+    first ones of the ensemble); its samples/s is S over the time those
+    measured per-size means give for the ensemble's mix."""
     import numpy as np
     import torch
     from alsvinn_gb300 import lib
 
-    S = args.uq_samples
-    sizes_choice = (128, 256, 512)
-    rng = np.random.default_rng(20240611)
-    sizes = rng.choice(sizes_choice, size=S)
-    T = 2.0
-    scheme = ("euler2", "hll3", "weno2", "rungekutta3", "periodic")
-    b0 = lib.Batch(*scheme, 1 << 20, 1, gamma=1.4, cfl=0.4, precision=lib.FP32)
-    pool = sum(b0.member_bytes((int(n), int(n), 1)) for n in sizes) + (64 << 20)
-    b0.close()
+    sizes = uq_sizes(S)
+    counts = {int(n): int((sizes == n).sum()) for n in UQ_SIZES}
+    probe = lib.Batch(*UQ_SCHEME, 1 << 20, 1, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    pool = sum(probe.member_bytes((int(n), int(n), 1)) for n in sizes) + (64 << 20)
+    probe.close()
+
+    def build():
+        b = lib.Batch(*UQ_SCHEME, pool, S, gamma=1.4, cfl=0.4, precision=lib.FP32)
+        if candidate >= 0:
+            b.select_candidate(candidate)
+        slots = [b.add((int(n), int(n), 1), (0, 0, 0), (1, 1, 0), lib.init_kelvin_helmholtz(int(n), sample=i),
+                       group=UQ_SIZES.index(int(n))) for i, n in enumerate(sizes)]
+        return b, slots
+
+    # warm-up ensemble of the same members: a few steps (the ensemble
+    # autotuner runs here and caches its choice for the scheme)
+    wb, _ = build()
+    wb.advance(UQ_T, 1, warmup)
+    torch.cuda.synchronize()
+    tune_ms = wb.autotune_result()
+    wb.close()
+
     t0 = time.perf_counter()
-    b = lib.Batch(*scheme, pool, S, gamma=1.4, cfl=0.4, precision=lib.FP32)
-    if args.candidate >= 0:
-        b.select_candidate(args.candidate)
-    slots = []
-    for s in range(S):
-        n = int(sizes[s])
-        slots.append(b.add((n, n, 1), (0, 0, 0), (1, 1, 0), lib.init_kelvin_helmholtz(n, sample=s),
-                           group=sizes_choice.index(n)))
+    b, slots = build()
+    torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(b.stream())
-    b.advance(T, 1, args.warmup)
-    torch.cuda.synchronize()
-    # each size's dt after warm-up -> steps to T
-    dts = {}
-    for s in range(S):
-        n = int(sizes[s])
-        if n not in dts:
-            t, st = b.member_time(slots[s])
-            dts[n] = t / st
     launches0 = b.launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clocks:
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
         e0.record(stream)
-        b.advance(T, 1, args.steps)
+        b.advance(UQ_T, 1, 0)
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+        wall = time.perf_counter() - w0
+    gpu_ms = e0.elapsed_time(e1)
     launches = b.launches() - launches0
+    steps = {}
+    cell_updates = 0
+    for i, n in enumerate(sizes):
+        t, st = b.member_time(slots[i])
+        if t != UQ_T:
+            raise RuntimeError("member %d ended at t=%r, not T" % (i, t))
+        steps.setdefault(int(n), []).append(st)
+        cell_updates += int(n) ** 2 * st
+    folded = {n: b.stats(UQ_SIZES.index(n), (n + 4) ** 2)[2] for n in UQ_SIZES if counts[n]}
     cand, tma_members = b.current_candidate()
-    tune_ms = b.autotune_result()
-    cells = float(sum(int(n) ** 2 for n in sizes))
-    rate = cells * args.steps / (ms * 1e-3)
-    work_to_T = sum((int(n) ** 2) * (T / dts[int(n)]) for n in sizes)
-    samples_per_s = S * rate / work_to_T
     b.close()
-    probe = lib.Solver(*scheme, (128, 128, 1), (0, 0, 0), (1, 1, 0), precision=lib.FP32)
+    probe = lib.Solver(*UQ_SCHEME, (128, 128, 1), (0, 0, 0), (1, 1, 0), precision=lib.FP32)
     cands = probe.candidates()
     probe.close()
     stage_kernel = {"candidate": cand, "tile": list(cands[cand][0]), "threads": cands[cand][1],
                     "tma": cands[cand][2], "members_staged_by_tma": tma_members,
                     "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
-                                               for c, m in zip(cands, tune_ms)],
-                    "autotune_score": "mean stage launch of one RK3 step over all members: (MODE_L + 2 x stage 1) / 3"}
+                                               for c, m in zip(cands, tune_ms)]}
 
-    # plain FP64, one solve at a time, each size
-    plain_step_ms = {}
-    for n in sizes_choice:
-        sv = lib.Solver(*scheme, (n, n, 1), (0, 0, 0), (1, 1, 0), gamma=1.4, cfl=0.4, precision=lib.FP64)
-        sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=0))
-        sv.advance(T, 1, 3)
-        st = torch.cuda.ExternalStream(sv.stream())
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        k = max(5, args.steps // 2)
-        a0.record(st)
-        sv.advance(T, 1, k)
-        a1.record(st)
-        torch.cuda.synchronize()
-        plain_step_ms[n] = a0.elapsed_time(a1) / k
-        sv.close()
-    plain_time_to_T = sum(plain_step_ms[int(n)] * 1e-3 * (T / dts[int(n)]) for n in sizes)
-    plain_samples_per_s = S / plain_time_to_T
-    line = {"metric": "UQ samples/s", "value": samples_per_s, "unit": "samples/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state, f64 statistics",
+    # plain FP64, one solve at a time, each run from t = 0 to T
+    plain = {}
+    for n in UQ_SIZES:
+        members = [i for i in range(S) if int(sizes[i]) == n][:plain_per_size]
+        times = []
+        for i in members:
+            sv = lib.Solver(*UQ_SCHEME, (n, n, 1), (0, 0, 0), (1, 1, 0), gamma=1.4, cfl=0.4, precision=lib.FP64)
+            sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=i))
+            sv.autotune()  # cached per scheme and grid, as a served process would have it
+            st = torch.cuda.ExternalStream(sv.stream())
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            p0 = time.perf_counter()
+            a0.record(st)
+            sv.advance(UQ_T, 1, 0)
+            a1.record(st)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - p0)
+            t, nst, _ = sv.time()
+            if t != UQ_T:
+                raise RuntimeError("plain solve ended at t=%r" % t)
+            sv.close()
+        if times:
+            plain[n] = {"members_timed": len(times), "mean_s_to_T": sum(times) / len(times)}
+    plain_time = sum(counts[n] * plain[n]["mean_s_to_T"] for n in UQ_SIZES if counts[n])
+    plain_rate = S / plain_time
+    return {"metric": "UQ samples/s", "value": S / wall, "unit": "samples/s", "samples": S,
+            "size_counts": {str(n): counts[n] for n in UQ_SIZES}, "end_time": UQ_T,
+            "wall_s_to_T": wall, "gpu_ms_to_T": gpu_ms, "setup_s": setup_s,
+            "steps_to_T": {str(n): [min(v), max(v)] for n, v in sorted(steps.items())},
+            "cell_updates_per_s": cell_updates / wall, "members_folded_per_size": {str(k): v for k, v in folded.items()},
+            "dtype": "f32 state, f64 statistics", "stage_kernel": stage_kernel,
+            "plain_fp64_one_at_a_time": {"samples_per_s": plain_rate, "per_size": {str(k): v for k, v in plain.items()},
+                                         "method": "members solved one at a time to T = 2 (FP64, autotuned "
+                                                   "single-grid path); the per-size mean time applied to the "
+                                                   "ensemble's size mix"},
+            "speedup_vs_plain_fp64": (S / wall) / plain_rate,
+            "measured": "every member run from t = 0 to T = 2 inside the timed region (no extrapolation)",
+            "gpu_launches": int(launches), "clocks": clocks.summary()}
+
+
+def run_uq(args):
+    r = measure_uq(args.uq_samples, args.uq_plain, args.warmup, args.candidate)
+    line = {"metric": r["metric"], "value": r["value"], "unit": r["unit"], "n_gpus": 1, "steps": None,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r["dtype"],
             "data": "synthetic (seeded KH perturbation per member, generator sample = member index)",
-            "config": {"workload": "uq_kh_%d_samples_128_256_512_fp32" % S, "samples": S,
-                       "size_counts": {str(n): int((sizes == n).sum()) for n in sizes_choice},
-                       "end_time": T, "l2": "working set %.1f GB >> L2" % (pool / 1e9),
-                       "stage_kernel": stage_kernel},
-            "batched_cell_updates_per_s": rate,
-            "plain_fp64_one_at_a_time_samples_per_s": plain_samples_per_s,
-            "speedup_vs_plain_fp64": samples_per_s / plain_samples_per_s,
-            "plain_fp64_step_ms": {str(k): v for k, v in plain_step_ms.items()},
-            "initial_dt": {str(k): v for k, v in dts.items()},
-            "extrapolation": "samples/s = samples * measured rate / sum_i n_i^2 * (T / dt_i(initial))",
-            "setup_s": setup_s, "gpu_launches": int(launches), "clocks": clocks.summary()}
+            "config": {"workload": "uq_kh_%d_samples_128_256_512_fp32_to_T2" % args.uq_samples,
+                       "samples": args.uq_samples, "l2": "working set of the ensemble >> L2"},
+            "e2e": None}
+    line.update({k: v for k, v in r.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 
-def run_serve(args):
-    """Serving stream: `--serve-requests` solve requests with Poisson arrivals
-    at `--serve-rate` per second (fixed seed), half 1D Burgers (1024-8192 cells,
-    periodic, Godunov, WENO2, RK2, T=0.5, random phase U[-1,1]) and half 2D
-    Kelvin-Helmholtz (128^2-1024^2, seeded perturbation, T=1.0), grid sizes
-    log-uniform, FP32 state, FP64 statistics, 120 GB HBM budget. Latency is
-    completion minus arrival. The plain FP64 one-at-a-time comparison uses
-    measured FP64 step times per (kind, size) and each request's step count,
-    served first-come first-served one after another on the same arrivals."""
+def _l1_scaled(a, b):
+    """Per-variable sum|a-b| over max(sum|b| of the variable, of variable 0)."""
     import numpy as np
-    import torch
+    a = a.reshape(a.shape[0], -1)
+    b = b.reshape(b.shape[0], -1)
+    den = np.maximum(np.abs(b).sum(axis=1), np.abs(b[0]).sum())
+    return np.abs(a - b).sum(axis=1) / den
+
+
+def run_uq_error(args):
+    """Error of the UQ ensemble's statistics against the FP64 reference at the
+    UQ configuration's grids, end time and save times: per grid size the
+    first `--uq-error-members` members of the 4096-member ensemble, run as
+    three ensembles -- GBFV_FP64_EXACT (bit-identical to the reference CPU
+    path at any length, so it is the FP64 oracle), GBFV_FP64 and GBFV_FP32 --
+    with mean / variance at 8 save times up to T = 2; per save time the
+    per-variable L1 error of the mean and of the variance over the interior
+    (scaled by max(the variable's L1 norm, the density's))."""
+    import numpy as np
     from alsvinn_gb300 import lib
 
+    M = args.uq_error_members
+    saves = 8
+    sizes = uq_sizes(4096)
+    out = {}
+    t0 = time.perf_counter()
+    for n in UQ_SIZES:
+        members = [i for i in range(4096) if int(sizes[i]) == n][:M]
+        total = (n + 4) ** 2
+        stats = {}
+        for name, prec in (("fp64_exact", lib.FP64_EXACT), ("fp64", lib.FP64), ("fp32", lib.FP32)):
+            probe = lib.Batch(*UQ_SCHEME, 1 << 20, 1, gamma=1.4, cfl=0.4, precision=prec)
+            pool = len(members) * probe.member_bytes((n, n, 1)) + (16 << 20)
+            probe.close()
+            with lib.Batch(*UQ_SCHEME, pool, len(members), gamma=1.4, cfl=0.4, precision=prec) as b:
+                b.set_statistics_saves(saves)
+                for i in members:
+                    b.add((n, n, 1), (0, 0, 0), (1, 1, 0), lib.init_kelvin_helmholtz(n, sample=i), group=0)
+                b.advance(UQ_T, saves, 0)
+                per_save = []
+                for k in range(saves):
+                    cnt, mean, m2 = b.stats_export(0, total, save=k)
+                    if cnt != len(members):
+                        raise RuntimeError("save %d folded %d of %d members" % (k, cnt, len(members)))
+                    g = 2
+                    sl = lambda X: X.reshape(4, n + 4, n + 4)[:, g:-g, g:-g]
+                    per_save.append((sl(mean), sl(m2 / cnt)))
+                stats[name] = per_save
+        ref = stats["fp64_exact"]
+        rows = []
+        for k in range(saves):
+            row = {"t": UQ_T * (k + 1) / saves}
+            for name in ("fp64", "fp32"):
+                m, v = stats[name][k]
+                row[name] = {"mean": [float(x) for x in _l1_scaled(m, ref[k][0])],
+                             "variance": [float(x) for x in _l1_scaled(v, ref[k][1])]}
+            rows.append(row)
+        out[str(n)] = {"members": len(members), "per_save": rows}
+    line = {"metric": "UQ statistics L1 error vs FP64 reference", "unit": "relative L1 (per variable)",
+            "value": max(max(r["fp32"]["variance"]) for v in out.values() for r in v["per_save"][-1:]),
+            "config": {"workload": "uq_kh_128_256_512_to_T2_first_members", "members_per_size": M,
+                       "saves": saves, "reference": "GBFV_FP64_EXACT ensembles (bit-identical to the reference CPU "
+                                                    "path)", "variables": ["rho", "mx", "my", "E"]},
+            "errors": out, "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+
+
+SERVE_BUDGET = 120 * (1 << 30)
+
+
+def serve_requests(R, rate):
+    """R requests with Poisson arrivals at `rate` per second (fixed seed),
+    about half 1D Burgers (1024-8192 cells, T = 0.5, phase U[-1, 1]) and half
+    2D Kelvin-Helmholtz (128^2-1024^2, T = 1.0, generator sample = request
+    index), sizes uniform over the powers of two."""
+    import numpy as np
+    from alsvinn_gb300 import lib
     rng = np.random.default_rng(20240612)
-    R = args.serve_requests
-    gaps = rng.exponential(1.0 / args.serve_rate, size=R)
+    gaps = rng.exponential(1.0 / rate, size=R)
     arrivals = np.cumsum(gaps) - gaps[0]
     kinds = rng.integers(0, 2, size=R)
     reqs = []
@@ -501,84 +646,126 @@ def run_serve(args):
         else:
             n = int(rng.choice([128, 256, 512, 1024]))
             reqs.append((lib.REQUEST_KELVIN_HELMHOLTZ, n, 1.0, 0.0, i, float(arrivals[i])))
-    budget = 120 * (1 << 30)
-    s = lib.Server(budget, precision=lib.FP32, max_slots=4096)
+    return reqs
+
+
+def serve_batched(reqs, chunk):
+    """Serves `reqs` through the continuous-batching loop (FP32 state, FP64
+    statistics, 120 GB budget); returns (wall s, results, launches, clocks)."""
+    from alsvinn_gb300 import lib
+    s = lib.Server(SERVE_BUDGET, precision=lib.FP32, max_slots=4096)
     ids = [s.submit(k, n, T, phase=ph, sample=sm, arrival=a) for (k, n, T, ph, sm, a) in reqs]
-    t0 = time.perf_counter()
     with ClockSampler(0) as clocks:
-        s.run(args.serve_chunk)
-    wall = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        s.run(chunk)
+        wall = time.perf_counter() - t0
     res = [s.result(i) for i in ids]
     launches = s.launches()
     s.close()
-    lat = np.array([r["finish"] - r["arrival"] for r in res])
-    done = sum(1 for r in res if r["status"] == 2)
-    steps = [r["steps"] for r in res]
+    return wall, res, launches, clocks.summary()
 
-    # plain FP64, one solve at a time: measured step time per (kind, n)
-    step_ms = {}
-    for (k, n) in sorted({(r[0], r[1]) for r in reqs}):
+
+def serve_plain_fp64(reqs):
+    """The same requests solved by plain FP64 solvers one at a time, first
+    come first served, each started no earlier than its arrival (real time)."""
+    import torch
+    from alsvinn_gb300 import lib
+    lat, steps = [], []
+    t0 = time.perf_counter()
+    for (k, n, T, ph, sm, a) in reqs:
+        now = time.perf_counter() - t0
+        if now < a:
+            time.sleep(a - now)
         if k == lib.REQUEST_BURGERS:
             sv = lib.Solver("burgers", "godunov", "weno2", "rungekutta2", "periodic", (n, 1, 1), (0, 0, 0),
                             (1, 1, 1), cfl=0.475, precision=lib.FP64)
-            sv.set_primitive(lib.init_burgers_sine(n, 0.3))
-            T = 0.5
+            sv.set_primitive(lib.init_burgers_sine(n, ph))
         else:
             sv = lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (n, n, 1), (0, 0, 0), (1, 1, 0),
                             cfl=0.4, precision=lib.FP64)
-            sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=0))
-            T = 1.0
-        sv.advance(T, 1, 5)
-        st = torch.cuda.ExternalStream(sv.stream())
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        kk = 40 if k == lib.REQUEST_BURGERS else 10
-        a0.record(st)
-        sv.advance(T, 1, kk)
-        a1.record(st)
+            sv.set_primitive(lib.init_kelvin_helmholtz(n, sample=sm))
+        sv.advance(T, 1, 0)
         torch.cuda.synchronize()
-        step_ms[(k, n)] = a0.elapsed_time(a1) / kk
+        steps.append(sv.time()[1])
         sv.close()
-    clock = 0.0
-    plain_lat = []
-    for (k, n, T, ph, sm, a), nsteps in zip(reqs, steps):
-        start = max(clock, a)
-        clock = start + nsteps * step_ms[(k, n)] * 1e-3
-        plain_lat.append(clock - a)
-    plain_lat = np.array(plain_lat)
-    plain_rate = R / (clock - arrivals[0])
-    line = {"metric": "serving samples/s", "value": done / wall, "unit": "samples/s", "n_gpus": 1,
-            "steps": int(sum(steps)), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state, f64 statistics",
-            "data": "synthetic (Poisson arrivals, seeded phases / perturbations)",
-            "config": {"workload": "serve_burgers1d_kh2d_mix", "requests": R, "rate_per_s": args.serve_rate,
-                       "budget_bytes": budget, "steps_per_chunk": args.serve_chunk},
+        lat.append(time.perf_counter() - t0 - a)
+    wall = time.perf_counter() - t0
+    return wall, lat, steps
+
+
+def measure_serve(R, rate, chunk, plain_subset):
+    """Serving stream: R requests through the continuous-batching loop
+    (latency = completion - arrival, samples/s = completed / wall from the
+    first arrival); then the first `plain_subset` requests of the same
+    stream, run both ways -- batched, and plain FP64 one at a time FIFO --
+    for a measured comparison on equal work."""
+    import numpy as np
+    reqs = serve_requests(R, rate)
+    wall, res, launches, clk = serve_batched(reqs, chunk)
+    lat = np.array([r["finish"] - r["arrival"] for r in res])
+    done = sum(1 for r in res if r["status"] == 2)
+    sub = reqs[:plain_subset]
+    swall, sres, _, sclk = serve_batched(sub, chunk)
+    slat = np.array([r["finish"] - r["arrival"] for r in sres])
+    pwall, plat, _ = serve_plain_fp64(sub)
+    plat = np.array(plat)
+    sub_rate = len(sub) / swall
+    plain_rate = len(sub) / pwall
+    kinds = {}
+    for (k, n, T, ph, sm, a) in reqs:
+        key = "%s_%d" % ("burgers1d" if k == 0 else "kh2d", n)
+        kinds[key] = kinds.get(key, 0) + 1
+    return {"metric": "serving samples/s", "value": done / wall, "unit": "samples/s", "requests": R,
+            "rate_per_s": rate, "completed": done, "wall_s": wall,
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
-            "completed": done, "wall_s": wall,
-            "plain_fp64_one_at_a_time": {"samples_per_s": plain_rate,
-                                         "latency_p50_s": float(np.percentile(plain_lat, 50)),
-                                         "latency_p99_s": float(np.percentile(plain_lat, 99)),
-                                         "method": "measured FP64 step time per (kind, n) x each request's "
-                                                   "steps, served FIFO one at a time on the same arrivals"},
-            "speedup_vs_plain_fp64": (done / wall) / plain_rate,
-            "fp64_step_ms": {"%s_%d" % ("burgers" if k == 0 else "kh", n): v for (k, n), v in step_ms.items()},
-            "gpu_launches": int(launches), "clocks": clocks.summary()}
+            "mix": kinds, "budget_bytes": SERVE_BUDGET, "steps_per_chunk": chunk,
+            "dtype": "f32 state, f64 statistics",
+            "subset_comparison": {
+                "requests": len(sub), "batched_fp32": {"samples_per_s": sub_rate,
+                                                        "latency_p50_s": float(np.percentile(slat, 50)),
+                                                        "latency_p99_s": float(np.percentile(slat, 99)),
+                                                        "clocks": sclk},
+                "plain_fp64_one_at_a_time": {"samples_per_s": plain_rate,
+                                             "latency_p50_s": float(np.percentile(plat, 50)),
+                                             "latency_p99_s": float(np.percentile(plat, 99)),
+                                             "method": "run: FP64 solver per request, FIFO, each started no "
+                                                       "earlier than its arrival"},
+                "speedup_vs_plain_fp64": sub_rate / plain_rate},
+            "gpu_launches": int(launches), "clocks": clk}
+
+
+def run_serve(args):
+    r = measure_serve(args.serve_requests, args.serve_rate, args.serve_chunk, args.serve_plain)
+    line = {"metric": r["metric"], "value": r["value"], "unit": r["unit"], "n_gpus": 1, "steps": None,
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": r["dtype"], "data": "synthetic (Poisson arrivals, seeded phases / perturbations)",
+            "config": {"workload": "serve_burgers1d_kh2d_mix", "requests": args.serve_requests,
+                       "rate_per_s": args.serve_rate}, "e2e": None}
+    line.update({k: v for k, v in r.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="kh1024", choices=["kh1024", "uq", "serve"])
-    ap.add_argument("--serve-requests", type=int, default=64)
-    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--workload", default="kh1024", choices=["kh1024", "uq", "serve", "uq-error"])
+    ap.add_argument("--uq-error-members", type=int, default=8, help="members per grid size of --workload uq-error")
+    ap.add_argument("--serve-requests", type=int, default=128)
+    ap.add_argument("--serve-rate", type=float, default=2.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--serve-plain", type=int, default=12,
+                    help="requests of the stream also run by plain FP64 one at a time")
     ap.add_argument("--uq-samples", type=int, default=4096)
+    ap.add_argument("--uq-plain", type=int, default=2, help="plain FP64 solves to T per grid size")
+    ap.add_argument("--headline-uq-samples", type=int, default=192,
+                    help="members of the UQ ensemble measured to T inside the default run (0: skip)")
+    ap.add_argument("--headline-serve-requests", type=int, default=96,
+                    help="requests of the serving stream measured inside the default run (0: skip)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=60)
+    ap.add_argument("--cpu-steps", type=int, default=200)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64-df", "fp64-exact"])
     ap.add_argument("--no-df", action="store_true", help="skip the double-float measurement")
     ap.add_argument("--candidate", type=int, default=-1,
@@ -592,6 +779,8 @@ def main():
         run_uq(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "uq-error":
+        run_uq_error(args)
     else:
         run_gpu(args)
 

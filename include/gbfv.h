@@ -203,6 +203,100 @@ int gbfv_apply_boundary(gbfv_solver* s, void* state_dev);
  * alsfvm/include/alsfvm/equation/CellComputer.hpp:61). */
 int gbfv_obeys_constraints(gbfv_solver* s, const void* state_dev, int* ok);
 
+/* The operator-level calls on a reference Volume as it is laid out: one
+ * padded device array per conserved variable (vars[k], k < nvar; separate
+ * allocations or one block), issued on `stream` (NULL: the solver's), and
+ * synchronous on return like the reference's CUDA path. */
+
+/* NumericalFlux::computeFlux(U, waveSpeed, computeWaveSpeed, out, start,
+ * end) (alsfvm/include/alsfvm/numflux/NumericalFlux.hpp:44-52,
+ * alsfvm/src/numflux/NumericalFluxCPU.cpp:167-221) on the region of cells
+ * [start, n + end) per active dimension (interior coordinates; start[d] >=
+ * 0, end[d] <= 0; inactive dimensions 0): out gets, on those cells only,
+ * sum_d (F_{i-1/2} - F_{i+1/2}) (unscaled); the other cells of out keep
+ * their values; ws[d] = the maximum wave speed of the faces from the
+ * region's lower to its upper face in direction d. ConservedSystem splits a
+ * stage into the interior and 2 x dim side strips
+ * (alsfvm/src/simulator/ConservedSystem.cpp:59-96): each call costs its
+ * region. start / end NULL: the whole interior. */
+int gbfv_compute_flux_region(gbfv_solver* s, const void* const* state_vars, void* const* out_vars, double ws[3],
+                             const int start[3], const int end[3], void* stream);
+
+/* Reconstruction::performReconstruction(in, direction, 0, left, right,
+ * start, end) (alsfvm/include/alsfvm/reconstruction/Reconstruction.hpp:
+ * 46-58, cell range of alsfvm/src/reconstruction/ReconstructionCPU.cpp:
+ * 64-72 shifted by start / end; "none" copies every cell). */
+int gbfv_reconstruct_vars(gbfv_solver* s, int direction, const void* const* state_vars, void* const* left_vars,
+                          void* const* right_vars, const int start[3], const int end[3], void* stream);
+
+/* Boundary::applyBoundaryConditions (alsfvm/include/alsfvm/boundary/
+ * Boundary.hpp:30-31) on one array per variable. */
+int gbfv_apply_boundary_vars(gbfv_solver* s, void* const* vars, void* stream);
+
+/* CellComputer::obeysConstraints on one array per variable. */
+int gbfv_obeys_constraints_vars(gbfv_solver* s, const void* const* vars, int* ok, void* stream);
+
+/* The other CellComputer maps (alsfvm/include/alsfvm/equation/CellComputer.hpp:
+ * 35-70, as CPUCellComputer computes them over every cell of the volume,
+ * alsfvm/src/equation/CPUCellComputer.cpp:31-140):
+ *   gbfv_prim_to_cons_vars      computeFromPrimitive (rho, u..., p) -> conserved
+ *   gbfv_extra_variables_vars   computeExtraVariables: p, then u (Euler; Burgers
+ *                               has none)
+ *   gbfv_max_wave_speed_vars    computeMaxWaveSpeed in one direction (cells whose
+ *                               speed is not a number are passed over) */
+int gbfv_prim_to_cons_vars(gbfv_solver* s, const void* const* prim_vars, void* const* cons_vars, void* stream);
+int gbfv_extra_variables_vars(gbfv_solver* s, const void* const* cons_vars, void* const* extra_vars, void* stream);
+int gbfv_max_wave_speed_vars(gbfv_solver* s, const void* const* cons_vars, int direction, double* speed,
+                             void* stream);
+
+/* ------------------------------------------------ device array arithmetic */
+
+/* Elementwise arithmetic on device arrays of `count` values (float for
+ * GBFV_FP32, double otherwise), issued on `stream` (a cudaStream_t; NULL:
+ * the default stream): what a device Memory<real> of the "gb300" platform
+ * needs so that the reference's own integrators and statistics run on
+ * device state (replaces memory::Memory<real>'s arithmetic,
+ * alsfvm/include/alsfvm/memory/Memory.hpp:166-302, which the reference's
+ * cuda platform implements in alsfvm/src/cuda/CudaMemory.cpp and
+ * alsfvm/src/cuda/vector_operations.cu). Operations run in the element type
+ * in the order of the reference's HostMemory loops
+ * (alsfvm/src/memory/HostMemory.cpp:97-311) without multiply-add
+ * contraction, so double results equal the reference CPU path's bit for bit
+ * (a power other than 1 or 2 uses CUDA's pow). A scalar is a double, as the
+ * reference's `real`: float elements are widened, operated on and rounded. */
+typedef enum {
+    GBFV_MEMORY_ADD = 0,      /* a += b  (Memory::operator+=) */
+    GBFV_MEMORY_SUBTRACT = 1, /* a -= b  (operator-=) */
+    GBFV_MEMORY_MULTIPLY = 2, /* a *= b  (operator*=) */
+    GBFV_MEMORY_DIVIDE = 3    /* a /= b  (operator/=) */
+} gbfv_memory_op_kind;
+
+int gbfv_memory_op(int op, void* a_dev, const void* b_dev, long long count, int precision, void* stream);
+/* a op= scalar (Memory::operator+=(real) etc.). */
+int gbfv_memory_op_scalar(int op, void* a_dev, double scalar, long long count, int precision, void* stream);
+/* a = 0 (Memory::makeZero). */
+int gbfv_memory_make_zero(void* a_dev, long long count, int precision, void* stream);
+/* v1 = a1 v1 + a2 v2 + a3 v3 + a4 v4 + a5 v5, left to right, coefficients in
+ * the element type (Memory::addLinearCombination). */
+int gbfv_memory_add_linear_combination(void* v1_dev, double a1, double a2, const void* v2_dev, double a3,
+                                       const void* v3_dev, double a4, const void* v4_dev, double a5,
+                                       const void* v5_dev, long long count, int precision, void* stream);
+/* a += factor * pow(b, power) (Memory::addPower; factor 1 for its
+ * two-argument form) and a -= pow(b, power) (Memory::subtractPower). */
+int gbfv_memory_add_power(void* a_dev, const void* b_dev, double power, double factor, long long count, int precision,
+                          void* stream);
+int gbfv_memory_subtract_power(void* a_dev, const void* b_dev, double power, long long count, int precision,
+                               void* stream);
+/* Total variation of a padded array with extents[3] (x fastest) over
+ * [start, end) (Memory::getTotalVariation, HostMemory.cpp:323-392):
+ * direction -1: sum of pow(sqrt((u - u(y-1))^2 + (u - u(x-1))^2), p) with
+ * x from start.x + 1, y from start.y + 1 (2D) and z from 0 (1D / 2D only);
+ * direction d: sum of pow(|u - u(-e_d)|, p) from start + e_d. Summed in FP64
+ * in a fixed order (equal to the reference's sequential sum to rounding);
+ * *result is written after the stream synchronises. */
+int gbfv_memory_total_variation(const void* a_dev, const int extents[3], int p, int direction, const int start[3],
+                                const int end[3], int precision, double* result, void* stream);
+
 /* ------------------------------------------------------- statistics */
 
 typedef struct gbfv_stats gbfv_stats;
@@ -345,6 +439,20 @@ int gbfv_batch_remove(gbfv_batch* b, int slot);
  * end_time stop; their states are folded into their statistics group. */
 int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int max_steps);
 
+/* A member's own end time: it stops at min(end_time, the end time of the
+ * advance) and, with number_of_saves > 0, its dt is clamped to the save times
+ * k * end_time / number_of_saves (the FixedIntervalWriter clamp, alsfvm/src/
+ * io/FixedIntervalWriter.cpp:45-53), so it lands exactly on end_time. The
+ * advance's number_of_saves no longer applies to it. A reference run's end
+ * time belongs to its configuration (alsfvm/src/config/SimulatorSetup.cpp:
+ * 102-232), so members of one ensemble may each have their own. */
+int gbfv_batch_set_member_end(gbfv_batch* b, int slot, double end_time, int number_of_saves);
+
+/* A member's status: 0 running or finished, 1 its state broke the constraint
+ * check (CPUCellComputer::obeysConstraints; the member stopped at
+ * *failed_step while the others went on), 2 a halo copy timed out. */
+int gbfv_batch_member_status(gbfv_batch* b, int slot, int* status, int* failed_step);
+
 int gbfv_batch_member_time(gbfv_batch* b, int slot, double* t, long long* steps);
 int gbfv_batch_member_state(gbfv_batch* b, int slot, double* state_host);
 
@@ -394,23 +502,30 @@ int gbfv_batch_autotune_result(gbfv_batch* b, double* ms, int capacity);
 /* ----------------------------------------------------------- serving */
 
 /* A continuous-batching request loop over two ensembles (no counterpart in
- * the reference, whose alsuq runs a fixed list of samples). Requests arrive
- * at their `arrival` time (seconds after gbfv_server_run starts), are
- * admitted once their grid fits the HBM budget (first fit in arrival order),
- * run next to the requests already in flight with their own dt, fold their
- * final state into the FP64 statistics of their (kind, grid) group and leave,
- * freeing their memory. Burgers and Kelvin-Helmholtz requests run in two
- * ensembles driven by two host threads on two streams. */
+ * the reference, whose alsuq runs a fixed list of samples). A request is a
+ * solve (equation, grid, end time, initial-data seed). Requests arrive at
+ * their `arrival` time (seconds after gbfv_server_run starts), are admitted
+ * once their grid fits the HBM budget (first fit in arrival order), run next
+ * to the requests already in flight with their own dt and their own end
+ * time, fold their final state into the FP64 statistics of their (kind,
+ * grid, end time) group and leave, freeing their memory. A request whose
+ * state breaks the constraint check fails alone (status 3) and leaves; the
+ * others run on. Burgers and Kelvin-Helmholtz requests run in two ensembles
+ * driven by two host threads on two streams. */
 typedef enum { GBFV_REQUEST_BURGERS = 0, GBFV_REQUEST_KELVIN_HELMHOLTZ = 1 } gbfv_request_kind;
 
 typedef struct {
-    int kind;         /* gbfv_request_kind */
+    int kind;         /* gbfv_request_kind: the equation and its scheme */
     int n;            /* cells per dimension (Burgers: nx; KH: nx = ny) */
-    double end_time;
+    double end_time;  /* the request's own end time */
     double phase;     /* Burgers: u0 = sin(2 pi x) + 0.5 phase, phase in [-1, 1] */
     int sample;       /* KH: generator sample of the interface perturbation */
     double arrival;   /* seconds after the start of gbfv_server_run */
     int keep;         /* 1: keep the final state for gbfv_server_final_state */
+    /* NULL: the kind's initial data from phase / sample. Otherwise the
+     * caller's interior primitive variables (Burgers n values, KH 4 n^2),
+     * copied by gbfv_server_submit. */
+    const double* initial_primitive;
 } gbfv_request;
 
 typedef struct gbfv_server gbfv_server;
@@ -422,13 +537,18 @@ int gbfv_server_destroy(gbfv_server* s);
 /* Queue requests before gbfv_server_run; their arrival times pace admission. */
 int gbfv_server_submit(gbfv_server* s, const gbfv_request* r, int* id);
 /* Serves every submitted request, advancing each ensemble in chunks of
- * steps_per_chunk time steps between admissions. */
+ * steps_per_chunk time steps between admissions. A request that fails does
+ * not stop the run; a CUDA error does (every request in flight fails). */
 int gbfv_server_run(gbfv_server* s, int steps_per_chunk);
 /* Times in seconds after the start of the run; status 2 done, 3 failed. */
 int gbfv_server_result(gbfv_server* s, int id, double* arrival_s, double* admit_s, double* finish_s,
                        long long* steps, int* status);
 int gbfv_server_final_state(gbfv_server* s, int id, double* state_host, long long capacity);
-/* FP64 mean / variance of the final states of every request of a (kind, n). */
+/* FP64 mean / variance of the final states of every request of a (kind, n,
+ * end_time) group; gbfv_server_stats needs the (kind, n) requests to share
+ * one end time. */
+int gbfv_server_stats_at(gbfv_server* s, int kind, int n, double end_time, double* mean_host, double* var_host,
+                         long long* count);
 int gbfv_server_stats(gbfv_server* s, int kind, int n, double* mean_host, double* var_host, long long* count);
 int gbfv_server_launches(gbfv_server* s, long long* launches);
 

@@ -79,7 +79,10 @@ private:
     ivec3 dims;
 };
 
-// One conserved variable's padded array inside a Volume's device block.
+// One conserved variable's padded array inside a Volume's device block, with
+// Memory<real>'s arithmetic on the device (the operations the reference's
+// integrators and MeanVariance use, alsfvm/include/alsfvm/memory/
+// Memory.hpp:166-302), each synchronous on return.
 class Memory {
 public:
     Memory(real* dev, size_t size) : dev(dev), size(size) {}
@@ -93,10 +96,44 @@ public:
     void copyFromHost(const real* host, size_t count) {
         check_cuda(cudaMemcpy(dev, host, count * sizeof(real), cudaMemcpyHostToDevice));
     }
+    void operator+=(const Memory& o) { binary(GBFV_MEMORY_ADD, o); }
+    void operator-=(const Memory& o) { binary(GBFV_MEMORY_SUBTRACT, o); }
+    void operator*=(const Memory& o) { binary(GBFV_MEMORY_MULTIPLY, o); }
+    void operator/=(const Memory& o) { binary(GBFV_MEMORY_DIVIDE, o); }
+    void operator+=(real x) { sync(gbfv_memory_op_scalar(GBFV_MEMORY_ADD, dev, x, n(), GBFV_FP64, nullptr)); }
+    void operator-=(real x) { sync(gbfv_memory_op_scalar(GBFV_MEMORY_SUBTRACT, dev, x, n(), GBFV_FP64, nullptr)); }
+    void operator*=(real x) { sync(gbfv_memory_op_scalar(GBFV_MEMORY_MULTIPLY, dev, x, n(), GBFV_FP64, nullptr)); }
+    void operator/=(real x) { sync(gbfv_memory_op_scalar(GBFV_MEMORY_DIVIDE, dev, x, n(), GBFV_FP64, nullptr)); }
+    void makeZero() { sync(gbfv_memory_make_zero(dev, n(), GBFV_FP64, nullptr)); }
+    void addLinearCombination(real a1, real a2, const Memory& v2, real a3, const Memory& v3, real a4,
+                              const Memory& v4, real a5, const Memory& v5) {
+        sync(gbfv_memory_add_linear_combination(dev, a1, a2, v2.dev, a3, v3.dev, a4, v4.dev, a5, v5.dev, n(),
+                                                GBFV_FP64, nullptr));
+    }
+    void addPower(const Memory& o, double power, double factor = 1.0) {
+        same_size(o);
+        sync(gbfv_memory_add_power(dev, o.dev, power, factor, n(), GBFV_FP64, nullptr));
+    }
+    void subtractPower(const Memory& o, double power) {
+        same_size(o);
+        sync(gbfv_memory_subtract_power(dev, o.dev, power, n(), GBFV_FP64, nullptr));
+    }
 
 private:
     real* dev;
     size_t size;
+    long long n() const { return (long long)size; }
+    void same_size(const Memory& o) const {
+        if (o.size != size) throw std::runtime_error("Memory size not the same");
+    }
+    static void sync(int rc) {
+        check(rc);
+        check_cuda(cudaStreamSynchronize(nullptr));
+    }
+    void binary(int op, const Memory& o) {
+        same_size(o);
+        sync(gbfv_memory_op(op, dev, o.dev, n(), GBFV_FP64, nullptr));
+    }
 };
 
 class Volume {
@@ -177,16 +214,26 @@ struct SolverHandle {
 };
 }  // namespace detail
 
-// NumericalFlux::computeFlux: out = sum_d (F_{i-1/2} - F_{i+1/2}) on interior
-// cells, unscaled; waveSpeed = per-direction maximum face speed. start / end
-// regions give the same cells as the whole domain, which is what is computed.
+// NumericalFlux::computeFlux: out = sum_d (F_{i-1/2} - F_{i+1/2}) on the cells
+// of the region [start, n + end) (the whole interior by default), unscaled,
+// the other cells of out unchanged; waveSpeed = per-direction maximum speed
+// of the region's faces. A stream (cudaStream_t) may be given; the call is
+// synchronous on return.
 class NumericalFlux {
 public:
     NumericalFlux(const Scheme& s, const Grid& g) : scheme(s), solver(s, g) {}
     void computeFlux(const Volume& conservedVariables, rvec3& waveSpeed, bool /*computeWaveSpeed*/, Volume& output,
-                     const ivec3& /*start*/ = ivec3(), const ivec3& /*end*/ = ivec3()) {
+                     const ivec3& start = ivec3(), const ivec3& end = ivec3(), void* stream = nullptr) {
+        const size_t nv = conservedVariables.getNumberOfVariables();
+        std::vector<const void*> in(nv);
+        std::vector<void*> out(nv);
+        for (size_t k = 0; k < nv; ++k) {
+            in[k] = conservedVariables.getScalarMemoryArea(k).getPointer();
+            out[k] = output.getScalarMemoryArea(k).getPointer();
+        }
+        const int s[3] = {start.x, start.y, start.z}, e[3] = {end.x, end.y, end.z};
         double ws[3];
-        check(gbfv_compute_flux(solver.h, conservedVariables.data(), output.data(), ws));
+        check(gbfv_compute_flux_region(solver.h, in.data(), out.data(), ws, s, e, stream));
         waveSpeed = rvec3(ws[0], ws[1], ws[2]);
     }
     size_t getNumberOfGhostCells() const { return (size_t)gbfv_ghost_cells(scheme.reconstruction.c_str()); }

@@ -18,6 +18,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -33,6 +34,18 @@ static int fail(int code, const char* fmt, ...) {
 }
 
 const char* fv_last_error(void) { return g_err; }
+
+/* Wall time of the last fv_run's step loop alone (initial data, allocation
+ * and the final copy excluded), from the monotonic clock. */
+static __thread double g_loop_seconds;
+
+double fv_last_loop_seconds(void) { return g_loop_seconds; }
+
+static double now_seconds(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 void fv_set_threads(int n) {
 #ifdef _OPENMP
@@ -837,6 +850,7 @@ int fv_run(const char* equation, const char* flux, const char* recon, const char
     long numberSaved = 1;
     double t = 0;
     int steps = 0;
+    const double loop_start = now_seconds();
     while (!(t >= end_time) && (max_steps <= 0 || steps < max_steps)) {
         double dt = 0;
         for (int s = 0; s < nsub; ++s) {
@@ -895,6 +909,7 @@ int fv_run(const char* equation, const char* flux, const char* recon, const char
         }
         if (number_of_saves > 0 && t >= numberSaved * timeInterval + 0.0) numberSaved++;
     }
+    g_loop_seconds = now_seconds() - loop_start;
     memcpy(out, U[0], (size_t)nvar * total * sizeof(double));
     *t_out = t;
     *steps_out = steps;

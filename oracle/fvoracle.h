@@ -45,6 +45,9 @@ int fv_run(const char* equation, const char* flux, const char* recon, const char
            const double* prim, double* out, double* t_out, int* steps_out, double* dts,
            int max_dts);
 
+/* Seconds the last fv_run on this thread spent in its step loop. */
+double fv_last_loop_seconds(void);
+
 int fv_prim_to_cons(const char* equation, const int n[3], int ghosts, double gamma,
                     const double* prim, double* cons);
 

@@ -24,6 +24,7 @@ def load():
             _build.build_oracle()
         _lib = ctypes.CDLL(LIB_PATH)
         _lib.fv_last_error.restype = ctypes.c_char_p
+        _lib.fv_last_loop_seconds.restype = ctypes.c_double
     return _lib
 
 
@@ -93,6 +94,11 @@ def run(equation, flux, recon, integrator, bc, n, lower, upper, gamma, cfl, end_
                        _i3(n), _d3(lower), _d3(upper), D(gamma), D(cfl), D(end_time), number_of_saves,
                        max_steps, _p(prim), _p(out), ctypes.byref(tt), ctypes.byref(st), None, 0)
     return rc, out, tt.value, st.value
+
+
+def last_loop_seconds():
+    """Seconds the last run() spent in its step loop (setup excluded)."""
+    return load().fv_last_loop_seconds()
 
 
 def prim_to_cons(equation, n, ghosts, gamma, prim_padded):

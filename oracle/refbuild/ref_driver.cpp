@@ -222,6 +222,36 @@ int ref_compute_flux(const char* equation, const char* flux, const char* recon,
     }
 }
 
+// One region call of the reference's NumericalFlux (NumericalFluxCPU::
+// computeFlux with start / end, alsfvm/src/numflux/NumericalFluxCPU.cpp:
+// 167-221): out (padded, nvar * total) is read first and only the region's
+// cells change; ws gets the wave speeds the call returns.
+int ref_compute_flux_region(const char* equation, const char* flux, const char* recon,
+    const int dims[3], double gamma, const double* U, double* out, double ws[3], const int start[3],
+    const int end[3]) {
+    try {
+        double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+        Setup s(equation, flux, recon, "periodic", "forwardeuler", dims, lo, hi, gamma, 0.5);
+        numflux::NumericalFluxFactory f(equation, flux, recon, s.params, s.device);
+        auto nf = f.createNumericalFlux(*s.grid);
+        volume::VolumeFactory vf(equation, s.memory);
+        const size_t g = nf->getNumberOfGhostCells();
+        auto vin = vf.createConservedVolume(dims[0], dims[1], dims[2], g);
+        auto vout = vf.createConservedVolume(dims[0], dims[1], dims[2], g);
+        const int nvar = nvar_of(equation);
+        copy_in(*vin, U, nvar);
+        copy_in(*vout, out, nvar);
+        rvec3 w(0, 0, 0);
+        nf->computeFlux(*vin, w, true, *vout, ivec3(start[0], start[1], start[2]), ivec3(end[0], end[1], end[2]));
+        copy_out(*vout, out, nvar);
+        ws[0] = w.x; ws[1] = w.y; ws[2] = w.z;
+        return 0;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -1;
+    }
+}
+
 // Reconstruction of every variable in one direction (indicator variable 0),
 // over the reference's own cell range; left/right are padded arrays that the
 // caller pre-fills (cells outside the range keep their contents).

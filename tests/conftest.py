@@ -49,3 +49,14 @@ def rel_l1(a, b):
     den = np.abs(b).sum(axis=1)
     den[den == 0] = 1.0
     return np.abs(a - b).sum(axis=1) / den
+
+
+def state_l1(a, b):
+    """Per-variable L1 error for the FP32 state against the FP64 reference:
+    sum|a-b| over max(sum|b| of the variable, sum|b| of variable 0, the
+    density or u). A variable that starts at zero (a transverse momentum) is
+    measured against the density's scale, the others against their own."""
+    a = a.reshape(a.shape[0], -1)
+    b = b.reshape(b.shape[0], -1)
+    den = np.maximum(np.abs(b).sum(axis=1), np.abs(b[0]).sum())
+    return np.abs(a - b).sum(axis=1) / den

@@ -4,6 +4,7 @@
 // WENO2 known answers (test/library_tests/src/fvm/reconstruction/WenoTest.cpp),
 // the boundary index maps (test/library_tests/src/fvm/boundary/BoundaryTest.cpp),
 // the constraint check, the simulator loop and mean / variance.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <functional>
@@ -226,6 +227,97 @@ int main() {
             EXPECT_NEAR(m[i], 7.0 / 3.0, 1e-15);
             EXPECT_NEAR(var[i], (1 + 4 + 16) / 3.0 - 49.0 / 9.0, 1e-14);
         }
+    });
+
+    run("NumericalFlux.ConservedSystemRegionsEqualWholeDomain", [] {
+        // ConservedSystem::operator() (alsfvm/src/simulator/ConservedSystem.cpp:
+        // 59-96): the interior region, then the bottom and top strip of every
+        // dimension; together they give the whole-domain operator
+        Scheme s;
+        ivec3 n(40, 28, 1);
+        Grid g(rvec3(0, 0, 0), rvec3(1, 1, 1), n);
+        NumericalFlux flux(s, g);
+        const int gc = (int)flux.getNumberOfGhostCells();
+        Volume U("euler2", n, gc), whole("euler2", n, gc), split("euler2", n, gc);
+        const size_t total = U.getTotalSize();
+        std::vector<real> h(4 * total);
+        for (size_t i = 0; i < total; ++i) {
+            const double x = 0.37 * (double)(i % 44), y = 0.21 * (double)(i / 44);
+            h[i] = 1.5 + 0.2 * std::sin(x + y);
+            h[total + i] = 0.3 * std::cos(x);
+            h[2 * total + i] = -0.2 * std::sin(y);
+            h[3 * total + i] = 4.0 + 0.1 * std::cos(x - y);
+        }
+        U.fromHost(h);
+        rvec3 wsWhole, ws(0, 0, 0);
+        flux.computeFlux(U, wsWhole, true, whole);
+        const int size[2] = {n.x + 2 * gc, n.y + 2 * gc};
+        rvec3 w;
+        flux.computeFlux(U, w, true, split, ivec3(gc, gc, 0), ivec3(-gc, -gc, 0));
+        ws = w;
+        for (int d = 0; d < 2; ++d) {
+            ivec3 endBottom(d == 0 ? -size[0] + 3 * gc : 0, d == 1 ? -size[1] + 3 * gc : 0, 0);
+            flux.computeFlux(U, w, true, split, ivec3(), endBottom);
+            ws = rvec3(std::max(ws.x, w.x), std::max(ws.y, w.y), 0);
+            ivec3 startTop(d == 0 ? size[0] - 3 * gc : 0, d == 1 ? size[1] - 3 * gc : 0, 0);
+            flux.computeFlux(U, w, true, split, startTop, ivec3());
+            ws = rvec3(std::max(ws.x, w.x), std::max(ws.y, w.y), 0);
+        }
+        const auto a = whole.toHost(), b = split.toHost();
+        bool same = true;
+        for (int k = 0; k < 4; ++k)
+            for (int y = gc; y < n.y + gc; ++y)
+                for (int x = gc; x < n.x + gc; ++x) {
+                    const size_t i = k * total + idx(U, x, y, 0);
+                    same = same && a[i] == b[i];
+                }
+        EXPECT_TRUE(same);
+        EXPECT_TRUE(ws.x == wsWhole.x && ws.y == wsWhole.y);
+    });
+
+    run("Memory.RungeKuttaStageAlgebra", [] {
+        // RungeKutta3::performSubstep's second stage (alsfvm/src/integrator/
+        // RungeKutta3.cpp:69-77): out *= dt/dx; out += U1; out *= 1/3;
+        // out += U0; out *= 3/4, on the device, against the same on the host
+        ivec3 n(50, 1, 1);
+        Volume out("burgers", n, 2), U1("burgers", n, 2), U0("burgers", n, 2);
+        const size_t total = out.getTotalSize();
+        std::vector<real> o(total), u1(total), u0(total);
+        for (size_t i = 0; i < total; ++i) {
+            o[i] = std::sin(0.3 * i);
+            u1[i] = 1.0 + 0.01 * i;
+            u0[i] = 2.0 - 0.02 * i;
+        }
+        out.fromHost(o);
+        U1.fromHost(u1);
+        U0.fromHost(u0);
+        const real c = 0.0123;
+        Memory& m = out.getScalarMemoryArea(0);
+        m *= c;
+        m += U1.getScalarMemoryArea(0);
+        m *= 1. / 3.;
+        m += U0.getScalarMemoryArea(0);
+        m *= 3. / 4.;
+        const auto got = out.toHost();
+        bool same = true;
+        for (size_t i = 0; i < total; ++i) {
+            real v = o[i];
+            v *= c;
+            v += u1[i];
+            v *= 1. / 3.;
+            v += u0[i];
+            v *= 3. / 4.;
+            same = same && got[i] == v;
+        }
+        EXPECT_TRUE(same);
+        // MeanVariance's second moment: addPower(u, 2), then subtractPower(mean, 2)
+        Volume sq("burgers", n, 2);
+        sq.getScalarMemoryArea(0).addPower(U1.getScalarMemoryArea(0), 2);
+        sq.getScalarMemoryArea(0).subtractPower(U0.getScalarMemoryArea(0), 2);
+        const auto q = sq.toHost();
+        bool ok = true;
+        for (size_t i = 0; i < total; ++i) ok = ok && q[i] == (0.0 + u1[i] * u1[i]) - u0[i] * u0[i];
+        EXPECT_TRUE(ok);
     });
 
     std::printf("%d checks, %d failures\n", g_checks, g_failures);

@@ -69,6 +69,51 @@ def flux_cases():
     np.savez_compressed(os.path.join(HERE, "flux.npz"), **out)
 
 
+def region_cases():
+    """Region calls of the reference's NumericalFlux (start / end), the calls
+    ConservedSystem makes for the interior and the side strips plus boxes of
+    other shapes; `out` starts from one random fill per case (out0), which
+    cells outside the region keep."""
+    rng = np.random.default_rng(20240615)
+    out = {}
+    cases = [("euler1", "hll3", "weno2", (24, 1, 1)), ("burgers", "godunov", "eno3", (21, 1, 1)),
+             ("euler2", "hll3", "weno2", (14, 11, 1)), ("euler2", "hll", "eno2", (12, 10, 1)),
+             ("euler3", "hll3", "weno2", (8, 7, 6))]
+    for eq, fl, rc, n in cases:
+        g = workloads.ghost_cells(rc)
+        dim = workloads.dimension(n)
+        t = padded_shape(n, g)
+        U = workloads.smooth_random_state(eq, t, rng)
+        o0 = rng.uniform(-1, 1, U.shape)
+        regions = [([g if d < dim else 0 for d in range(3)], [-g if d < dim else 0 for d in range(3)])]
+        for d in range(dim):
+            # ConservedSystem's strips (ConservedSystem.cpp:67-96), in interior coordinates
+            hi = [0, 0, 0]
+            hi[d] = -n[d] + g
+            regions.append(([0, 0, 0], hi))
+            lo = [0, 0, 0]
+            lo[d] = n[d] - g
+            regions.append((lo, [0, 0, 0]))
+        regions.append(([1 if d < dim else 0 for d in range(3)], [-2 if d < dim else 0 for d in range(3)]))
+        regions.append(([0, 0, 0], [0, 0, 0]))
+        case = f"{eq}_{fl}_{rc}"
+        out[case + "_U"] = U
+        out[case + "_out0"] = o0
+        out[case + "_n"] = np.array(n)
+        out[case + "_regions"] = np.array(len(regions))
+        for k, (lo, hi) in enumerate(regions):
+            o = o0.copy()
+            ws = (D * 3)()
+            check(R.ref_compute_flux_region(eq.encode(), fl.encode(), rc.encode(), i3(n), D(1.4), P(U), P(o), ws,
+                                            i3(lo), i3(hi)))
+            key = f"{case}_{k}"
+            out[key + "_out"] = o
+            out[key + "_ws"] = np.array(list(ws))
+            out[key + "_start"] = np.array(lo)
+            out[key + "_end"] = np.array(hi)
+    np.savez_compressed(os.path.join(HERE, "flux_region.npz"), **out)
+
+
 def extra_flux_combinations():
     """(equation, flux, reconstruction) pairs beyond the base set: the extra
     fluxes with every reconstruction, the limiters with every base flux."""
@@ -273,6 +318,7 @@ elif __name__ == "__main__":
     generator_cases()
     generator_sequence_cases()
     flux_cases()
+    region_cases()
     flux_extra_cases()
     structure_cases()
     structure_basic_cases()

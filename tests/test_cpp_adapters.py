@@ -38,6 +38,46 @@ def test_adapters_pass_their_tests(cuda_device, tmp_path):
     assert "ALL PASSED" in r.stdout
 
 
+PLATFORM = os.path.join(ROOT, "tests", "cpp", "test_alsvinn_platform.cpp")
+REFBUILD = os.path.join(ROOT, "oracle", "refbuild")
+REF_LIB = os.path.join(ROOT, "oracle", "_ref")
+
+
+def reference_root():
+    """The reference sources: REF_ROOT, else the location the reference
+    recipe names; None where they are absent (as on the GPU machine)."""
+    ref = os.environ.get("REF_ROOT")
+    if not ref:
+        p = subprocess.run(["make", "-s", "--no-print-directory", "-C", REFBUILD, "print-ref"], capture_output=True,
+                           text=True)
+        ref = p.stdout.strip() if p.returncode == 0 else ""
+    return ref if ref and os.path.isdir(os.path.join(ref, "alsfvm", "include")) else None
+
+
+def test_platform_classes_build_against_the_reference(tmp_path):
+    """include/gbfv_alsvinn.hpp's classes derive from the reference's own
+    Memory<real>, NumericalFlux, Reconstruction, Boundary and CellComputer:
+    compiled against the reference's headers (with the oracle build's
+    stand-ins for Boost and MPI) and linked with the reference's CPU library
+    and libgbfv.so, every pure virtual is implemented with its signature."""
+    ref = reference_root()
+    if ref is None or not os.path.exists(os.path.join(REF_LIB, "libalsref.so")):
+        pytest.skip("the reference's sources or its CPU build are absent")
+    cxx = shutil.which("g++") or "g++"
+    lib = os.path.join(ROOT, "alsvinn_gb300", "lib")
+    exe = str(tmp_path / "test_alsvinn_platform")
+    cmd = [cxx, "-std=c++17", "-O1", "-fopenmp", "-I" + os.path.join(REFBUILD, "stubs"),
+           "-I" + os.path.join(ref, "alsfvm", "include"), "-I" + os.path.join(ref, "alsutils", "include"),
+           "-I" + os.path.join(ref, "alsuq", "include"), "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(CUDA, "include"), PLATFORM, "-o", exe, "-L" + REF_LIB, "-lalsref", "-L" + lib, "-lgbfv",
+           "-L" + os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath," + REF_LIB, "-Wl,-rpath," + lib,
+           "-Wl,-rpath," + os.path.join(CUDA, "lib64")]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "linked" in r.stdout, r.stdout + r.stderr
+
+
 SPECIAL = os.path.join(ROOT, "tests", "cpp", "test_special_functions.cu")
 
 

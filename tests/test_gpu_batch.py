@@ -1,10 +1,13 @@
 """The ensemble engine (gbfv_batch_*): members of mixed grid sizes advanced
-together with their own dt must equal single-grid solves; their statistics
-must equal alsuq's MeanVariance over the same samples (the oracle); the FP32
-ensemble's mean must stay within 1e-4 of the FP64 oracle and its variance
-within 1e-2 (L1 errors scaled by the variable's or the density's L1 norm);
-admission follows the memory pool; a member's result is the same alone and in
-a mix."""
+together with their own dt and their own end times must equal single-grid
+solves; their statistics must equal alsuq's MeanVariance over the same
+samples (the oracle), and the FP32 ensemble's statistics the mean / variance
+of FP32 single-grid solves; against the FP64 oracle the FP32 ensemble's mean
+stays within 1e-4 and its variance within 1e-2 over a short run (L1 errors
+scaled by the variable's or the density's L1 norm); a member whose state
+breaks the constraints stops alone and stays out of the statistics;
+admission follows the memory pool; a member's result is the same alone and
+in a mix."""
 import numpy as np
 import pytest
 
@@ -61,6 +64,81 @@ def test_members_have_their_own_dt(cuda_device):
         (ta, sa), (tc, sc) = b.member_time(a), b.member_time(c)
         assert ta == tc == 0.02
         assert sc > sa  # the finer grid takes more, smaller steps
+
+
+def test_members_have_their_own_end_times(cuda_device):
+    members = [(32, 0.01, 0), (48, 0.02, 1), (32, 0.03, 2), (40, 0.015, 3)]
+    with kh_batch() as b:
+        slots = []
+        for n, T, k in members:
+            slot = b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, k))
+            b.set_member_end(slot, T, 1)
+            slots.append(slot)
+        b.advance(1.0, 0)
+        for slot, (n, T, k) in zip(slots, members):
+            t, steps = b.member_time(slot)
+            ref, t_ref, steps_ref = solo(n, kh_member(n, k), T, 1)
+            assert t == t_ref == T
+            assert steps == steps_ref
+            assert np.array_equal(b.member_state(slot, (n + 4) ** 2), ref)
+    with kh_batch() as b:
+        slot = b.add((32, 32, 1), KH["lower"], KH["upper"], kh_member(32, 0))
+        b.set_member_end(slot, 0.03, 1)
+        b.advance(0.01, 0)
+        t = b.member_time(slot)[0]
+        assert 0.01 <= t < 0.03  # the advance's end time still bounds every member
+
+
+def test_a_failing_member_stops_alone(cuda_device):
+    # a negative pressure patch (set on the host) breaks the constraint check
+    # of one member in its first step; the others run to the end time with
+    # the bits of their single-grid solves and only they are folded into the
+    # statistics
+    n, T = 48, 0.02
+    bad = kh_member(n, 9).reshape(4, n, n).copy()
+    bad[3, 10:20, 30:40] = -0.5
+    with kh_batch() as b:
+        good = [b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, k), group=0) for k in range(3)]
+        sb = b.add((n, n, 1), KH["lower"], KH["upper"], bad.reshape(4, -1), group=0)
+        with pytest.raises(lib.GbfvError) as e:
+            b.advance(T, 1)
+        assert e.value.code == lib.ERR_CONSTRAINT
+        assert b.member_status(sb) == (1, 1)
+        assert all(b.member_status(s) == (0, 0) for s in good)
+        mean, var, count = b.stats(0, (n + 4) ** 2)
+        states = []
+        for k, slot in enumerate(good):
+            ref, t_ref, _ = solo(n, kh_member(n, k), T, 1)
+            assert b.member_time(slot)[0] == t_ref == T
+            U = b.member_state(slot, (n + 4) ** 2)
+            assert np.array_equal(U, ref)
+            states.append(U)
+    assert count == 3
+    with kh_batch() as b:
+        for k in range(3):
+            b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, k), group=0)
+        b.advance(T, 1)
+        mean_ok, var_ok, count_ok = b.stats(0, (n + 4) ** 2)
+    assert count_ok == 3
+    assert np.array_equal(mean, mean_ok) and np.array_equal(var, var_ok)
+
+
+def test_fp32_ensemble_statistics_equal_fp32_solo_solves(cuda_device):
+    # isolates the ensemble engine: the FP64 Welford statistics of FP32
+    # members against a two-pass mean / variance of the FP32 single-grid
+    # solves of the same samples
+    n, M, T = 128, 6, 0.05
+    with kh_batch(precision=lib.FP32) as b:
+        for s in range(M):
+            b.add((n, n, 1), KH["lower"], KH["upper"], kh_member(n, s), group=0)
+        b.advance(T, 1)
+        mean, var, count = b.stats(0, (n + 4) ** 2)
+    assert count == M
+    X = np.stack([solo(n, kh_member(n, s), T, 1, precision=lib.FP32)[0] for s in range(M)])
+    m_ref = X.mean(axis=0)
+    v_ref = ((X - m_ref) ** 2).mean(axis=0)
+    assert (var_error(mean, m_ref) <= 1e-13).all(), var_error(mean, m_ref)
+    assert (var_error(var, v_ref) <= 1e-11).all(), var_error(var, v_ref)
 
 
 def var_error(var, v_ref):

@@ -101,19 +101,19 @@ def kh_parameters(X):
 
 def kh_prim(n, X):
     """Kelvin-Helmholtz on [0,1]^2: rho=2, u=-0.5 inside 0.25+d1(x) < y < 0.75+d2(x),
-    rho=1, u=0.5 outside; v=0, p=2.5."""
+    rho=1, u=0.5 outside; v=0, p=2.5. The interface heights come from math.cos
+    per column; the inside test is a comparison of doubles, done for all rows
+    at once (numpy's addition and comparison are the IEEE operations)."""
     a1, b1, a2, b2 = kh_parameters(X)
     xs, ys, _ = midpoints((n, n, 1), (0, 0, 0), (1, 1, 0))
-    d1 = [kh_perturbation(x, a1, b1) for x in xs]
-    d2 = [kh_perturbation(x, a2, b2) for x in xs]
+    lo = 0.25 + np.array([kh_perturbation(x, a1, b1) for x in xs])
+    hi = 0.75 + np.array([kh_perturbation(x, a2, b2) for x in xs])
+    y = np.array(ys)[:, None]
+    inside = ((lo[None, :] < y) & (y < hi[None, :])).ravel()
     prim = np.zeros((4, n * n))
-    for j, y in enumerate(ys):
-        for i in range(n):
-            inside = (0.25 + d1[i] < y) and (y < 0.75 + d2[i])
-            k = j * n + i
-            prim[0, k] = 2.0 if inside else 1.0
-            prim[1, k] = -0.5 if inside else 0.5
-            prim[3, k] = 2.5
+    prim[0] = np.where(inside, 2.0, 1.0)
+    prim[1] = np.where(inside, -0.5, 0.5)
+    prim[3] = 2.5
     return prim
 
 
