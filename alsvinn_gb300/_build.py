@@ -30,6 +30,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + C
 VARIANTS = (0, 1, 2, 3)   # fp64, fp64 exact, fp32, fp64 state with double-float arithmetic
 EQUATIONS = (0, 1, 2, 3)  # burgers, euler1, euler2, euler3
 TUNED_VARIANTS = (0, 1, 2, 3)  # variants with autotuning candidates (all; TMA where storage = arithmetic type)
+REGION_VARIANTS = (0, 1, 2)  # variants with region kernels (operator calls on part of the grid)
 
 
 def _nvcc():
@@ -53,6 +54,8 @@ def _units():
             units.append(("fv_variant.cu", "fv_v%d_e%d.o" % (v, e), flags + ["-DFV_PART=0"]))
             if v in TUNED_VARIANTS:
                 units.append(("fv_variant.cu", "fv_v%d_e%d_tune.o" % (v, e), flags + ["-DFV_PART=1"]))
+            if v in REGION_VARIANTS:
+                units.append(("fv_variant.cu", "fv_v%d_e%d_region.o" % (v, e), flags + ["-DFV_PART=2"]))
     units.append(("gbfv_tune.cu", "gbfv_tune.o", []))
     units.append(("gbfv_api.cu", "gbfv_api.o", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]))
     units.append(("gbfv_stats.cu", "gbfv_stats.o", []))

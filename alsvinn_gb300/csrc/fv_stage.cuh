@@ -537,9 +537,11 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
 // into su and, for the stage-1 modes, that of L0 into l0s, both signalling
 // bar. `global_maps`: the maps live in global memory, written by the host.
 template <class R, class SL, int DIM>
+// `extra_tx`: bytes announced on top of the copies' (0; a test of the bounded
+// wait's error path announces more than arrives, so the wait runs out).
 __device__ __forceinline__ void tma_stage_issue(const StageArgs& A, const CUtensorMap* tm_in, const CUtensorMap* tm_l0,
                                                 const int* org, R* su, R* l0s, unsigned long long* bar,
-                                                bool global_maps) {
+                                                bool global_maps, unsigned extra_tx = 0) {
     const bool s1 = A.mode == MODE_RK3_S1 || A.mode == MODE_RK2_S1;
     if (global_maps) {
         fence_tensormap_acquire(tm_in);
@@ -547,7 +549,7 @@ __device__ __forceinline__ void tma_stage_issue(const StageArgs& A, const CUtens
     }
     // earlier generic accesses of su / l0s (the previous tile) before the copies
     fence_proxy_async_smem();
-    mbar_arrive_expect_tx(bar, (unsigned)((s1 ? 2 : 1) * SL::box_bytes));
+    mbar_arrive_expect_tx(bar, (unsigned)((s1 ? 2 : 1) * SL::box_bytes) + extra_tx);
     tma_load_halo<DIM>(su, tm_in, bar, org[0], org[1], org[2]);
     if (s1) tma_load_halo<DIM>(l0s, tm_l0, bar, org[0], org[1], org[2]);
 }
@@ -636,7 +638,7 @@ __global__ void __launch_bounds__(NTH, MINB) stage_kernel_tma(StageArgs A, const
     const int org[3] = {(int)blockIdx.x * TX, (int)blockIdx.y * TY, (int)blockIdx.z * TZ};
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
-    if (threadIdx.x == 0) tma_stage_issue<R, SL, DIM>(A, &M.in, &M.l0, org, su, work, &bar, false);
+    if (threadIdx.x == 0) tma_stage_issue<R, SL, DIM>(A, &M.in, &M.l0, org, su, work, &bar, false, A.tma_extra_tx);
     if (!tma_stage_finish<R, SL, NTH>(A, su, work, &bar, 0)) return;
     stage_tile_compute<R, EQ, FLUX, RC, DIM, TX, TY, TZ, NTH, R>(A, org, su, work, wred);
 }

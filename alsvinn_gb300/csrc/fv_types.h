@@ -201,6 +201,9 @@ struct StageArgs {
     int rhi[3];
     const void* vin[5];
     void* vout[5];
+    // single-grid TMA stages: bytes announced on the halo barrier beyond the
+    // copies' (0; nonzero only in a test of the bounded wait's error path)
+    unsigned tma_extra_tx;
 };
 
 // Reconstruction of one direction over the reference's cell range

@@ -35,13 +35,14 @@ typedef Real Compute;
 #endif
 
 #ifndef FV_PART
-#define FV_PART 0  // 0: default candidates and the other launchers, 1: autotuning candidates
+#define FV_PART 0  // 0: default candidates and the other launchers, 1: autotuning candidates, 2: region kernels
 #endif
 
 #define FV_CAT2(a, b, c, d) a##b##c##d
 #define FV_CAT(a, b, c, d) FV_CAT2(a, b, c, d)
 #define FV_REGISTER_FN FV_CAT(gbfv_register_v, FV_VARIANT, _e, FV_EQ)
 #define FV_TUNE_FN FV_CAT(gbfv_tune_v, FV_VARIANT, _e, FV_EQ)
+#define FV_REGION_FN FV_CAT(gbfv_region_v, FV_VARIANT, _e, FV_EQ)
 
 namespace gbfv {
 namespace GBFV_VARIANT_NS {
@@ -221,9 +222,7 @@ static int launch_check(const CheckArgs& a, cudaStream_t s) {
 template <int FLUX, int RC, int DIM>
 static void reg_one(Registry& R) {
     using TS = TileShape<DIM, FV_VARIANT>;
-    using C0 = Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>;
-    C0::add(R, FLUX, RC);
-    R.region[FV_VARIANT][FV_EQ][FLUX][RC][DIM - 1] = &C0::launch_region;
+    Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>::add(R, FLUX, RC);
 }
 
 // Every reconstruction for one flux in one dimension. The double-float
@@ -242,6 +241,31 @@ static void reg_dim(Registry& R) {
 #if FV_EQ != 0
     reg_one<FLUX, RC_WENOF2, DIM>(R);
 #endif
+#endif
+}
+#elif FV_PART == 2
+// The region kernels (the operator on part of the grid, for the
+// reference's NumericalFlux::computeFlux with start / end) of every scheme
+// with the default candidate's tile; their own translation units so they
+// compile in parallel with the stage kernels.
+template <int FLUX, int RC, int DIM>
+static void reg_region_one(Registry& R) {
+    using TS = TileShape<DIM, FV_VARIANT>;
+    using C0 = Cand<FV_EQ, FLUX, RC, DIM, TS::X, TS::Y, TS::Z, TS::THREADS, false, (DIM == 2 ? 3 : 1)>;
+    R.region[FV_VARIANT][FV_EQ][FLUX][RC][DIM - 1] = &C0::launch_region;
+}
+
+template <int FLUX, int DIM>
+static void reg_region_dim(Registry& R) {
+    reg_region_one<FLUX, RC_NONE, DIM>(R);
+    reg_region_one<FLUX, RC_WENO2, DIM>(R);
+    reg_region_one<FLUX, RC_ENO2, DIM>(R);
+    reg_region_one<FLUX, RC_ENO3, DIM>(R);
+    reg_region_one<FLUX, RC_ENO4, DIM>(R);
+    reg_region_one<FLUX, RC_MC, DIM>(R);
+    reg_region_one<FLUX, RC_MM, DIM>(R);
+#if FV_EQ != 0
+    reg_region_one<FLUX, RC_WENOF2, DIM>(R);
 #endif
 }
 #else
@@ -335,6 +359,29 @@ extern "C" void FV_REGISTER_FN(gbfv::Registry* R) {
     R->recon[V][E][RC_MM] = &launch_recon<E, RC_MM>;
 #if FV_EQ != 0
     R->recon[V][E][RC_WENOF2] = &launch_recon<E, RC_WENOF2>;
+#endif
+}
+#elif FV_PART == 2
+extern "C" void FV_REGION_FN(gbfv::Registry* R) {
+    using namespace gbfv;
+    using namespace gbfv::GBFV_VARIANT_NS;
+#if FV_EQ == 0
+    reg_region_dim<FL_GODUNOV, 1>(*R);
+    reg_region_dim<FL_GODUNOV, 2>(*R);
+    reg_region_dim<FL_GODUNOV, 3>(*R);
+    reg_region_dim<FL_CENTRAL, 1>(*R);
+    reg_region_dim<FL_CENTRAL, 2>(*R);
+    reg_region_dim<FL_CENTRAL, 3>(*R);
+    reg_region_dim<FL_RUSANOV, 1>(*R);
+    reg_region_dim<FL_RUSANOV, 2>(*R);
+    reg_region_dim<FL_RUSANOV, 3>(*R);
+    reg_region_dim<FL_ROE, 1>(*R);
+    reg_region_dim<FL_ROE, 2>(*R);
+    reg_region_dim<FL_ROE, 3>(*R);
+#else
+    reg_region_dim<FL_HLL, FV_EQ>(*R);
+    reg_region_dim<FL_HLL3, FV_EQ>(*R);
+    reg_region_dim<FL_CENTRAL, FV_EQ>(*R);
 #endif
 }
 #else

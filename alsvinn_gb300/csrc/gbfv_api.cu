@@ -27,6 +27,10 @@ GBFV_TUNE_DECL(0, 0) GBFV_TUNE_DECL(0, 1) GBFV_TUNE_DECL(0, 2) GBFV_TUNE_DECL(0,
 GBFV_TUNE_DECL(1, 0) GBFV_TUNE_DECL(1, 1) GBFV_TUNE_DECL(1, 2) GBFV_TUNE_DECL(1, 3)
 GBFV_TUNE_DECL(2, 0) GBFV_TUNE_DECL(2, 1) GBFV_TUNE_DECL(2, 2) GBFV_TUNE_DECL(2, 3)
 GBFV_TUNE_DECL(3, 0) GBFV_TUNE_DECL(3, 1) GBFV_TUNE_DECL(3, 2) GBFV_TUNE_DECL(3, 3)
+#define GBFV_REGION_DECL(v, e) extern "C" void gbfv_region_v##v##_e##e(gbfv::Registry*);
+GBFV_REGION_DECL(0, 0) GBFV_REGION_DECL(0, 1) GBFV_REGION_DECL(0, 2) GBFV_REGION_DECL(0, 3)
+GBFV_REGION_DECL(1, 0) GBFV_REGION_DECL(1, 1) GBFV_REGION_DECL(1, 2) GBFV_REGION_DECL(1, 3)
+GBFV_REGION_DECL(2, 0) GBFV_REGION_DECL(2, 1) GBFV_REGION_DECL(2, 2) GBFV_REGION_DECL(2, 3)
 
 namespace gbfv {
 
@@ -44,6 +48,10 @@ Registry& registry() {
         gbfv_tune_v1_e0(r); gbfv_tune_v1_e1(r); gbfv_tune_v1_e2(r); gbfv_tune_v1_e3(r);
         gbfv_tune_v2_e0(r); gbfv_tune_v2_e1(r); gbfv_tune_v2_e2(r); gbfv_tune_v2_e3(r);
         gbfv_tune_v3_e0(r); gbfv_tune_v3_e1(r); gbfv_tune_v3_e2(r); gbfv_tune_v3_e3(r);
+        // region kernels of the operator-level calls (no double-float variant)
+        gbfv_region_v0_e0(r); gbfv_region_v0_e1(r); gbfv_region_v0_e2(r); gbfv_region_v0_e3(r);
+        gbfv_region_v1_e0(r); gbfv_region_v1_e1(r); gbfv_region_v1_e2(r); gbfv_region_v1_e3(r);
+        gbfv_region_v2_e0(r); gbfv_region_v2_e1(r); gbfv_region_v2_e2(r); gbfv_region_v2_e3(r);
         return r;
     }();
     return *R;
@@ -236,6 +244,7 @@ struct gbfv_solver {
     bool tm_ok = false;
     std::vector<double> tune_ms;  // the autotuner's MODE_L time per candidate (-1: not eligible)
     void* op_block = nullptr;     // scratch of the per-variable operator calls (allocated at first use)
+    unsigned tma_extra_tx = 0;    // gbfv_test_tma_wait_limit: extra bytes announced on the halo barrier
     // kGraphSteps time steps captured as one CUDA graph, replayed for the
     // long stretches of an advance (valid for graph_params and graph_cand)
     cudaGraphExec_t step_graph = nullptr;
@@ -507,6 +516,7 @@ static StageArgs stage_args(gbfv_solver* s, StepState* st, const void* in, const
     a.mode = mode;
     a.periodic = s->periodic;
     a.check = check;
+    a.tma_extra_tx = s->tma_extra_tx;
     return a;
 }
 
@@ -714,6 +724,8 @@ static int use_candidate(gbfv_solver* s, int idx) {
 // current state (out = L, a scratch step state: no effect on the solve) and
 // keeps the fastest; the choice is cached per scheme and grid for the
 // process. GBFV_AUTOTUNE=0 in the environment keeps candidate 0.
+constexpr long long kTuneFloorCells = 4096;
+
 static int tune(gbfv_solver* s, bool force) {
     int n = 0;
     const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &n);
@@ -723,6 +735,11 @@ static int tune(gbfv_solver* s, bool force) {
              s->G.n[1], s->G.n[2]);
     int best = 0;
     if (n <= 1 || !gbfv_autotune_enabled()) return use_candidate(s, 0);
+    // grids below kTuneFloorCells interior cells launch a handful of CTAs per
+    // stage: every candidate times the same within the launch latency, and
+    // timing them would cost more launches than a short solve makes
+    const long long cells = (long long)s->G.n[0] * s->G.n[1] * s->G.n[2];
+    if (!force && cells < kTuneFloorCells) return use_candidate(s, 0);
     if (!force && gbfv_tune_cache_get(key, &best) && best < n && try_candidate(s, best)) return GBFV_OK;
     StepState z;
     std::memset(&z, 0, sizeof z);
@@ -1300,6 +1317,19 @@ int gbfv_max_wave_speed_vars(gbfv_solver* s, const void* const* cons_vars, int d
     return cells_launch(s, 2, cons_vars, nullptr, direction, speed, stream);
 }
 
+int gbfv_test_tma_wait_limit(gbfv_solver* s, unsigned extra_bytes) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->tma_extra_tx = extra_bytes;
+    // captured step graphs hold the old launch parameters
+    if (s->step_graph) {
+        cudaGraphExecDestroy(s->step_graph);
+        s->step_graph = nullptr;
+        s->graph_cand = -2;
+    }
+    return GBFV_OK;
+}
+
 // ------------------------------------------------------- generator
 
 // The process-wide engine of STLMersenne as an object: one mt19937_64 with
@@ -1413,6 +1443,7 @@ int gbfv_internal_step(const GbfvPlan& p, void* U, void* V, void* L, StepState* 
     auto stage = [&](const StageArgs& a, cudaStream_t qq) { return launch0(a, nullptr, qq); };
     auto args = [&](const void* in, const void* u0, const void* l0, void* out, int mode, int check) {
         StageArgs a;
+        std::memset(&a, 0, sizeof a);
         a.in = in; a.u0 = u0; a.l0 = l0; a.out = out; a.st = st; a.G = p.G; a.gamma = p.gamma;
         a.gamma_f = (float)p.gamma;
         a.tm_in = nullptr; a.tm_l0 = nullptr;

@@ -9,9 +9,11 @@
 // allocates; this entry point takes them from one file-scope device array of
 // GBFV_NOALLOC_SCRATCH_BYTES instead. Every GPU that loads the library holds
 // that array until the process exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "fv_registry.h"
@@ -23,10 +25,47 @@ using namespace gbfv;
 // second state buffer V, each at a 256-byte boundary.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBFV_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device, looked up once per device
-// (host code may not take the address of a __device__ array directly: in host
-// code the name is a host-side stand-in).
-static void* g_scratch_address[256];
+// Device address of g_noalloc_scratch per device, looked up at the first call
+// on the device (host code may not take the address of a __device__ array
+// directly: in host code the name is a host-side stand-in). The address
+// belongs to the device's context: it is kept with that context's unique id
+// and looked up again when the current context is another one (after a
+// cudaDeviceReset, for instance). Calls from several host threads share the
+// table under a mutex.
+struct ScratchAddress {
+    unsigned long long context_id = 0;
+    void* ptr = nullptr;
+};
+static ScratchAddress g_scratch_address[256];
+static std::mutex g_scratch_mutex;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// The unique id of the calling thread's current context (0: unknown).
+static unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (CtxGetCurrentFn) nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    static CtxGetIdFn get_id = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (CtxGetIdFn) nullptr;
+        return reinterpret_cast<CtxGetIdFn>(p);
+    }();
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -52,16 +91,25 @@ extern "C" int gbfv_advance_noalloc(const gbfv_desc* desc, void* state_dev, doub
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess || device < 0 || device >= 256)
         return gbfv_internal_fail(GBFV_ERR_CUDA, "gbfv_advance_noalloc: no current CUDA device");
-    // set-up, once per device, with that device current
-    if (!g_scratch_address[device]) {
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            return gbfv_internal_fail(GBFV_ERR_CUDA, (std::string("gbfv_advance_noalloc: cudaGetSymbolAddress: ") +
-                                                      cudaGetErrorString(e)).c_str());
-        g_scratch_address[device] = ptr;
+    // set-up, at the first call on a device (and again in a new context of
+    // it), with that device current
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        ScratchAddress& a = g_scratch_address[device];
+        const unsigned long long id = current_context_id();
+        if (!a.ptr || id == 0 || id != a.context_id) {
+            void* ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+                return gbfv_internal_fail(GBFV_ERR_CUDA,
+                                          (std::string("gbfv_advance_noalloc: cudaGetSymbolAddress: ") +
+                                           cudaGetErrorString(e)).c_str());
+            a.ptr = ptr;
+            a.context_id = id;
+        }
+        base = static_cast<unsigned char*>(a.ptr);
     }
-    unsigned char* base = static_cast<unsigned char*>(g_scratch_address[device]);
     StepState* st = reinterpret_cast<StepState*>(base);
     void* L = base + round256(sizeof(StepState));
     void* V = base + round256(sizeof(StepState)) + round256(state_bytes);

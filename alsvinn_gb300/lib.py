@@ -158,6 +158,7 @@ _SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "gbfv_init_burgers_sine": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_void_p]),
+    "gbfv_test_tma_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint]),
     "gbfv_memory_op": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int,
                                       ctypes.c_void_p]),
     "gbfv_memory_op_scalar": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong,
@@ -520,6 +521,11 @@ class Solver:
         ok = ctypes.c_int()
         _check(load().gbfv_obeys_constraints(self.h, ctypes.c_void_p(state_dev), ctypes.byref(ok)))
         return bool(ok.value)
+
+    def test_tma_wait_limit(self, extra_bytes):
+        """Test hook: TMA halo waits of this solver's stage launches run out
+        their time limit (see gbfv_test_tma_wait_limit); 0 restores."""
+        _check(load().gbfv_test_tma_wait_limit(self.h, int(extra_bytes)))
 
     # one device array per variable (a reference Volume's layout)
     def compute_flux_region(self, state_vars, out_vars, start=(0, 0, 0), end=(0, 0, 0), stream=None):

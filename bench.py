@@ -254,7 +254,9 @@ def run_gpu(args):
     from alsvinn_gb300 import lib
 
     prim = kh_initial_primitives(N, sample=rank)
-    precision = {"fp64": lib.FP64, "fp64-df": lib.FP64_DF, "fp64-exact": lib.FP64_EXACT}[args.precision]
+    precision = {"fp64": lib.FP64, "fp64-df": lib.FP64_DF, "fp64-exact": lib.FP64_EXACT, "fp32": lib.FP32}[
+        args.precision]
+    elem = 4 if args.precision == "fp32" else 8
     s = lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0), (1, 1, 0),
                    gamma=1.4, cfl=0.4, precision=precision)
     s.set_primitive(prim)
@@ -329,7 +331,7 @@ def run_gpu(args):
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    state_bytes = NVAR * s.total * 8
+    state_bytes = NVAR * s.total * 8  # gbfv_advance_host moves the FP64 host state
     e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes, "steps": e2e_steps}
 
@@ -368,7 +370,7 @@ def run_gpu(args):
 
     peak, peak_kind = measured_peaks()
     per_launch_ms = stage_ms / max(stage_launches, 1)
-    alg_bytes_per_launch = cells * BYTES_PER_CELL_STEP / 3.0
+    alg_bytes_per_launch = cells * (8 * NVAR * elem) / 3.0
     achieved = alg_bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profile_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
@@ -394,7 +396,7 @@ def run_gpu(args):
         base = cpu_baseline(args.cpu_steps) if world == 1 else None
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if elem == 4 else "f64",
                 "data": "synthetic (seeded KH interface perturbation, sample = rank)",
                 "config": headline_config(args.precision), "stage_kernel": stage_kernel,
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clk,
@@ -414,6 +416,62 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_tg(args):
+    """Taylor-Green (euler3, WENO2, HLL3, SSP-RK3, CFL 0.4, periodic on
+    [0, 2 pi]^3) on n^3 cells: `--warmup` steps, then `--steps` timed steps
+    with CUDA events on the solver's stream (the L2 flushed before each);
+    the autotuner's table, or `--candidate` pinned (profiler runs)."""
+    import math
+    import torch
+    from alsvinn_gb300 import lib
+
+    n = args.tg_n
+    precision = {"fp64": lib.FP64, "fp32": lib.FP32, "fp64-df": lib.FP64_DF, "fp64-exact": lib.FP64_EXACT}[
+        args.precision]
+    s = lib.Solver("euler3", "hll3", "weno2", "rungekutta3", "periodic", (n, n, n), (0, 0, 0), (2 * math.pi,) * 3,
+                   gamma=1.4, cfl=0.4, precision=precision)
+    s.set_primitive(lib.init_taylor_green(n))
+    cands = s.candidates()
+    if args.candidate >= 0:
+        s.select_candidate(args.candidate)
+        chosen, tune_ms = args.candidate, [-1.0] * len(cands)
+    else:
+        chosen, tune_ms = s.autotune()
+    s.advance(1e9, 0, args.warmup)
+    stream = torch.cuda.ExternalStream(s.stream())
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    s.profile(True)
+    s.profile_read()
+    total = 0.0
+    with ClockSampler(0) as clocks:
+        for i in range(args.steps):
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)
+                a0.record(stream)
+            s.advance(1e9, 0, 1)
+            with torch.cuda.stream(stream):
+                a1.record(stream)
+            torch.cuda.synchronize()
+            total += a0.elapsed_time(a1)
+    stage_ms, stage_n, _ = s.profile_read()
+    s.close()
+    cells = n ** 3
+    line = {"metric": METRIC, "value": cells * args.steps / (total * 1e-3), "unit": METRIC, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic (Taylor-Green initial data)",
+            "config": {"workload": "tg3d_%d_euler3_weno2_hll3_rk3" % n, "grid": [n, n, n],
+                       "precision": args.precision, "l2": "flushed before every timed step (512 MiB memset)"},
+            "stage_kernel": {"candidate": chosen, "tile": list(cands[chosen][0]), "threads": cands[chosen][1],
+                             "tma": cands[chosen][2],
+                             "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
+                                                        for c, m in zip(cands, tune_ms)]},
+            "stage_launch_ms": stage_ms / max(stage_n, 1), "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
 
 
 UQ_SIZES = (128, 256, 512)
@@ -544,7 +602,44 @@ def measure_uq(S, plain_per_size, warmup, candidate=-1):
             "gpu_launches": int(launches), "clocks": clocks.summary()}
 
 
+def run_uq_steps(args):
+    """A fixed number of ensemble steps (profiler runs): the first
+    `--uq-samples` members, `--warmup` steps, then `--uq-steps` timed steps."""
+    import torch
+    from alsvinn_gb300 import lib
+
+    S = args.uq_samples
+    sizes = uq_sizes(S)
+    probe = lib.Batch(*UQ_SCHEME, 1 << 20, 1, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    pool = sum(probe.member_bytes((int(n), int(n), 1)) for n in sizes) + (64 << 20)
+    probe.close()
+    b = lib.Batch(*UQ_SCHEME, pool, S, gamma=1.4, cfl=0.4, precision=lib.FP32)
+    if args.candidate >= 0:
+        b.select_candidate(args.candidate)
+    for i, n in enumerate(sizes):
+        b.add((int(n), int(n), 1), (0, 0, 0), (1, 1, 0), lib.init_kelvin_helmholtz(int(n), sample=i),
+              group=UQ_SIZES.index(int(n)))
+    b.advance(UQ_T, 1, args.warmup)
+    stream = torch.cuda.ExternalStream(b.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.advance(UQ_T, 1, args.uq_steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = float(sum(int(n) ** 2 for n in sizes))
+    cand, tma = b.current_candidate()
+    b.close()
+    print(json.dumps({"metric": "ensemble cell-updates/s", "value": cells * args.uq_steps / (ms * 1e-3),
+                      "unit": "cell-updates/s", "samples": S, "steps": args.uq_steps, "ms_per_step":
+                      ms / args.uq_steps, "candidate": cand, "members_staged_by_tma": tma}), flush=True)
+
+
 def run_uq(args):
+    if args.uq_steps > 0:
+        return run_uq_steps(args)
     r = measure_uq(args.uq_samples, args.uq_plain, args.warmup, args.candidate)
     line = {"metric": r["metric"], "value": r["value"], "unit": r["unit"], "n_gpus": 1, "steps": None,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
@@ -670,12 +765,13 @@ def serve_plain_fp64(reqs):
     come first served, each started no earlier than its arrival (real time)."""
     import torch
     from alsvinn_gb300 import lib
-    lat, steps = [], []
+    lat, steps, busy = [], [], []
     t0 = time.perf_counter()
     for (k, n, T, ph, sm, a) in reqs:
         now = time.perf_counter() - t0
         if now < a:
             time.sleep(a - now)
+        b0 = time.perf_counter()
         if k == lib.REQUEST_BURGERS:
             sv = lib.Solver("burgers", "godunov", "weno2", "rungekutta2", "periodic", (n, 1, 1), (0, 0, 0),
                             (1, 1, 1), cfl=0.475, precision=lib.FP64)
@@ -688,9 +784,10 @@ def serve_plain_fp64(reqs):
         torch.cuda.synchronize()
         steps.append(sv.time()[1])
         sv.close()
+        busy.append(time.perf_counter() - b0)
         lat.append(time.perf_counter() - t0 - a)
     wall = time.perf_counter() - t0
-    return wall, lat, steps
+    return wall, lat, steps, busy
 
 
 def measure_serve(R, rate, chunk, plain_subset):
@@ -707,10 +804,15 @@ def measure_serve(R, rate, chunk, plain_subset):
     sub = reqs[:plain_subset]
     swall, sres, _, sclk = serve_batched(sub, chunk)
     slat = np.array([r["finish"] - r["arrival"] for r in sres])
-    pwall, plat, _ = serve_plain_fp64(sub)
+    pwall, plat, _, pbusy = serve_plain_fp64(sub)
     plat = np.array(plat)
     sub_rate = len(sub) / swall
     plain_rate = len(sub) / pwall
+    # capacity: the same requests all present at t = 0 (batched: one run;
+    # plain: the sum of the measured one-at-a-time solve times)
+    cwall, cres, _, cclk = serve_batched([r[:5] + (0.0,) for r in sub], chunk)
+    cap_batched = len(sub) / cwall
+    cap_plain = len(sub) / sum(pbusy)
     kinds = {}
     for (k, n, T, ph, sm, a) in reqs:
         key = "%s_%d" % ("burgers1d" if k == 0 else "kh2d", n)
@@ -731,7 +833,11 @@ def measure_serve(R, rate, chunk, plain_subset):
                                              "latency_p99_s": float(np.percentile(plat, 99)),
                                              "method": "run: FP64 solver per request, FIFO, each started no "
                                                        "earlier than its arrival"},
-                "speedup_vs_plain_fp64": sub_rate / plain_rate},
+                "speedup_vs_plain_fp64": sub_rate / plain_rate,
+                "capacity": {"batched_fp32_samples_per_s": cap_batched, "plain_fp64_samples_per_s": cap_plain,
+                             "speedup": cap_batched / cap_plain, "clocks": cclk,
+                             "method": "the subset's requests all present at t = 0: batched wall time of one "
+                                       "run; plain = the sum of its measured one-at-a-time solve times"}},
             "gpu_launches": int(launches), "clocks": clk}
 
 
@@ -748,7 +854,8 @@ def run_serve(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="kh1024", choices=["kh1024", "uq", "serve", "uq-error"])
+    ap.add_argument("--workload", default="kh1024", choices=["kh1024", "uq", "serve", "uq-error", "tg"])
+    ap.add_argument("--tg-n", type=int, default=256, help="cells per dimension of --workload tg")
     ap.add_argument("--uq-error-members", type=int, default=8, help="members per grid size of --workload uq-error")
     ap.add_argument("--serve-requests", type=int, default=128)
     ap.add_argument("--serve-rate", type=float, default=2.0)
@@ -757,6 +864,8 @@ def main():
                     help="requests of the stream also run by plain FP64 one at a time")
     ap.add_argument("--uq-samples", type=int, default=4096)
     ap.add_argument("--uq-plain", type=int, default=2, help="plain FP64 solves to T per grid size")
+    ap.add_argument("--uq-steps", type=int, default=0,
+                    help="--workload uq: a fixed number of ensemble steps instead of the run to T (profiler runs)")
     ap.add_argument("--headline-uq-samples", type=int, default=192,
                     help="members of the UQ ensemble measured to T inside the default run (0: skip)")
     ap.add_argument("--headline-serve-requests", type=int, default=96,
@@ -766,7 +875,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=200)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64-df", "fp64-exact"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64-df", "fp64-exact", "fp32"])
     ap.add_argument("--no-df", action="store_true", help="skip the double-float measurement")
     ap.add_argument("--candidate", type=int, default=-1,
                     help="pin this stage kernel configuration instead of autotuning (profiler runs)")
@@ -781,6 +890,8 @@ def main():
         run_serve(args)
     elif args.workload == "uq-error":
         run_uq_error(args)
+    elif args.workload == "tg":
+        run_tg(args)
     else:
         run_gpu(args)
 

@@ -157,7 +157,9 @@ int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt);
  * box copies (tma = 1) or per-thread loads. Candidate 0 is the default. At
  * the first advance the autotuner times every eligible candidate on the
  * solver's state and keeps the fastest (cached per scheme and grid for the
- * process; GBFV_AUTOTUNE=0 in the environment keeps candidate 0). Every
+ * process; GBFV_AUTOTUNE=0 in the environment keeps candidate 0); grids of
+ * fewer than 4096 interior cells keep candidate 0 unless gbfv_autotune is
+ * called. Every
  * candidate gives bit-identical states. TMA candidates need padded rows
  * (t_x * element size) that are multiples of 16 bytes.
  *   gbfv_select_candidate: pin candidate idx (-1: back to the autotuner);
@@ -599,6 +601,19 @@ int gbfv_generator_destroy(gbfv_generator* g);
 int gbfv_generator_uniform(gbfv_generator* g, int dimension, int component, long long sample, double lower,
                            double upper, double* out);
 
+/* ------------------------------------------------- failure-path testing */
+
+/* Makes the solver's TMA-staged stage launches announce extra_bytes more on
+ * their halo barrier than their copies deliver (0 restores the normal
+ * launches). Every halo wait then runs out its time limit (about a second
+ * per CTA, twice), the kernel records status 2 in the step state and
+ * returns without writing, and the advance reports GBFV_ERR_CUDA; the
+ * copies themselves complete, the context stays usable and the solver's
+ * state is the one before the step. For tests of that error path only:
+ * nothing faults and nothing waits without a limit. No counterpart in the
+ * reference. */
+int gbfv_test_tma_wait_limit(gbfv_solver* s, unsigned extra_bytes);
+
 /* ----------------------------------------------- allocation-free stepping */
 
 /* Size of the library's built-in scratch array for gbfv_advance_noalloc. */
@@ -613,15 +628,21 @@ int gbfv_generator_uniform(gbfv_generator* g, int dimension, int component, long
  * The caller owns the padded device state (state_dev, nvar * total values of
  * desc->precision, ghosts filled), the stream (NULL: the default stream), the
  * time *t_inout and the step count *steps_inout, which the call advances like
- * gbfv_advance (same kernels, same results). Scratch -- the stage-0 flux
+ * gbfv_advance (the same results, bit for bit). It always runs the scheme's
+ * default stage kernels (candidate 0: per-thread halo loads; no tensor maps
+ * are encoded on the caller's buffers and nothing is autotuned), which on
+ * KH 1024^2 FP64 take 0.653 against 0.601 ms per stage launch of the tuned
+ * TMA candidate that gbfv_advance picks. Scratch -- the stage-0 flux
  * difference, the second state buffer and the step state -- comes from one
  * static device array of GBFV_NOALLOC_SCRATCH_BYTES that every GPU loading the
  * library holds until exit; grids needing more (2 * nvar * total * element
  * size plus under 1 KiB of step state and alignment) are rejected with GBFV_ERR_UNSUPPORTED. The call makes no
  * cudaMalloc, cudaFree or other allocating call.
  *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress) with that device current, and so does the first
+ *    call in a new context of the device (after a cudaDeviceReset); make the
+ *    first call before any stream capture. Host threads share the looked-up
+ *    address under a lock.
  *  - All calls share the one array and it keeps the last call's contents;
  *    calls that overlap on the GPU (other streams, other host threads) race.
  *  - The save-time clamp restarts from *t_inout on every call. */

@@ -236,7 +236,7 @@ def test_cell_maps(cuda_device, eq):
         dot = U[1] * U[1]
         for k in range(2, 1 + nsd):
             dot = dot + U[k] * U[k]
-        p = 0.4 * (U[-1] - 0.5 * dot / U[0])
+        p = (1.4 - 1.0) * (U[-1] - 0.5 * dot / U[0])  # Euler::computeExtra, (gamma - 1) * ie
         assert np.array_equal(E[0], p)
         for k in range(nsd):
             assert np.array_equal(E[1 + k], U[1 + k] / U[0])
