@@ -121,6 +121,73 @@ template <int DIM, int TX, int TY, int TZ> struct Tile {
     static constexpr int T[3] = {TX, TY, TZ};
 };
 
+// Line buffers keep each item's NV values together, padded to a multiple of
+// 16 bytes (LinePad), so that a reconstruction's, a face's or a cell's
+// values move with 128-bit shared-memory accesses: one to four per item
+// instead of NV scalar accesses.
+template <class R, int NV> struct LinePad {
+    static constexpr int per16 = (int)(16 / sizeof(R));
+    static constexpr int value = NV == 1 ? 1 : ((NV + per16 - 1) / per16) * per16;
+};
+
+template <int NV, class R> __device__ __forceinline__ R lane_or_zero(const R* v, int i) {
+    return i < NV ? v[i < NV ? i : 0] : R(0);
+}
+
+// p: item slot of LinePad<R, NV>::value values, 16-byte aligned when NV > 1.
+template <class R, int NV> __device__ __forceinline__ void line_put(R* p, const R* v) {
+    constexpr int P = LinePad<R, NV>::value;
+    if constexpr (P == 1) {
+        p[0] = v[0];
+    } else if constexpr (std::is_same<R, float>::value) {
+#pragma unroll
+        for (int c = 0; c < P / 4; ++c)
+            reinterpret_cast<float4*>(p)[c] =
+                make_float4(lane_or_zero<NV>(v, 4 * c), lane_or_zero<NV>(v, 4 * c + 1),
+                            lane_or_zero<NV>(v, 4 * c + 2), lane_or_zero<NV>(v, 4 * c + 3));
+    } else if constexpr (std::is_same<R, double>::value) {
+#pragma unroll
+        for (int c = 0; c < P / 2; ++c)
+            reinterpret_cast<double2*>(p)[c] = make_double2(lane_or_zero<NV>(v, 2 * c), lane_or_zero<NV>(v, 2 * c + 1));
+    } else {  // double-float: two pairs per 16 bytes
+#pragma unroll
+        for (int c = 0; c < P / 2; ++c) {
+            const R a = lane_or_zero<NV>(v, 2 * c), b = lane_or_zero<NV>(v, 2 * c + 1);
+            reinterpret_cast<float4*>(p)[c] = make_float4(a.hi, a.lo, b.hi, b.lo);
+        }
+    }
+}
+
+template <class R, int NV> __device__ __forceinline__ void line_get(const R* p, R* v) {
+    constexpr int P = LinePad<R, NV>::value;
+    if constexpr (P == 1) {
+        v[0] = p[0];
+    } else if constexpr (std::is_same<R, float>::value) {
+#pragma unroll
+        for (int c = 0; c < P / 4; ++c) {
+            const float4 q = reinterpret_cast<const float4*>(p)[c];
+            if (4 * c < NV) v[4 * c < NV ? 4 * c : 0] = q.x;
+            if (4 * c + 1 < NV) v[4 * c + 1 < NV ? 4 * c + 1 : 0] = q.y;
+            if (4 * c + 2 < NV) v[4 * c + 2 < NV ? 4 * c + 2 : 0] = q.z;
+            if (4 * c + 3 < NV) v[4 * c + 3 < NV ? 4 * c + 3 : 0] = q.w;
+        }
+    } else if constexpr (std::is_same<R, double>::value) {
+#pragma unroll
+        for (int c = 0; c < P / 2; ++c) {
+            const double2 q = reinterpret_cast<const double2*>(p)[c];
+            if (2 * c < NV) v[2 * c < NV ? 2 * c : 0] = q.x;
+            if (2 * c + 1 < NV) v[2 * c + 1 < NV ? 2 * c + 1 : 0] = q.y;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < P / 2; ++c) {
+            const float4 q = reinterpret_cast<const float4*>(p)[c];
+            if (2 * c < NV) v[2 * c < NV ? 2 * c : 0] = R(q.x, q.y);
+            if (2 * c + 1 < NV) v[2 * c + 1 < NV ? 2 * c + 1 : 0] = R(q.z, q.w);
+        }
+    }
+}
+
 template <class R, int NV, int G, int DIM, int TX, int TY, int TZ>
 struct SmemLayout {
     static constexpr int GX = G, GY = DIM > 1 ? G : 0, GZ = DIM > 2 ? G : 0;
@@ -136,7 +203,8 @@ struct SmemLayout {
     static constexpr size_t round128(size_t b) { return (b + 127) & ~(size_t)127; }
     static constexpr size_t box_bytes = sizeof(R) * (size_t)NV * HALO;  // one halo of every variable
     static constexpr size_t halo_bytes = round128(box_bytes);           // its slot (TMA wants 128 B aligned)
-    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NV * REC);
+    static constexpr int NVP = LinePad<R, NV>::value;  // values per line-buffer item
+    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NVP * REC);
     // Dynamic shared memory per kernel, plus 128 bytes to align the base:
     //   plain staging:    halo | line buffers
     //   TMA staging:      halo | line buffers, which first hold the L0 halo of the stage-1 modes
@@ -179,11 +247,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
     constexpr int NFACE = (TD + 1) * (NT / TD);
     constexpr int DS = D == 0 ? 1 : (D == 1 ? SL::HX : SL::HX * SL::HY);
     constexpr int VS = SL::HALO;
+    constexpr int NVP = SL::NVP;
+    (void)NREC;
 
     // Work items: along x (D = 0) the cells of a line are consecutive; for
     // D >= 1 consecutive items step along x (p, the first other dimension),
     // so a warp's shared-memory accesses stay unit-stride in every phase.
-    // Line buffers hold item w at index w in both layouts:
+    // Line buffers hold item w at slot w (NVP values from w * NVP) in both layouts:
     //   D = 0:  w = (o * LEN + a),            o = p + O1 q
     //   D >= 1: w = ((q * LEN + a) * O1 + p)  (faces: LEN -> TD + 1)
     // reconstruction of cells -1 .. TD along D
@@ -208,11 +278,8 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         const int s = ((c[2] + SL::GZ) * SL::HY + (c[1] + SL::GY)) * SL::HX + (c[0] + SL::GX);
         R l[NV], r[NV];
         reconstruct_cell<R, NV, RC>(su + s, VS, DS, l, r, gamma);
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            rl[k * NREC + w] = l[k];
-            rr[k * NREC + w] = r[k];
-        }
+        line_put<R, NV>(rl + w * NVP, l);
+        line_put<R, NV>(rr + w * NVP, r);
     }
     __syncthreads();
     // face b is the left face of tile cell b along D (between cells b-1 and b)
@@ -234,16 +301,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
             ir = il + O1;
         }
         R a[NV], bb[NV], F[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            a[k] = rr[k * NREC + il];   // cell b-1 at its right face
-            bb[k] = rl[k * NREC + ir];  // cell b at its left face
-        }
+        line_get<R, NV>(rr + il * NVP, a);   // cell b-1 at its right face
+        line_get<R, NV>(rl + ir * NVP, bb);  // cell b at its left face
         const R w = Ph::template face_flux<D>(a, bb, gamma, F);
 #pragma unroll
         // the flux of face b replaces the right value of cell b - 1 (item il),
         // which no other face reads
-        for (int k = 0; k < NV; ++k) rr[k * NREC + il] = F[k];
+        line_put<R, NV>(rr + il * NVP, F);
         // the face counts if both neighbours lie in the grid's interior range
         int c[3];
         c[D] = b;
@@ -271,10 +335,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         // the items of cells cd - 1 and cd
         const int fli = D == 0 ? (p + O1 * q) * LEN + cd : (q * LEN + cd) * O1 + p;
         const int fri = D == 0 ? fli + 1 : fli + O1;
+        R FL[NV], FR[NV];
+        line_get<R, NV>(rr + fli * NVP, FL);
+        line_get<R, NV>(rr + fri * NVP, FR);
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R fl = rr[k * NREC + fli];
-            const R fr = rr[k * NREC + fri];
+            const R fl = FL[k];
+            const R fr = FR[k];
             if constexpr (!kExact && D == 0)
                 acc[j * NV + k] = fl - fr;  // the first direction starts the sum
             else
@@ -415,7 +482,7 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     constexpr int CPT = CellsPerThread<NT, NTH>::value;
     constexpr bool kSame = std::is_same<R, C>::value;
     C* rl = work;
-    C* rr = rl + NV * SL::REC;
+    C* rr = rl + SL::NVP * SL::REC;
 
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;

@@ -245,20 +245,26 @@ def test_step_graph_replay_matches_direct_launches(cuda_device, case, integ):
 
 def test_small_grids_keep_the_default_without_tuning(cuda_device):
     """Below 4096 interior cells the first advance keeps candidate 0 and
-    launches no tuning kernels (a few CTAs per stage time alike); an explicit
+    launches no tuning kernels (a few CTAs per stage time alike): the same
+    kernel launches as a solve with candidate 0 pinned. An explicit
     gbfv_autotune still tunes."""
-    s = lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (32, 32, 1), (0, 0, 0), (1, 1, 0),
-                   cfl=0.4, precision=lib.FP64)
-    try:
-        s.set_primitive(workloads.kh_prim(32, lib.uniform(40, 0)))
-        s.profile(True)
-        s.profile_read()
-        _, _, k0 = s.profile_read()
-        s.advance(1e9, 0, 5)
-        _, stage_launches, k1 = s.profile_read()
-        assert s.current_candidate() == 0
-        assert stage_launches == 15  # 5 SSP-RK3 steps, 3 stage launches each, no tuning launches
-        chosen, ms = s.autotune()
-        assert all(m > 0 for m, c in zip(ms, s.candidates()))
-    finally:
-        s.close()
+    launches = []
+    for pin in (False, True):
+        s = lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (32, 32, 1), (0, 0, 0), (1, 1, 0),
+                       cfl=0.4, precision=lib.FP64)
+        try:
+            s.set_primitive(workloads.kh_prim(32, lib.uniform(40, 0)))
+            if pin:
+                s.select_candidate(0)
+            s.profile(True)
+            _, _, k0 = s.profile_read()
+            s.advance(1e9, 0, 5)
+            _, _, k1 = s.profile_read()
+            assert s.current_candidate() == 0
+            launches.append(k1 - k0)
+            if not pin:
+                chosen, ms = s.autotune()
+                assert all(m > 0 for m in ms)
+        finally:
+            s.close()
+    assert launches[0] == launches[1], launches
