@@ -56,7 +56,7 @@ CONSERVED_VARIABLES = {
 
 
 class ConfigError(RuntimeError):
-    """A configuration the reference rejects, or one this build does not run."""
+    """A configuration the reference rejects, or one this library does not run."""
 
 
 @dataclass
