@@ -596,6 +596,15 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
         if (atomicCAS(&A.st->status, 0, 1) == 0) A.st->failed_step = (int)A.st->steps + 1;
     }
     store_with_images<R, NV>(out, total, Gd, ix, iy, iz, A.periodic != 0, res);
+    if (A.out2) store_with_images<R, NV>(reinterpret_cast<R*>(A.out2), total, Gd, ix, iy, iz, A.periodic != 0, res);
+    if constexpr (kSame) {
+        if (A.copy_in) {
+            R vin[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) vin[k] = su[k * SL::HALO + sidx];
+            store_with_images<R, NV>(reinterpret_cast<R*>(A.copy_in), total, Gd, ix, iy, iz, A.periodic != 0, vin);
+        }
+    }
     }
     }
 }
@@ -728,6 +737,8 @@ __device__ __forceinline__ bool batch_tile_args(const BatchArgs& B, int t, Stage
     A.periodic = B.periodic;
     A.check = 0;
     A.l0 = nullptr;
+    A.copy_in = nullptr;
+    A.out2 = nullptr;
     if (B.mode == MODE_L) {
         A.in = cur; A.u0 = cur; A.out = m.l;
     } else if (B.mode == MODE_RK3_S1) {

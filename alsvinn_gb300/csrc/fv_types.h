@@ -204,6 +204,12 @@ struct StageArgs {
     // single-grid TMA stages: bytes announced on the halo barrier beyond the
     // copies' (0; nonzero only in a test of the bounded wait's error path)
     unsigned tma_extra_tx;
+    // single-grid stages reading / writing a host state in place (null:
+    // none): MODE_L writes its input cells, with their ghost images, to
+    // copy_in (the device copy of a state read from mapped host memory);
+    // a combination stage writes its output to out2 as well as to out
+    void* copy_in;
+    void* out2;
 };
 
 // Reconstruction of one direction over the reference's cell range

@@ -52,6 +52,7 @@ Registry& registry() {
         gbfv_region_v0_e0(r); gbfv_region_v0_e1(r); gbfv_region_v0_e2(r); gbfv_region_v0_e3(r);
         gbfv_region_v1_e0(r); gbfv_region_v1_e1(r); gbfv_region_v1_e2(r); gbfv_region_v1_e3(r);
         gbfv_region_v2_e0(r); gbfv_region_v2_e1(r); gbfv_region_v2_e2(r); gbfv_region_v2_e3(r);
+
         return r;
     }();
     return *R;
@@ -915,8 +916,96 @@ int gbfv_time(gbfv_solver* s, double* t, long long* steps, double* last_dt) {
     return GBFV_OK;
 }
 
+// The device address of a host buffer the GPU reads and writes in place
+// (pinned memory mapped into the device's address space; on a GB300 node
+// the accesses travel over NVLink-C2C), or null.
+static void* mapped_host(const void* host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return a.devicePointer;
+}
+
+// One time step on a state in mapped host memory, without the two state
+// copies: the first stage reads the host state itself (the default
+// candidate's per-thread loads) and writes the device copy the later stages
+// read, and the last stage writes its result to the host state as well as
+// to the device state. The copies' link time overlaps the FP64-bound stage
+// arithmetic. The same kernels compute every cell, so the result is the
+// copying path's bit for bit. Returns 1 (nothing done) when the step does not
+// apply and the copying path must run.
+static int advance_host_mapped(gbfv_solver* s, void* hdev, double end_time, int number_of_saves) {
+    if (s->cand < 0 && !s->pinned) {
+        const int r = tune(s, false);
+        if (r) return r;
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (!(s->st_host->t < end_time) || s->st_host->status != 0) return 1;
+    if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
+    StepParams P = step_params(s, end_time);
+    P.time_interval = number_of_saves > 0 ? s->time_interval : 0.0;
+    begin_kernel<<<1, 1, 0, s->stream>>>(s->st, P.end_time, s->st_host->steps + 1);
+    CUDA_TRY(cudaGetLastError());
+    s->launches += 1;
+    int ncand = 0;
+    const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &ncand);
+    const StageCandidate& stage = c[s->cand < 0 ? 0 : s->cand];
+    cudaStream_t q = s->stream;
+    StageArgs a = stage_args(s, s->st, hdev, hdev, nullptr, s->L, MODE_L, 0);
+    a.copy_in = s->U;
+    STAGE_TRY(launch_stage(s, c[0], a));
+    dt_kernel<<<1, 1, 0, q>>>(s->st, P);
+    CUDA_TRY(cudaGetLastError());
+    s->launches += 2;  // dt + finish
+    if (s->in == IN_RK3) {
+        STAGE_TRY(launch_stage(s, stage, stage_args(s, s->st, s->U, s->U, s->L, s->V, MODE_RK3_S1, 0)));
+        StageArgs b = stage_args(s, s->st, s->V, s->U, nullptr, s->U, MODE_RK3_S2, 1);
+        b.out2 = hdev;
+        STAGE_TRY(launch_stage(s, stage, b));
+    } else {
+        StageArgs b = stage_args(s, s->st, s->U, s->U, s->L, s->V, MODE_RK2_S1, 1);
+        b.out2 = hdev;
+        STAGE_TRY(launch_stage(s, stage, b));
+        s->launches += 1;
+        const long long n = (long long)s->nvar * s->G.total;
+        copy_state_kernel<double><<<1184, 256, 0, q>>>(s->st, (const double*)s->V, (double*)s->U, n);
+        CUDA_TRY(cudaGetLastError());
+    }
+    finish_kernel<<<1, 1, 0, q>>>(s->st, P);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, q));
+    CUDA_TRY(cudaStreamSynchronize(q));
+    if (s->st_host->status == kStatusTmaTimeout) {
+        char msg[256];
+        snprintf(msg, sizeof msg, "a TMA halo copy did not complete within the time limit (step %d)",
+                 s->st_host->failed_step);
+        return fail(GBFV_ERR_CUDA, msg);
+    }
+    if (s->st_host->status != 0) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "Simulation state does not obey constraints! At time %.17g, number of timesteps performed %d",
+                 s->st_host->t, s->st_host->failed_step);
+        return fail(GBFV_ERR_CONSTRAINT, msg);
+    }
+    return GBFV_OK;
+}
+
 int gbfv_advance_host(gbfv_solver* s, double* host, double end_time, int number_of_saves, int max_steps) {
     if (!s || !host) return fail(GBFV_ERR_ARGUMENT, "null argument");
+    // one step of an FP64 state in mapped (pinned) host memory: in place
+    if (max_steps == 1 && !s->profiling && (s->var == VAR_F64 || s->var == VAR_F64_EXACT) &&
+        (s->in == IN_RK3 || s->in == IN_RK2)) {
+        void* hdev = mapped_host(host);
+        if (hdev) {
+            const int r = advance_host_mapped(s, hdev, end_time, number_of_saves);
+            if (r <= 0) return r;
+        }
+    }
     int r = upload(s, host);
     if (r) return r;
     r = gbfv_advance(s, end_time, number_of_saves, max_steps);

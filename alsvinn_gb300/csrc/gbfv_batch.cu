@@ -35,7 +35,8 @@ namespace {
 
 struct MemberParam {
     double cell_lengths[3];
-    double time_interval;  // save-time clamp interval (0: none)
+    double time_interval;  // save-time clamp interval (0: none): the statistics' (FixedIntervalStatistics)
+    double time_interval2; // second clamp (0: none): the fvm writer's (FixedIntervalWriter)
     double end_time;       // the member's own end time (+inf: the advance's)
     int dim;
     int active;
@@ -52,7 +53,7 @@ struct GroupAcc {
 __global__ void batch_dt_kernel(StepState* st, const MemberParam* mp, int M, double cfl) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= M || !mp[s].active || st[s].done) return;
-    set_step_dt(st[s], mp[s].dim, mp[s].cell_lengths, cfl, mp[s].time_interval, 0.0);
+    set_step_dt(st[s], mp[s].dim, mp[s].cell_lengths, cfl, mp[s].time_interval, mp[s].time_interval2);
 }
 
 __global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M, int alternate) {
@@ -67,6 +68,7 @@ __global__ void batch_finish_kernel(StepState* st, const MemberParam* mp, int M,
         S.just_saved = (int)(S.number_saved - 1);  // save index k reached: t >= (k + 1) * interval
         S.number_saved += 1;
     }
+    if (P.time_interval2 > 0 && S.t >= (double)S.number_saved2 * P.time_interval2) S.number_saved2 += 1;
     S.ws_bits[0] = S.ws_bits[1] = S.ws_bits[2] = 0ull;
     if (alternate) S.parity ^= 1;
     const bool reached = !(S.t < S.end_time);
@@ -98,8 +100,8 @@ __global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, 
 // into accumulator (group, k) at each save k its clamp stopped it at.
 // list[i] = (member, accumulator, count after the fold). One warp: the lanes
 // read 32 members' flags at a time, lane 0 numbers the (few) folds in order.
-__global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* accs, int nacc, int nsaves, int4* list,
-                                    int* nlist) {
+__global__ void batch_assign_kernel(StepState* st, const MemberParam* mp, int M, GroupAcc* accs, int nacc,
+                                    int nsaves, int4* list, int* nlist) {
     const int lane = threadIdx.x;
     int m = 0;
     for (int base = 0; base < M; base += 32) {
@@ -111,7 +113,12 @@ __global__ void batch_assign_kernel(StepState* st, int M, GroupAcc* accs, int na
             if (done || saved >= 0) {
                 st[s].just_done = 0;
                 st[s].just_saved = -1;
-                const int k = nsaves <= 1 ? (done ? 0 : -1) : (st[s].status == 0 ? saved : -1);
+                // one save: at the statistics clamp's save when the member has
+                // one (its advance may stop earlier, at a writer's save), else
+                // at the end of the advance
+                const bool clamp = mp[s].time_interval > 0;
+                const int k = nsaves <= 1 ? ((clamp ? (saved == 0 && st[s].status == 0) : done) ? 0 : -1)
+                                          : (st[s].status == 0 ? saved : -1);
                 const int g = st[s].group;
                 if (k >= 0 && k < nsaves && g >= 0 && g * nsaves + k < nacc) a = g * nsaves + k;
             }
@@ -354,8 +361,8 @@ int enqueue_batch_step(gbfv_batch* b) {
     if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
     batch_finish_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.in == 1 ? 1 : 0);
     if (!b->groups.empty()) {
-        batch_assign_kernel<<<1, 32, 0, q>>>(b->d_states, M, b->d_groups, (int)b->groups.size(), b->stats_saves,
-                                             b->d_list, b->d_nlist);
+        batch_assign_kernel<<<1, 32, 0, q>>>(b->d_states, b->d_params, M, b->d_groups, (int)b->groups.size(),
+                                             b->stats_saves, b->d_list, b->d_nlist);
         const long long cells = b->stats_cells;
         unsigned nb = (unsigned)std::min<long long>((cells + 255) / 256, 152 * 8);
         if (b->scheme.elem == 8)
@@ -684,6 +691,7 @@ int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const d
     h.m.G = p.G;
     for (int k = 0; k < 3; ++k) h.p.cell_lengths[k] = p.cell_lengths[k];
     h.p.time_interval = 0;
+    h.p.time_interval2 = 0;
     h.p.end_time = std::numeric_limits<double>::infinity();
     h.own_end = false;
     h.p.dim = p.G.dim;
@@ -704,6 +712,7 @@ int gbfv_batch_add(gbfv_batch* b, const int n[3], const double lower[3], const d
     StepState z;
     std::memset(&z, 0, sizeof z);
     z.number_saved = 1;
+    z.number_saved2 = 1;
     z.done = 1;
     z.group = group;
     b->h_states[slot] = z;
@@ -850,6 +859,14 @@ int gbfv_batch_set_member_end(gbfv_batch* b, int slot, double end_time, int numb
     h.own_end = true;
     h.p.end_time = end_time;
     h.p.time_interval = number_of_saves > 0 ? end_time / number_of_saves : 0;
+    return upload_members(b);
+}
+
+int gbfv_batch_set_member_write_interval(gbfv_batch* b, int slot, double interval) {
+    if (!b || slot < 0 || slot >= b->max_members || !b->members[slot].active)
+        return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_set_member_write_interval: bad slot");
+    if (!(interval >= 0)) return bfail(GBFV_ERR_ARGUMENT, "gbfv_batch_set_member_write_interval: bad interval");
+    b->members[slot].p.time_interval2 = interval;
     return upload_members(b);
 }
 

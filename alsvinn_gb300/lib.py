@@ -782,6 +782,10 @@ class Batch:
         """The member's own end time (and save clamp)."""
         _check(load().gbfv_batch_set_member_end(self.h, int(slot), float(end_time), int(number_of_saves)))
 
+    def set_member_write_interval(self, slot, interval):
+        """The member's second save clamp (the fvm writer's interval)."""
+        _check(load().gbfv_batch_set_member_write_interval(self.h, int(slot), float(interval)))
+
     def member_status(self, slot):
         """(status, failed step): 0 fine, 1 constraint check failed, 2 halo copy timed out."""
         st = ctypes.c_int()
@@ -877,6 +881,7 @@ _SIGNATURES.update({
     "gbfv_server_stats_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "gbfv_batch_set_member_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+    "gbfv_batch_set_member_write_interval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
     "gbfv_batch_member_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                                 ctypes.POINTER(ctypes.c_int)]),
     "gbfv_server_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),

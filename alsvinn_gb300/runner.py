@@ -18,9 +18,12 @@ Follows alsuq's Setup::makeRunner and Runner::run
 Two engines run the samples:
   * "batch" - the ensemble engine (lib.Batch): every sample of a wave is a
     member of one persistent launch per RK stage, each with its own dt; the
-    statistics are folded on the device as members reach the end time. Used
-    when mean / variance statistics are taken once, at the end time, and no
-    per-sample fvm writer is configured.
+    statistics are folded on the device as members reach their save times.
+    An fvm writer is the member's second save clamp: the wave advances to
+    each writer save, where every member stops exactly, and the host writes
+    the members' states (Runner::run attaches the writers to every sample's
+    simulator, alsuq/src/run/Runner.cpp:55-73). Used for mean / variance
+    statistics without an initial-time save and without fvm functionals.
   * "serial" - one lib.Solver reused sample after sample with the writer and
     statistics save clamps (any schedule).
 Both give each sample the reference's trajectory; the statistics are FP64
@@ -32,8 +35,8 @@ import numpy as np
 
 from . import initdata, lib, uq
 from .config import ConfigError
-from .simulator import Simulator
-from .writers import NetCDFWriter, NumpyWriter
+from .simulator import Simulator, interior
+from .writers import NetCDFWriter, NumpyWriter, make_writer
 
 
 class _FunctionalAccumulator:
@@ -132,14 +135,14 @@ class Runner:
         self.stats_interval = intervals.pop() if intervals else 0.0
         self.stats_saves = stats[0].number_of_saves if stats else 0
         self.stats_initial = bool(stats and stats[0].write_initial_timestep)
-        batch_ok = (self.fvm.writer is None and not self.fvm.functionals
+        batch_ok = (not self.fvm.functionals
                     and not self.stats_initial and all(st.name == "meanvar" for st in stats)
                     and self.fvm.integrator in ("rungekutta2", "rungekutta3"))
         if engine == "auto":
             engine = "batch" if batch_ok else "serial"
         if engine == "batch" and not batch_ok:
             raise ConfigError("the batch engine needs rungekutta2/3, mean/variance statistics (no initial-time "
-                              "statistics) and no fvm writer or functionals; use the serial engine")
+                              "statistics) and no fvm functionals; use the serial engine")
         self.engine = engine
         self.timesteps = 0
         self.wall_s = 0.0
@@ -232,17 +235,26 @@ class Runner:
         # device as every member's save clamp stops it there
         saves = max(1, self.stats_saves)
         per_save = []
+        writer = None
+        if f.writer is not None:
+            writer = make_writer(f.writer, f.equation, f.lower, f.upper, f.dimension, self.uqc.samples,
+                                 self.output_dir)
+        g = lib.ghost_cells(f.reconstruction)
         try:
             b.set_statistics_saves(saves)
             for i in range(0, len(self.samples), wave):
                 chunk = self.samples[i:i + wave]
                 slots = [b.add(f.dimension, f.lower, f.upper, self._prim(params[s]), group=0) for s in chunk]
-                b.advance(f.end_time, saves if self.stats_saves > 0 else 1, 0)
+                if writer is None:
+                    b.advance(f.end_time, saves if self.stats_saves > 0 else 1, 0)
+                else:
+                    self._advance_with_writer(b, writer, slots, chunk, saves, g)
                 for sl in slots:
                     self.timesteps += b.member_time(sl)[1]
                     b.remove(sl)
+            if writer is not None:
+                writer.finalize()
             nv = lib.num_variables(f.equation)
-            g = lib.ghost_cells(f.reconstruction)
             dim = f.dim
             total = int(np.prod([f.dimension[d] + 2 * g if d < dim else f.dimension[d] for d in range(3)]))
             for k in range(saves):
@@ -254,6 +266,38 @@ class Runner:
         finally:
             b.close()
         return [list(per_save) for _ in self.uqc.stats]
+
+    def _advance_with_writer(self, b, writer, slots, samples, saves, g):
+        """A wave with the fvm writer: each member's own end time with the
+        statistics clamp (interval endTime / saves) and the writer's clamp
+        (endTime / numberOfSaves); the wave advances to each writer save
+        k * interval, where every member stops exactly, and the host writes
+        the members' states (snapshot 0 at t = 0 with writeInitialTimestep),
+        as the serial engine's simulator does between its advances."""
+        f = self.fvm
+        W = f.save_interval()
+        nvar = lib.num_variables(f.equation)
+        total = int(np.prod([f.dimension[d] + 2 * g if d < f.dim else f.dimension[d] for d in range(3)]))
+        for sl in slots:
+            b.set_member_end(sl, f.end_time, saves)
+            b.set_member_write_interval(sl, W)
+
+        def write_all(snapshot):
+            for sl, s in zip(slots, samples):
+                U = b.member_state(sl, total)
+                t, _ = b.member_time(sl)
+                writer.write(interior(U.reshape(nvar, total), f.dimension, g), s, snapshot, time=t)
+
+        snapshot = 0
+        if f.writer.write_initial_timestep:
+            write_all(snapshot)
+            snapshot += 1
+        for k in range(1, f.writer.number_of_saves + 1):
+            b.advance(k * W, 0, 0)
+            write_all(snapshot)
+            snapshot += 1
+        # the end time itself (k * interval may fall an ulp short of it)
+        b.advance(f.end_time, 0, 0)
 
     # -- output ------------------------------------------------------------
 

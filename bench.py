@@ -10,8 +10,10 @@ Metric: cell-updates/s = interior cells x time steps / time (RK stages are
 not counted separately). `value` is measured with the state resident in HBM;
 the L2 (129 MB) is flushed by a 512 MiB memset on the solver's stream before
 every timed step, outside the step's events. `e2e` is the same metric through
-gbfv_advance_host with the state in pinned host memory: every step copies the
-padded state host->device, advances one step and copies it back.
+gbfv_advance_host with the state in pinned host memory, one step per call:
+each step's input state comes from host memory and its result goes back to
+it (the first stage reads the mapped host state in place and the last stage
+writes it back, over NVLink-C2C, instead of two copies around the step).
 
 The roofline uses the algorithmic bytes of an SSP-RK3 step, 8 * nvar * 8 bytes
 per interior cell (stage 0 reads U0 and writes L0, stages 1 and 2 read two
@@ -333,7 +335,9 @@ def run_gpu(args):
         e2e_s = float(t.item())
     state_bytes = NVAR * s.total * 8  # gbfv_advance_host moves the FP64 host state
     e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": state_bytes,
-           "d2h_bytes_per_step": state_bytes, "steps": e2e_steps}
+           "d2h_bytes_per_step": state_bytes, "steps": e2e_steps,
+           "transfer": "the padded FP64 state read from and written to pinned host memory every step, by the "
+                       "first and last stage kernels in place (mapped memory over NVLink-C2C)"}
 
     # the same workload with the reconstruction and flux arithmetic in
     # double-float on the FP32 pipes (FP64 state and RK update): reported

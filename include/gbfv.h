@@ -175,7 +175,13 @@ int gbfv_autotune(gbfv_solver* s, int* chosen, double* ms, int capacity);
 int gbfv_current_candidate(gbfv_solver* s, int* idx);
 
 /* Same as gbfv_advance, reading the state from host memory first and writing
- * it back after: the call a host-side Volume owner makes per step. */
+ * it back after: the call a host-side Volume owner makes per step. For one
+ * step (max_steps == 1) of an FP64 / FP64-exact RK2 or RK3 solver on pinned
+ * host memory the GPU can address (cudaHostAlloc / pinned allocations; on a
+ * GB300 node reached over NVLink-C2C), the first stage reads the host state
+ * in place and the last stage writes the result back, with no copies around
+ * the step; other calls copy the state in and out. Both give the same bits,
+ * and the solver's device state afterwards is the host's. */
 int gbfv_advance_host(gbfv_solver* s, double* state_host_inout, double end_time, int number_of_saves,
                       int max_steps);
 
@@ -449,6 +455,17 @@ int gbfv_batch_advance(gbfv_batch* b, double end_time, int number_of_saves, int 
  * time belongs to its configuration (alsfvm/src/config/SimulatorSetup.cpp:
  * 102-232), so members of one ensemble may each have their own. */
 int gbfv_batch_set_member_end(gbfv_batch* b, int slot, double end_time, int number_of_saves);
+
+/* The second save clamp of a member, the fvm writer's FixedIntervalWriter
+ * (alsfvm/src/io/FixedIntervalWriter.cpp:45-53): dt is also clamped to the
+ * next k * interval (0: none), beside the statistics clamp. With it an
+ * advance to end_time = k * interval stops every member exactly at its k-th
+ * writer save, where the host reads its state for the writer (alsuq's
+ * Runner attaches the writers to every sample's simulator,
+ * alsuq/src/run/Runner.cpp:55-73). With one statistics save, a member with a
+ * statistics clamp is folded at that clamp's save, not at the end of an
+ * advance that stopped earlier. */
+int gbfv_batch_set_member_write_interval(gbfv_batch* b, int slot, double interval);
 
 /* A member's status: 0 running or finished, 1 its state broke the constraint
  * check (CPUCellComputer::obeysConstraints; the member stopped at

@@ -290,3 +290,41 @@ def test_alsvinncli_functionals_write_at_their_save_times(cuda_device, tmp_path)
         want.append(fvoracle.functional("log_entropy", f.equation, f.boundary, n, g, f.lower, f.upper, Uk,
                                         gamma=f.gamma)[0])
     np.testing.assert_allclose(le, [w[-1, 0] for w in want], rtol=1e-12)
+
+
+def test_batch_engine_writes_the_fvm_writer_like_the_serial_engine(cuda_device, tmp_path):
+    """An alsuqcli input with an fvm writer runs on the ensemble engine: the
+    writer is each member's second save clamp, the wave stops at every
+    writer save and the host writes the members' states. The file equals
+    the serial engine's bit for bit (exact variant); the statistics, taken
+    at two save times that differ from the writer's three, match the
+    serial engine's to the Welford fold order's rounding."""
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    out = {}
+    for engine in ("serial", "batch"):
+        d = tmp_path / engine
+        d.mkdir()
+        _copy_inputs(d, ["kh_uq.xml", "kh_global.py"])
+        xml = str(d / "kh_uq.xml")
+        text = open(xml).read().replace("<numberOfSaves>1</numberOfSaves>", "<numberOfSaves>2</numberOfSaves>")
+        text = text.replace("</integrator>", "</integrator>\n  <writer><type>netcdf</type><basename>kh_uq_fvm</basename>"
+                            "<numberOfSaves>3</numberOfSaves><writeInitialTimestep>1</writeInitialTimestep>"
+                            "</writer>")
+        open(xml, "w").write(text)
+        cfg = config.read_config(xml)
+        r = runner.Runner(cfg, lib.FP64_EXACT, output_dir=str(d), engine=engine)
+        assert r.engine == engine
+        stats = r.run()
+        with netcdf(str(d / "kh_uq_fvm"), "r", mmap=False) as nc:
+            arrays = {v: np.array(nc.variables[v][:]) for v in ("rho", "mx", "my", "E")}
+        out[engine] = (stats, arrays, r.timesteps)
+    (s_stats, s_arr, s_steps), (b_stats, b_arr, b_steps) = out["serial"], out["batch"]
+    assert s_steps == b_steps
+    for v in s_arr:
+        assert s_arr[v].shape[:2] == (4, 4)  # members x (initial + 3 saves)
+        assert np.array_equal(s_arr[v], b_arr[v]), v
+    assert len(s_stats) == len(b_stats) == 2
+    for (n1, m1, v1), (n2, m2, v2) in zip(s_stats, b_stats):
+        assert n1 == n2 == 4
+        np.testing.assert_allclose(m2, m1, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(v2, v1, rtol=1e-9, atol=1e-13)

@@ -323,6 +323,49 @@ def test_advance_host_equals_device_path(cuda_device):
     assert np.array_equal(U, U_dev)
 
 
+@pytest.mark.parametrize("precision", [lib.FP64, lib.FP64_EXACT])
+@pytest.mark.parametrize("integrator", ["rungekutta3", "rungekutta2"])
+@pytest.mark.parametrize("saves", [0, 3])
+def test_advance_host_in_place_equals_device_path(cuda_device, precision, integrator, saves):
+    """One step per call on a state in pinned (mapped) host memory: the first
+    stage reads the host state in place and the last writes it back, without
+    the two state copies. Every step's state, time and step count equal the
+    device path's and the copying path's (pageable host memory), bit for
+    bit; the solver's device state follows too."""
+    import torch
+    case = LARGE["kh128_50"]
+    prim = case["prim"]()
+    T = 0.004  # a few steps; with saves the clamp lands the steps on T/3, 2T/3, T
+
+    def make():
+        s = lib.Solver(case["equation"], case["flux"], case["recon"], integrator, "periodic", case["n"], (0, 0, 0),
+                       case["upper"], cfl=case["cfl"], precision=precision)
+        s.set_primitive(prim)
+        return s
+
+    with make() as dev, make() as mapped, make() as copied:
+        pinned = torch.empty((dev.nvar, dev.total), dtype=torch.float64).pin_memory()
+        Um = pinned.numpy()
+        Um[...] = dev.get_state()
+        Uc = dev.get_state().copy()
+        for _ in range(40):
+            if dev.time()[0] >= T:
+                break
+            dev.advance(T, saves, 1)
+            mapped.advance_host(Um, T, saves, 1)
+            copied.advance_host(Uc, T, saves, 1)
+            ref = dev.get_state()
+            assert np.array_equal(Um, ref)
+            assert np.array_equal(Uc, ref)
+            assert mapped.time() == dev.time() == copied.time()
+            assert np.array_equal(mapped.get_state(), ref)
+        assert dev.time()[0] >= T
+        # past the end: nothing changes
+        before = Um.copy()
+        mapped.advance_host(Um, T, saves, 1)
+        assert np.array_equal(Um, before) and mapped.time() == dev.time()
+
+
 def test_constraint_violation_is_reported(cuda_device):
     prim = workloads.sod_prim(64)
     prim[2, 30] = -1.0
