@@ -4,6 +4,10 @@
   oracle/libfvoracle.so          the CPU oracle (test infrastructure)
   oracle/_ref/libalsref.so       the reference's own CPU path, only where the
                                  reference sources are present (REF_ROOT)
+  oracle/_ref/cuda/*.cubin       the reference's own CUDA kernels (device code
+                                 only), where the reference sources are present
+  oracle/librefcuda.so           the host driver of those kernels (test and
+                                 baseline infrastructure)
 
 Translation units compile in parallel; a unit is rebuilt only when a source or
 header it may include changed (timestamps over csrc/ and include/).
@@ -23,6 +27,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgbfv.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "libfvoracle.so")
+REFCUDA_LIB = os.path.join(ORACLE_DIR, "librefcuda.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + INCLUDE]
@@ -30,7 +35,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + C
 VARIANTS = (0, 1, 2, 3)   # fp64, fp64 exact, fp32, fp64 state with double-float arithmetic
 EQUATIONS = (0, 1, 2, 3)  # burgers, euler1, euler2, euler3
 TUNED_VARIANTS = (0, 1, 2, 3)  # variants with autotuning candidates (all; TMA where storage = arithmetic type)
-REGION_VARIANTS = (0, 1, 2)  # variants with region kernels (operator calls on part of the grid)
+REGION_VARIANTS = (0, 1, 2, 3)  # variants with region kernels (operator calls on part of the grid)
 
 
 def _nvcc():
@@ -131,15 +136,29 @@ def build_reference_oracle(ref_root=None):
             return None
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "alsfvm", "src")):
         return None
-    _run(["make", "-s", "-C", refbuild, "-j%d" % (os.cpu_count() or 4), "REF=" + ref_root])
+    _run(["make", "-s", "-C", refbuild, "-j%d" % (os.cpu_count() or 4), "REF=" + ref_root, "all", "cuda",
+          "NVCC=" + _nvcc()])
     return os.path.join(ORACLE_DIR, "_ref", "libalsref.so")
+
+
+def build_refcuda():
+    """The host driver of the reference's CUDA kernels (oracle/refcuda/)."""
+    src = os.path.join(ORACLE_DIR, "refcuda", "refcuda.cu")
+    hdr = os.path.join(ORACLE_DIR, "refcuda", "refcuda.h")
+    if os.path.exists(REFCUDA_LIB) and os.path.getmtime(REFCUDA_LIB) >= max(os.path.getmtime(src),
+                                                                            os.path.getmtime(hdr)):
+        return REFCUDA_LIB
+    _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-I" + os.path.dirname(src),
+                             src, "-o", REFCUDA_LIB])
+    return REFCUDA_LIB
 
 
 def build_all(verbose=False):
     lib = build_cuda(verbose=verbose)
     orc = build_oracle()
     ref = build_reference_oracle()
-    return lib, orc, ref
+    rcu = build_refcuda()
+    return lib, orc, ref, rcu
 
 
 if __name__ == "__main__":

@@ -255,6 +255,8 @@ static void reg_region_one(Registry& R) {
     R.region[FV_VARIANT][FV_EQ][FLUX][RC][DIM - 1] = &C0::launch_region;
 }
 
+// the schemes reg_dim registers (the double-float variant: the WENO / ENO
+// reconstructions with HLL, HLL3 and Godunov)
 template <int FLUX, int DIM>
 static void reg_region_dim(Registry& R) {
     reg_region_one<FLUX, RC_NONE, DIM>(R);
@@ -262,10 +264,12 @@ static void reg_region_dim(Registry& R) {
     reg_region_one<FLUX, RC_ENO2, DIM>(R);
     reg_region_one<FLUX, RC_ENO3, DIM>(R);
     reg_region_one<FLUX, RC_ENO4, DIM>(R);
+#if FV_VARIANT != 3
     reg_region_one<FLUX, RC_MC, DIM>(R);
     reg_region_one<FLUX, RC_MM, DIM>(R);
 #if FV_EQ != 0
     reg_region_one<FLUX, RC_WENOF2, DIM>(R);
+#endif
 #endif
 }
 #else
@@ -369,6 +373,7 @@ extern "C" void FV_REGION_FN(gbfv::Registry* R) {
     reg_region_dim<FL_GODUNOV, 1>(*R);
     reg_region_dim<FL_GODUNOV, 2>(*R);
     reg_region_dim<FL_GODUNOV, 3>(*R);
+#if FV_VARIANT != 3
     reg_region_dim<FL_CENTRAL, 1>(*R);
     reg_region_dim<FL_CENTRAL, 2>(*R);
     reg_region_dim<FL_CENTRAL, 3>(*R);
@@ -378,10 +383,13 @@ extern "C" void FV_REGION_FN(gbfv::Registry* R) {
     reg_region_dim<FL_ROE, 1>(*R);
     reg_region_dim<FL_ROE, 2>(*R);
     reg_region_dim<FL_ROE, 3>(*R);
+#endif
 #else
     reg_region_dim<FL_HLL, FV_EQ>(*R);
     reg_region_dim<FL_HLL3, FV_EQ>(*R);
+#if FV_VARIANT != 3
     reg_region_dim<FL_CENTRAL, FV_EQ>(*R);
+#endif
 #endif
 }
 #else

@@ -31,6 +31,7 @@ GBFV_TUNE_DECL(3, 0) GBFV_TUNE_DECL(3, 1) GBFV_TUNE_DECL(3, 2) GBFV_TUNE_DECL(3,
 GBFV_REGION_DECL(0, 0) GBFV_REGION_DECL(0, 1) GBFV_REGION_DECL(0, 2) GBFV_REGION_DECL(0, 3)
 GBFV_REGION_DECL(1, 0) GBFV_REGION_DECL(1, 1) GBFV_REGION_DECL(1, 2) GBFV_REGION_DECL(1, 3)
 GBFV_REGION_DECL(2, 0) GBFV_REGION_DECL(2, 1) GBFV_REGION_DECL(2, 2) GBFV_REGION_DECL(2, 3)
+GBFV_REGION_DECL(3, 0) GBFV_REGION_DECL(3, 1) GBFV_REGION_DECL(3, 2) GBFV_REGION_DECL(3, 3)
 
 namespace gbfv {
 
@@ -48,10 +49,11 @@ Registry& registry() {
         gbfv_tune_v1_e0(r); gbfv_tune_v1_e1(r); gbfv_tune_v1_e2(r); gbfv_tune_v1_e3(r);
         gbfv_tune_v2_e0(r); gbfv_tune_v2_e1(r); gbfv_tune_v2_e2(r); gbfv_tune_v2_e3(r);
         gbfv_tune_v3_e0(r); gbfv_tune_v3_e1(r); gbfv_tune_v3_e2(r); gbfv_tune_v3_e3(r);
-        // region kernels of the operator-level calls (no double-float variant)
+        // region kernels of the operator-level calls
         gbfv_region_v0_e0(r); gbfv_region_v0_e1(r); gbfv_region_v0_e2(r); gbfv_region_v0_e3(r);
         gbfv_region_v1_e0(r); gbfv_region_v1_e1(r); gbfv_region_v1_e2(r); gbfv_region_v1_e3(r);
         gbfv_region_v2_e0(r); gbfv_region_v2_e1(r); gbfv_region_v2_e2(r); gbfv_region_v2_e3(r);
+        gbfv_region_v3_e0(r); gbfv_region_v3_e1(r); gbfv_region_v3_e2(r); gbfv_region_v3_e3(r);
 
         return r;
     }();

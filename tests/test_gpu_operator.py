@@ -31,7 +31,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "flux_region.npz")
 CASES = ["euler1_hll3_weno2", "burgers_godunov_eno3", "euler2_hll3_weno2", "euler2_hll_eno2", "euler3_hll3_weno2"]
-DTYPE = {lib.FP64: np.float64, lib.FP64_EXACT: np.float64, lib.FP32: np.float32}
+DTYPE = {lib.FP64: np.float64, lib.FP64_EXACT: np.float64, lib.FP32: np.float32, lib.FP64_DF: np.float64}
 
 
 def to_dev(a):
@@ -107,7 +107,7 @@ def conserved_system_regions(n, g, dim):
     return regions
 
 
-@pytest.mark.parametrize("precision", [lib.FP64, lib.FP64_EXACT, lib.FP32])
+@pytest.mark.parametrize("precision", [lib.FP64, lib.FP64_EXACT, lib.FP32, lib.FP64_DF])
 @pytest.mark.parametrize("eq,n", [("euler1", (200, 1, 1)), ("euler2", (70, 45, 1)), ("euler3", (20, 18, 22))])
 def test_conserved_system_split_equals_whole_domain(cuda_device, eq, n, precision):
     import torch
