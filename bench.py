@@ -242,7 +242,46 @@ def run_reference(args):
                                        "%d steps on 1 thread; step loop only" % (done, max(args.warmup, 1),
                                                                                  threads, done1)},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["reference_gpu_path"] = time_reference_cuda(prim, args)
     print(json.dumps(line), flush=True)
+
+
+def time_reference_cuda(prim, args):
+    """The reference's own CUDA path on the same workload, beside its CPU
+    path: its kernels compiled from its sources for sm_103a (oracle/_ref/cuda)
+    and launched by oracle/refcuda in the order the reference's Simulator
+    launches them on the cuda platform, state resident on the device. Reported
+    next to the line's value, not as it."""
+    import numpy as np
+    from oracle import fvoracle, refcuda
+    why = refcuda.missing()
+    if why:
+        return {"unavailable": why}
+    g = 2
+    t = N + 2 * g
+    P = np.zeros((4, t, t))
+    P[:, g:g + N, g:g + N] = prim.reshape(4, N, N)
+    U0 = fvoracle.prim_to_cons("euler2", (N, N, 1), g, 1.4, P.reshape(4, -1))
+    steps = max(1, min(args.steps, 20))
+    try:
+        with refcuda.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", (N, N, 1), (0, 0, 0), (1, 1, 0),
+                            1.4, 0.4) as s:
+            s.set_state(U0)
+            s.run(1e9, 0, max(args.warmup, 3))
+            l0 = s.launches()
+            _, done = s.run(1e9, 0, steps)
+            ms = s.last_ms()
+            per_step = (s.launches() - l0) / max(done, 1)
+    except refcuda.RefCudaError as e:
+        return {"unavailable": str(e)}
+    return {"value": N * N * done / (ms * 1e-3), "unit": METRIC, "steps": done, "ms_per_step": ms / done,
+            "kernels_per_step": per_step, "blocking_copies_per_step": 3 * 5 * 2,
+            "executor": "the reference's CUDA kernels (NumericalFluxCUDA, ReconstructionCUDA, BoundaryCUDA, "
+                        "vector_operations, CUDACellComputer) built from its sources for sm_103a with its release "
+                        "flags; host sequence restated by oracle/refcuda (cub max and a blocking copy per direction "
+                        "and computeFlux call, thrust constraint reduce per step)",
+            "timing": "CUDA events on the legacy default stream around %d steps after %d warm-up steps; working "
+                      "set (seven FP64 volumes, 237 MB) larger than L2" % (done, max(args.warmup, 3))}
 
 
 def run_gpu(args):
