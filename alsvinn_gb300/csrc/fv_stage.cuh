@@ -121,23 +121,35 @@ template <int DIM, int TX, int TY, int TZ> struct Tile {
     static constexpr int T[3] = {TX, TY, TZ};
 };
 
-// Line buffers keep each item's NV values together, padded to a multiple of
-// 16 bytes (LinePad), so that a reconstruction's, a face's or a cell's
-// values move with 128-bit shared-memory accesses: one to four per item
-// instead of NV scalar accesses.
+// Line buffers keep each item's values together so that a reconstruction's,
+// a face's or a cell's values move with 128-bit shared-memory accesses: one
+// to four per item instead of NV scalar accesses. The first VEC values of an
+// item sit item-major in 16-byte vectors; when NV leaves a remainder of more
+// than one value short of a whole vector (five floats: 4 + 1), the remainder
+// (TAIL values per item) sits item-major in a second array after the first,
+// so no item carries more than one value of padding. A buffer holds CAP
+// items (the capacity rounded up to a multiple of 4, which keeps both parts
+// and the next buffer 16-byte aligned).
 template <class R, int NV> struct LinePad {
     static constexpr int per16 = (int)(16 / sizeof(R));
-    static constexpr int value = NV == 1 ? 1 : ((NV + per16 - 1) / per16) * per16;
+    static constexpr int rem = NV % per16;
+    static constexpr bool split = NV > 1 && rem != 0 && per16 - rem > 1;
+    static constexpr int VEC = NV == 1 ? 1 : (split ? NV - rem : ((NV + per16 - 1) / per16) * per16);
+    static constexpr int TAIL = split ? rem : 0;
+    static constexpr int value = VEC + TAIL;  // values per item
+    static constexpr int cap(int items) { return (items + 3) / 4 * 4; }
 };
 
 template <int NV, class R> __device__ __forceinline__ R lane_or_zero(const R* v, int i) {
     return i < NV ? v[i < NV ? i : 0] : R(0);
 }
 
-// p: item slot of LinePad<R, NV>::value values, 16-byte aligned when NV > 1.
-template <class R, int NV> __device__ __forceinline__ void line_put(R* p, const R* v) {
-    constexpr int P = LinePad<R, NV>::value;
-    if constexpr (P == 1) {
+// Item `item` of a line buffer of CAP items at `base` (16-byte aligned).
+template <class R, int NV, int CAP> __device__ __forceinline__ void line_put(R* base, int item, const R* v) {
+    using LP = LinePad<R, NV>;
+    constexpr int P = LP::VEC;
+    R* p = base + item * P;
+    if constexpr (NV == 1) {
         p[0] = v[0];
     } else if constexpr (std::is_same<R, float>::value) {
 #pragma unroll
@@ -156,11 +168,18 @@ template <class R, int NV> __device__ __forceinline__ void line_put(R* p, const 
             reinterpret_cast<float4*>(p)[c] = make_float4(a.hi, a.lo, b.hi, b.lo);
         }
     }
+    if constexpr (LP::TAIL > 0) {
+        R* t = base + CAP * P + item * LP::TAIL;
+#pragma unroll
+        for (int k = 0; k < LP::TAIL; ++k) t[k] = v[P + k];
+    }
 }
 
-template <class R, int NV> __device__ __forceinline__ void line_get(const R* p, R* v) {
-    constexpr int P = LinePad<R, NV>::value;
-    if constexpr (P == 1) {
+template <class R, int NV, int CAP> __device__ __forceinline__ void line_get(const R* base, int item, R* v) {
+    using LP = LinePad<R, NV>;
+    constexpr int P = LP::VEC;
+    const R* p = base + item * P;
+    if constexpr (NV == 1) {
         v[0] = p[0];
     } else if constexpr (std::is_same<R, float>::value) {
 #pragma unroll
@@ -186,6 +205,11 @@ template <class R, int NV> __device__ __forceinline__ void line_get(const R* p, 
             if (2 * c + 1 < NV) v[2 * c + 1 < NV ? 2 * c + 1 : 0] = R(q.z, q.w);
         }
     }
+    if constexpr (LP::TAIL > 0) {
+        const R* t = base + CAP * P + item * LP::TAIL;
+#pragma unroll
+        for (int k = 0; k < LP::TAIL; ++k) v[P + k] = t[k];
+    }
 }
 
 template <class R, int NV, int G, int DIM, int TX, int TY, int TZ>
@@ -203,8 +227,9 @@ struct SmemLayout {
     static constexpr size_t round128(size_t b) { return (b + 127) & ~(size_t)127; }
     static constexpr size_t box_bytes = sizeof(R) * (size_t)NV * HALO;  // one halo of every variable
     static constexpr size_t halo_bytes = round128(box_bytes);           // its slot (TMA wants 128 B aligned)
-    static constexpr int NVP = LinePad<R, NV>::value;  // values per line-buffer item
-    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)NVP * REC);
+    static constexpr int CAP = LinePad<R, NV>::cap(REC);  // items per line buffer
+    static constexpr int LINE = LinePad<R, NV>::value * CAP;  // values per line buffer
+    static constexpr size_t work_bytes = sizeof(R) * (2 * (size_t)LINE);
     // Dynamic shared memory per kernel, plus 128 bytes to align the base:
     //   plain staging:    halo | line buffers
     //   TMA staging:      halo | line buffers, which first hold the L0 halo of the stage-1 modes
@@ -247,13 +272,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
     constexpr int NFACE = (TD + 1) * (NT / TD);
     constexpr int DS = D == 0 ? 1 : (D == 1 ? SL::HX : SL::HX * SL::HY);
     constexpr int VS = SL::HALO;
-    constexpr int NVP = SL::NVP;
+    constexpr int CAP = SL::CAP;
     (void)NREC;
 
     // Work items: along x (D = 0) the cells of a line are consecutive; for
     // D >= 1 consecutive items step along x (p, the first other dimension),
     // so a warp's shared-memory accesses stay unit-stride in every phase.
-    // Line buffers hold item w at slot w (NVP values from w * NVP) in both layouts:
+    // Line buffers hold item w at slot w in both layouts:
     //   D = 0:  w = (o * LEN + a),            o = p + O1 q
     //   D >= 1: w = ((q * LEN + a) * O1 + p)  (faces: LEN -> TD + 1)
     // reconstruction of cells -1 .. TD along D
@@ -278,8 +303,8 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         const int s = ((c[2] + SL::GZ) * SL::HY + (c[1] + SL::GY)) * SL::HX + (c[0] + SL::GX);
         R l[NV], r[NV];
         reconstruct_cell<R, NV, RC>(su + s, VS, DS, l, r, gamma);
-        line_put<R, NV>(rl + w * NVP, l);
-        line_put<R, NV>(rr + w * NVP, r);
+        line_put<R, NV, CAP>(rl, w, l);
+        line_put<R, NV, CAP>(rr, w, r);
     }
     __syncthreads();
     // face b is the left face of tile cell b along D (between cells b-1 and b)
@@ -301,13 +326,13 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
             ir = il + O1;
         }
         R a[NV], bb[NV], F[NV];
-        line_get<R, NV>(rr + il * NVP, a);   // cell b-1 at its right face
-        line_get<R, NV>(rl + ir * NVP, bb);  // cell b at its left face
+        line_get<R, NV, CAP>(rr, il, a);   // cell b-1 at its right face
+        line_get<R, NV, CAP>(rl, ir, bb);  // cell b at its left face
         const R w = Ph::template face_flux<D>(a, bb, gamma, F);
 #pragma unroll
         // the flux of face b replaces the right value of cell b - 1 (item il),
         // which no other face reads
-        line_put<R, NV>(rr + il * NVP, F);
+        line_put<R, NV, CAP>(rr, il, F);
         // the face counts if both neighbours lie in the grid's interior range
         int c[3];
         c[D] = b;
@@ -336,8 +361,8 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         const int fli = D == 0 ? (p + O1 * q) * LEN + cd : (q * LEN + cd) * O1 + p;
         const int fri = D == 0 ? fli + 1 : fli + O1;
         R FL[NV], FR[NV];
-        line_get<R, NV>(rr + fli * NVP, FL);
-        line_get<R, NV>(rr + fri * NVP, FR);
+        line_get<R, NV, CAP>(rr, fli, FL);
+        line_get<R, NV, CAP>(rr, fri, FR);
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             const R fl = FL[k];
@@ -482,7 +507,7 @@ __device__ __forceinline__ void stage_tile_compute(const StageArgs& A, const int
     constexpr int CPT = CellsPerThread<NT, NTH>::value;
     constexpr bool kSame = std::is_same<R, C>::value;
     C* rl = work;
-    C* rr = rl + SL::NVP * SL::REC;
+    C* rr = rl + SL::LINE;
 
     const Grid& Gd = A.G;
     const int tid = threadIdx.x;

@@ -21,9 +21,15 @@ state arrays and write one), against the measured HBM copy bandwidth in
 MEASURED_PEAKS.json. The stage kernel's per-launch time comes from CUDA events
 the library records around every stage launch on its stream.
 
+The headline line also carries sub-objects measured in the same run: the
+double-float variant (`fp64_df`), the batched UQ ensemble (`uq`) and the
+serving stream (`serve`) to their end times, the Sod configuration to its end
+time (`sod`) and Taylor-Green 256^3 in FP64 and FP32 state (`tg`).
+
 --impl reference times the reference's CPU algorithm (the oracle restatement,
 bit-identical to the reference CPU path) on all host cores for the same
-workload.
+workload, and beside it the reference's own CUDA kernels built for sm_103a
+(`reference_gpu_path`).
 """
 import argparse
 import json
@@ -453,6 +459,11 @@ def run_gpu(args):
         if world == 1 and args.headline_serve_requests > 0:
             line["serve"] = measure_serve(args.headline_serve_requests, args.serve_rate, args.serve_chunk,
                                           args.serve_plain)
+        # the other two finite-volume configurations: Sod 2048 to its end
+        # time, Taylor-Green 256^3 (FP64 and FP32 state)
+        if world == 1 and args.headline_fv:
+            line["sod"] = measure_sod(warmup=1)
+            line["tg"] = {"fp64": measure_tg(256, "fp64", 5, 3), "fp32": measure_tg(256, "fp32", 5, 3)}
         print(json.dumps(line), flush=True)
     else:
         s.close()
@@ -461,60 +472,123 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def run_tg(args):
+def measure_tg(n, precision_name, steps, warmup, candidate=-1):
     """Taylor-Green (euler3, WENO2, HLL3, SSP-RK3, CFL 0.4, periodic on
-    [0, 2 pi]^3) on n^3 cells: `--warmup` steps, then `--steps` timed steps
-    with CUDA events on the solver's stream (the L2 flushed before each);
-    the autotuner's table, or `--candidate` pinned (profiler runs)."""
+    [0, 2 pi]^3) on n^3 cells: `warmup` steps, then `steps` timed steps with
+    CUDA events on the solver's stream (the L2 flushed before each); the
+    autotuner's table, or `candidate` pinned (profiler runs). Roofline of the
+    stage launch as for the headline: 8 nvar b / 3 algorithmic bytes per cell
+    per stage (5 variables)."""
     import math
     import torch
     from alsvinn_gb300 import lib
 
-    n = args.tg_n
     precision = {"fp64": lib.FP64, "fp32": lib.FP32, "fp64-df": lib.FP64_DF, "fp64-exact": lib.FP64_EXACT}[
-        args.precision]
+        precision_name]
+    elem = 4 if precision_name == "fp32" else 8
     s = lib.Solver("euler3", "hll3", "weno2", "rungekutta3", "periodic", (n, n, n), (0, 0, 0), (2 * math.pi,) * 3,
                    gamma=1.4, cfl=0.4, precision=precision)
-    s.set_primitive(lib.init_taylor_green(n))
-    cands = s.candidates()
-    if args.candidate >= 0:
-        s.select_candidate(args.candidate)
-        chosen, tune_ms = args.candidate, [-1.0] * len(cands)
-    else:
-        chosen, tune_ms = s.autotune()
-    s.advance(1e9, 0, args.warmup)
-    stream = torch.cuda.ExternalStream(s.stream())
-    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    s.profile(True)
-    s.profile_read()
-    total = 0.0
-    with ClockSampler(0) as clocks:
-        for i in range(args.steps):
-            a0 = torch.cuda.Event(enable_timing=True)
-            a1 = torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                flush.fill_(i & 0xFF)
-                a0.record(stream)
-            s.advance(1e9, 0, 1)
-            with torch.cuda.stream(stream):
-                a1.record(stream)
-            torch.cuda.synchronize()
-            total += a0.elapsed_time(a1)
-    stage_ms, stage_n, _ = s.profile_read()
-    s.close()
+    try:
+        s.set_primitive(lib.init_taylor_green(n))
+        cands = s.candidates()
+        if candidate >= 0:
+            s.select_candidate(candidate)
+            chosen, tune_ms = candidate, [-1.0] * len(cands)
+        else:
+            chosen, tune_ms = s.autotune()
+        s.advance(1e9, 0, warmup)
+        stream = torch.cuda.ExternalStream(s.stream())
+        flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        s.profile(True)
+        s.profile_read()
+        total = 0.0
+        with ClockSampler(0) as clocks:
+            for i in range(steps):
+                a0 = torch.cuda.Event(enable_timing=True)
+                a1 = torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    flush.fill_(i & 0xFF)
+                    a0.record(stream)
+                s.advance(1e9, 0, 1)
+                with torch.cuda.stream(stream):
+                    a1.record(stream)
+                torch.cuda.synchronize()
+                total += a0.elapsed_time(a1)
+        stage_ms, stage_n, _ = s.profile_read()
+    finally:
+        s.close()
+    del flush
     cells = n ** 3
-    line = {"metric": METRIC, "value": cells * args.steps / (total * 1e-3), "unit": METRIC, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
-            "data": "synthetic (Taylor-Green initial data)",
-            "config": {"workload": "tg3d_%d_euler3_weno2_hll3_rk3" % n, "grid": [n, n, n],
-                       "precision": args.precision, "l2": "flushed before every timed step (512 MiB memset)"},
+    launch_ms = stage_ms / max(stage_n, 1)
+    alg = 8 * 5 * elem / 3 * cells
+    peak = measured_peaks()
+    return {"metric": METRIC, "value": cells * steps / (total * 1e-3), "unit": METRIC, "steps": steps,
+            "warmup": warmup, "ms_per_step": total / steps, "dtype": precision_name,
+            "workload": "tg3d_%d_euler3_weno2_hll3_rk3" % n, "grid": [n, n, n],
+            "l2": "flushed before every timed step (512 MiB memset)",
             "stage_kernel": {"candidate": chosen, "tile": list(cands[chosen][0]), "threads": cands[chosen][1],
                              "tma": cands[chosen][2],
                              "autotune_ms_per_launch": [{"tile": list(c[0]), "threads": c[1], "tma": c[2], "ms": m}
                                                         for c, m in zip(cands, tune_ms)]},
-            "stage_launch_ms": stage_ms / max(stage_n, 1), "clocks": clocks.summary()}
+            "stage_launch_ms": launch_ms,
+            "roofline": {"bound": "hbm", "achieved": alg / (launch_ms * 1e-3) / 1e9, "peak": peak[0], "unit": "GB/s",
+                         "frac": alg / (launch_ms * 1e-3) / 1e9 / peak[0], "alg_bytes_per_launch": alg,
+                         "peak_source": peak[1],
+                         "note": "FP64 builds are FP64-pipe bound (77 %% of the pipe, "
+                                 "profiles/stage_kernel_tg128_fp64.md)" if elem == 8 else
+                                 "FP32: arithmetic-bound stencil"},
+            "clocks": clocks.summary()}
+
+
+def run_tg(args):
+    """`--workload tg`: the Taylor-Green measurement as its own line."""
+    m = measure_tg(args.tg_n, args.precision, args.steps, args.warmup, args.candidate)
+    line = {"metric": METRIC, "value": m["value"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.precision, "data": "synthetic (Taylor-Green initial data)",
+            "config": {"workload": m["workload"], "grid": m["grid"], "precision": args.precision, "l2": m["l2"]},
+            "stage_kernel": m["stage_kernel"], "stage_launch_ms": m["stage_launch_ms"], "roofline": m["roofline"],
+            "clocks": m["clocks"]}
     print(json.dumps(line), flush=True)
+
+
+def measure_sod(warmup=1):
+    """The Sod configuration (euler1, 2048 cells on [-5, 5], Neumann, WENO2,
+    HLL3, SSP-RK3, CFL 0.475) run from t = 0 to its end time 1.3 in FP64 with
+    the writer's dt clamp (one save): `warmup` untimed whole runs, then one
+    timed run from the initial data, CUDA events on the solver's stream around
+    the advance. A 2048-cell grid is latency bound (one 16-step CUDA graph per
+    16 steps, a few microseconds per stage launch)."""
+    import torch
+    from alsvinn_gb300 import lib
+
+    prim = lib.init_sod(2048)
+    s = lib.Solver("euler1", "hll3", "weno2", "rungekutta3", "neumann", (2048, 1, 1), (-5, 0, 0), (5, 1, 1),
+                   gamma=1.4, cfl=0.475, precision=lib.FP64)
+    try:
+        for _ in range(warmup):
+            s.set_primitive(prim)
+            s.advance(1.3, 1)
+        s.set_primitive(prim)
+        stream = torch.cuda.ExternalStream(s.stream())
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with ClockSampler(0) as clocks:
+            with torch.cuda.stream(stream):
+                a0.record(stream)
+            s.advance(1.3, 1)
+            with torch.cuda.stream(stream):
+                a1.record(stream)
+            torch.cuda.synchronize()
+        ms = a0.elapsed_time(a1)
+        t, steps, _ = s.time()
+    finally:
+        s.close()
+    return {"metric": METRIC, "value": 2048 * steps / (ms * 1e-3), "unit": METRIC, "dtype": "f64",
+            "workload": "sod1d_2048_euler1_weno2_hll3_rk3_to_t1.3", "end_time": t, "steps": steps,
+            "ms_to_end_time": ms, "us_per_step": 1e3 * ms / steps, "warmup_runs": warmup,
+            "bound": "launch / latency (2048 cells: 8 CTAs per stage)", "clocks": clocks.summary()}
 
 
 UQ_SIZES = (128, 256, 512)
@@ -913,6 +987,8 @@ def main():
                     help="members of the UQ ensemble measured to T inside the default run (0: skip)")
     ap.add_argument("--headline-serve-requests", type=int, default=96,
                     help="requests of the serving stream measured inside the default run (0: skip)")
+    ap.add_argument("--headline-fv", type=int, default=1,
+                    help="add the Sod 2048 and Taylor-Green 256^3 measurements to the headline line (0: skip)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
