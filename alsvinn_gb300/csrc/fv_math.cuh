@@ -150,10 +150,10 @@ __device__ __forceinline__ bool df_range(double x, int max_exp) {  // |x| < 2^ma
 }
 
 template <bool CORRECT>
-__device__ __forceinline__ void wave_speeds_df(double wl, double wr, double ul, double ur, double pl, double pr,
-                                               double il, double ir, double rl, double rr, double gamma,
+__device__ __forceinline__ void wave_speeds_df(const dfloat& Wl, const dfloat& Wr, double ul, double ur, double pl,
+                                               double pr, double il, double ir, double rl, double rr, double gamma,
                                                double& sL, double& sR) {
-    const dfloat Wl(wl), Wr(wr), Ul(ul), Ur(ur), Pl(pl), Pr(pr), Il(il), Ir(ir), G(gamma);
+    const dfloat Ul(ul), Ur(ur), Pl(pl), Pr(pr), Il(il), Ir(ir), G(gamma);
     const dfloat winv = dfloat(1) / (Wl + Wr);
     const dfloat ud = (Wl * Ul + Wr * Ur) * winv;
     const dfloat p = (Wl * Pl + Wr * Pr) * winv;
@@ -203,26 +203,53 @@ template <> __device__ __forceinline__ void inv_sqrt_pair<float>(float rho, floa
         w = sqrtf(rho);
     }
 }
-template <> __device__ __forceinline__ void inv_sqrt_pair<double>(double rho, double& rinv, double& w) {
+// FP64: sqrt(rho) enters only the wave-speed estimates, which the fast
+// policy evaluates in double-float (wave_speeds_df), so the root is formed
+// there directly: the double-float split of rho and its double-float square
+// root run on the FP32 and integer pipes, and the FP64 pipe computes only the
+// reciprocal (three FMAs after the hardware approximation, instead of the
+// five of a refined reciprocal square root plus two products). States outside
+// the double-float range (df_root_range) take the FP64 formulas, which form
+// the root themselves (wave_root).
+__device__ __forceinline__ void inv_sqrt_pair(double rho, double& rinv, dfloat& w) {
     if (in_rsqrt_range(rho)) {
-        const double rs = rsqrt_nr(rho);
-        rinv = rs * rs;
-        w = rho * rs;
+        rinv = rcp_(rho);
+        w = sqrt(dfloat(rho));
     } else {
         rinv = 1.0 / rho;
-        w = sqrt(rho);
+        w = dfloat(0.f);
     }
+}
+
+// 2^-100 <= rho < 2^120: the double-float root of rho and the wave-speed
+// products stay normal FP32 numbers
+__device__ __forceinline__ bool df_root_range(double rho) {
+    constexpr long long lo = (1023LL - 100) << 52, hi = (1023LL + 120) << 52;
+    return (unsigned long long)(dbits(rho) - lo) < (unsigned long long)(hi - lo);
 }
 
 // ---------------------------------------------------------------- Euler
 
 // Conserved variables of one cell side plus the derived pressure and velocity
 // (Euler<nsd>::computeExtra, alsfvm/include/alsfvm/equation/euler/Euler.hpp:204-211).
+// sqrt(rho) as the fast policy keeps it: a double-float for the FP64 state
+// (see inv_sqrt_pair), the state's own type otherwise
+template <class R> struct WaveRoot { using type = R; };
+template <> struct WaveRoot<double> { using type = dfloat; };
+
 template <class R, int NSD> struct EulerState {
     R rho, m[NSD], E, p, u[NSD];
-    R rinv;  // 1/rho (fast policy only)
-    R w;     // sqrt(rho) (fast policy only)
+    R rinv;                        // 1/rho (fast policy only)
+    typename WaveRoot<R>::type w;  // sqrt(rho) (fast policy only)
 };
+
+// sqrt(rho) in the state's type, for the FP64 formulas of the fast policy
+template <class R, int NSD> __device__ __forceinline__ R wave_root(const EulerState<R, NSD>& s) {
+    if constexpr (std::is_same<R, double>::value)
+        return sqrt_(s.rho);
+    else
+        return s.w;
+}
 
 template <class R, int NSD>
 __device__ __forceinline__ void euler_extra(EulerState<R, NSD>& a, R gamma) {
@@ -332,7 +359,7 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
     } else {
         bool done = false;
         if constexpr (std::is_same<R, double>::value) {
-            if (df_range(L.w, 60) && df_range(Rs.w, 60) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
+            if (df_root_range(L.rho) && df_root_range(Rs.rho) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
                 df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
                 wave_speeds_df<true>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
                                      speedLeft, speedRight);
@@ -340,8 +367,8 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
             }
         }
         if (!done) {
-            const R waveLeft = L.w;
-            const R waveRight = Rs.w;
+            const R waveLeft = wave_root(L);
+            const R waveRight = wave_root(Rs);
             const R winv = rcp_(waveLeft + waveRight);
             const R ud = fma(waveLeft, L.u[D], waveRight * Rs.u[D]) * winv;
             const R p = fma(waveLeft, L.p, waveRight * Rs.p) * winv;
@@ -426,9 +453,9 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
                                       R gamma, R* F) {
     constexpr int NV = NSD + 2;
     R speedLeft, speedRight;
-    const R waveLeft = kExact ? sqrt(L.rho) : L.w;
-    const R waveRight = kExact ? sqrt(Rs.rho) : Rs.w;
     if (kExact) {
+        const R waveLeft = sqrt(L.rho);
+        const R waveRight = sqrt(Rs.rho);
         const R rho = (L.rho + Rs.rho) / R(2);
         const R ud = (waveLeft * L.u[D] + waveRight * Rs.u[D]) / (waveLeft + waveRight);
         const R p = (L.p * waveLeft + Rs.p * waveRight) / (waveLeft + waveRight);
@@ -438,7 +465,7 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
     } else {
         bool done = false;
         if constexpr (std::is_same<R, double>::value) {
-            if (df_range(L.w, 60) && df_range(Rs.w, 60) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
+            if (df_root_range(L.rho) && df_root_range(Rs.rho) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
                 df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
                 wave_speeds_df<false>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
                                       speedLeft, speedRight);
@@ -446,6 +473,8 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
             }
         }
         if (!done) {
+            const R waveLeft = wave_root(L);
+            const R waveRight = wave_root(Rs);
             const R winv = rcp_(waveLeft + waveRight);
             const R ud = fma(waveLeft, L.u[D], waveRight * Rs.u[D]) * winv;
             const R p = fma(L.p, waveLeft, Rs.p * waveRight) * winv;
