@@ -149,11 +149,26 @@ __device__ __forceinline__ bool df_range(double x, int max_exp) {  // |x| < 2^ma
     return (dbits(x) & kAbsMask) < ((long long)(1023 + max_exp) << 52);
 }
 
+// The double-float split of an input of those coefficients: a magnitude
+// below 2^-80 (a velocity or a one-sided difference far below the O(1) terms
+// it is added to, or a zero) splits to a signed zero on the integer pipes;
+// the general split takes conversion instructions there, FP64-pipe
+// instructions that would then run for the few lanes of a warp holding such
+// values. The coefficients do not change: 2^-80 is below their double-float
+// resolution next to the terms beside it (eps = 1e-8 in the WENO weights,
+// the sound speeds in the wave speeds).
+__device__ __forceinline__ dfloat df_coef(double v) {
+    const unsigned hw = (unsigned)((unsigned long long)__double_as_longlong(v) >> 32);
+    if (((hw >> 20) & 0x7ffu) < 1023u - 80u) return dfloat(__uint_as_float(hw & 0x80000000u), 0.f);
+    return dfloat(v);
+}
+
 template <bool CORRECT>
 __device__ __forceinline__ void wave_speeds_df(const dfloat& Wl, const dfloat& Wr, double ul, double ur, double pl,
                                                double pr, double il, double ir, double rl, double rr, double gamma,
                                                double& sL, double& sR) {
-    const dfloat Ul(ul), Ur(ur), Pl(pl), Pr(pr), Il(il), Ir(ir), G(gamma);
+    const dfloat Ul = df_coef(ul), Ur = df_coef(ur), Pl = df_coef(pl), Pr = df_coef(pr), Il(il), Ir(ir),
+                 G(gamma);
     const dfloat winv = dfloat(1) / (Wl + Wr);
     const dfloat ud = (Wl * Ul + Wr * Ur) * winv;
     const dfloat p = (Wl * Pl + Wr * Pr) * winv;
@@ -765,7 +780,7 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
                 bool done = false;
                 if constexpr (std::is_same<R, double>::value) {
                     if (df_range(d0, 30) && df_range(d1, 30)) {
-                        const dfloat D0(d0), D1(d1), E(FV_WENO_EPSILON);
+                        const dfloat D0 = df_coef(d0), D1 = df_coef(d1), E(FV_WENO_EPSILON);
                         const dfloat e0 = E + D0 * D0, e1 = E + D1 * D1;
                         const dfloat s0 = e0 * e0, s1 = e1 * e1;
                         const dfloat iL = dfloat(1) / (s1 + s0 + s0), iR = dfloat(1) / (s1 + s1 + s0);
