@@ -163,12 +163,65 @@ __device__ __forceinline__ dfloat df_coef(double v) {
     return dfloat(v);
 }
 
-template <bool CORRECT>
+// A double-float coefficient back to a double on the integer pipes: hi's 24
+// significant bits and lo's aligned under them in one 53-bit integer
+// significand (a normalised pair has lo at least 24 bits below hi's leading
+// bit; lo's bits past the 53rd are dropped, an error under one ulp), with the
+// one-bit renormalisation a lo of the other sign can need. A zero lo widens
+// hi alone; pairs with a subnormal or non-finite part take the FP64 addition.
+__device__ __forceinline__ double df_coef_to_double(const dfloat& a) {
+    const unsigned uh = __float_as_uint(a.hi), ul = __float_as_uint(a.lo);
+    const unsigned eh = (uh >> 23) & 0xffu, el = (ul >> 23) & 0xffu;
+    if (eh - 1u < 254u) {
+        if ((ul << 1) == 0u) return df_widen(a.hi);
+        const int sh = (int)eh - (int)el;
+        if (el - 1u < 254u && sh >= 24 && sh < 64) {
+            const unsigned long long mh = (unsigned long long)((uh & 0x7fffffu) | 0x800000u) << 29;
+            const unsigned long long mlo = (unsigned long long)((ul & 0x7fffffu) | 0x800000u);
+            const unsigned long long ml = sh <= 29 ? mlo << (29 - sh) : mlo >> (sh - 29);
+            unsigned long long m;
+            int e = (int)eh - 127 + 1023;
+            if ((uh ^ ul) & 0x80000000u) {
+                m = mh - ml;
+                if (m < (1ull << 52)) {
+                    m <<= 1;
+                    e -= 1;
+                }
+            } else {
+                m = mh + ml;
+            }
+            return __longlong_as_double((long long)(((unsigned long long)(uh & 0x80000000u) << 32) |
+                                                    ((unsigned long long)e << 52) | (m & ((1ull << 52) - 1))));
+        }
+    }
+    return df_widen(a.hi) + df_widen(a.lo);
+}
+
+// The integer-pipe edges of the double-float coefficients (df_coef,
+// df_coef_to_double) pay in the 1D and 2D kernels; the 3D kernels (five
+// variables, 108 registers, two CTAs per SM) have too few warps to hide
+// their integer latency and keep the general split and the FP64 addition.
+template <int NSD> struct CoefEdges { static constexpr bool integer = NSD <= 2; };
+
+template <bool INT> __device__ __forceinline__ dfloat coef_in(double v) {
+    if constexpr (INT)
+        return df_coef(v);
+    else
+        return dfloat(v);
+}
+template <bool INT> __device__ __forceinline__ double coef_out(const dfloat& a) {
+    if constexpr (INT)
+        return df_coef_to_double(a);
+    else
+        return (double)a;
+}
+
+template <bool CORRECT, bool INT>
 __device__ __forceinline__ void wave_speeds_df(const dfloat& Wl, const dfloat& Wr, double ul, double ur, double pl,
                                                double pr, double il, double ir, double rl, double rr, double gamma,
                                                double& sL, double& sR) {
-    const dfloat Ul = df_coef(ul), Ur = df_coef(ur), Pl = df_coef(pl), Pr = df_coef(pr), Il(il), Ir(ir),
-                 G(gamma);
+    const dfloat Ul = coef_in<INT>(ul), Ur = coef_in<INT>(ur), Pl = coef_in<INT>(pl), Pr = coef_in<INT>(pr),
+                 Il(il), Ir(ir), G(gamma);
     const dfloat winv = dfloat(1) / (Wl + Wr);
     const dfloat ud = (Wl * Ul + Wr * Ur) * winv;
     const dfloat p = (Wl * Pl + Wr * Pr) * winv;
@@ -176,8 +229,8 @@ __device__ __forceinline__ void wave_speeds_df(const dfloat& Wl, const dfloat& W
     const dfloat cs = sqrt((G + G) * p / (dfloat(rl) + dfloat(rr)));
     dfloat corr(0.f);
     if (CORRECT) corr = dfloat(0.5f) * fmax(dfloat(0), Ul - Ur);
-    sL = (double)fmin(Ul + corr - cl, ud - cs);
-    sR = (double)fmax(Ur - corr + cr, ud + cs);
+    sL = coef_out<INT>(fmin(Ul + corr - cl, ud - cs));
+    sR = coef_out<INT>(fmax(Ur - corr + cr, ud + cs));
 }
 
 // sqrt(x) = x / sqrt(x) for positive finite x; zero, negative and NaN
@@ -376,7 +429,7 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
         if constexpr (std::is_same<R, double>::value) {
             if (df_root_range(L.rho) && df_root_range(Rs.rho) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
                 df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
-                wave_speeds_df<true>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
+                wave_speeds_df<true, CoefEdges<NSD>::integer>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
                                      speedLeft, speedRight);
                 done = true;
             }
@@ -482,7 +535,7 @@ __device__ __forceinline__ R flux_hll(const EulerState<R, NSD>& L, const EulerSt
         if constexpr (std::is_same<R, double>::value) {
             if (df_root_range(L.rho) && df_root_range(Rs.rho) && df_range(L.u[D], 60) && df_range(Rs.u[D], 60) &&
                 df_range(L.p, 60) && df_range(Rs.p, 60) && df_range(L.rinv, 60) && df_range(Rs.rinv, 60)) {
-                wave_speeds_df<false>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
+                wave_speeds_df<false, CoefEdges<NSD>::integer>(L.w, Rs.w, L.u[D], Rs.u[D], L.p, Rs.p, L.rinv, Rs.rinv, L.rho, Rs.rho, gamma,
                                       speedLeft, speedRight);
                 done = true;
             }
@@ -780,14 +833,15 @@ __device__ __forceinline__ void reconstruct_cell(const R* __restrict__ u, int vs
                 bool done = false;
                 if constexpr (std::is_same<R, double>::value) {
                     if (df_range(d0, 30) && df_range(d1, 30)) {
-                        const dfloat D0 = df_coef(d0), D1 = df_coef(d1), E(FV_WENO_EPSILON);
+                        constexpr bool kInt = CoefEdges<NV - 2>::integer;  // Euler: NV = NSD + 2
+                        const dfloat D0 = coef_in<kInt>(d0), D1 = coef_in<kInt>(d1), E(FV_WENO_EPSILON);
                         const dfloat e0 = E + D0 * D0, e1 = E + D1 * D1;
                         const dfloat s0 = e0 * e0, s1 = e1 * e1;
                         const dfloat iL = dfloat(1) / (s1 + s0 + s0), iR = dfloat(1) / (s1 + s1 + s0);
-                        h0L = (double)(dfloat(0.5f) * s1 * iL);
-                        h1L = (double)(s0 * iL);
-                        h0R = (double)(s1 * iR);
-                        h1R = (double)(dfloat(0.5f) * s0 * iR);
+                        h0L = coef_out<kInt>(dfloat(0.5f) * s1 * iL);
+                        h1L = coef_out<kInt>(s0 * iL);
+                        h0R = coef_out<kInt>(s1 * iR);
+                        h1R = coef_out<kInt>(dfloat(0.5f) * s0 * iR);
                         done = true;
                     }
                 }

@@ -329,7 +329,6 @@ __device__ __forceinline__ void tile_direction(const R* su, R* rl, R* rr, R* acc
         line_get<R, NV, CAP>(rr, il, a);   // cell b-1 at its right face
         line_get<R, NV, CAP>(rl, ir, bb);  // cell b at its left face
         const R w = Ph::template face_flux<D>(a, bb, gamma, F);
-#pragma unroll
         // the flux of face b replaces the right value of cell b - 1 (item il),
         // which no other face reads
         line_put<R, NV, CAP>(rr, il, F);
