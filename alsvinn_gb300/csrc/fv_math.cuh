@@ -452,6 +452,43 @@ __device__ __forceinline__ R flux_hll3(const EulerState<R, NSD>& L, const EulerS
         // FP32 and double-float: evaluate only the point flux a branch uses
         return hll3_branches_one_side<R, NSD, D>(L, Rs, speedLeft, speedRight, F);
     }
+    if constexpr (!kExact) {
+        // FP64: the contact speed first, then one point flux -- of the side
+        // every branch but the zero-speed one uses (the upwind state, or the
+        // star state's side of sm) -- selected without branching, and the
+        // star's transverse velocities as ((uR - sR) mR - (uL - sL) mL) / a
+        const R udl = L.u[D] - speedLeft;
+        const R udr = Rs.u[D] - speedRight;
+        const R ainv = rcp_(fma(udr, Rs.rho, -(udl * L.rho)));
+        const R sm = (fma(Rs.m[D], udr, -(L.m[D] * udl)) + Rs.p - L.p) * ainv;
+        const bool upLeft = gt0(speedLeft), upRight = lt0(speedRight);
+        const bool useLeft = upLeft || (!upRight && ge0(sm));
+        const EulerState<R, NSD>& S = useLeft ? L : Rs;
+        R fS[NV];
+        euler_point_flux<R, NSD, D>(S, fS);
+        if (is0(speedLeft)) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) F[k] = R(0);
+        } else if (upLeft || upRight) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) F[k] = fS[k];
+        } else {
+            const R s = useLeft ? speedLeft : speedRight;
+            const R ud = useLeft ? udl : udr;
+            const R sinv = rcp_(sm - s);
+            const R mid0 = S.rho * ud * sinv;
+            F[0] = fma(s, mid0 - S.rho, fS[0]);
+#pragma unroll
+            for (int k = 0; k < NSD; ++k) {
+                const R usk = (k == D) ? sm : fma(udr, Rs.m[k], -(udl * L.m[k])) * ainv;
+                F[1 + k] = fma(s, fma(mid0, usk, -S.m[k]), fS[1 + k]);
+            }
+            const R pp = fma(S.rho * (S.u[D] - sm), ud, S.p);
+            const R eS = fma(ud, S.E, fma(S.p, S.u[D], -(pp * sm)));
+            F[1 + NSD] = fma(s, fma(eS, sinv, -S.E), fS[1 + NSD]);
+        }
+        return fmax_(fabs(speedLeft), fabs(speedRight));
+    }
     R fluxLeft[NV], fluxRight[NV];
     euler_point_flux<R, NSD, D>(L, fluxLeft);
     euler_point_flux<R, NSD, D>(Rs, fluxRight);
