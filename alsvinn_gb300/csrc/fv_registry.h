@@ -51,7 +51,7 @@ struct StageCandidate {
     int nv;       // variables per cell (the box's fourth extent)
     int min_blocks;  // resident CTAs per SM the single-grid kernel is compiled for
 };
-constexpr int kMaxCandidates = 6;
+constexpr int kMaxCandidates = 8;
 
 struct Registry {
     // [variant][equation][flux][recon][dim-1][candidate]

@@ -312,6 +312,9 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 2, 64, 8, 1, 256, true>::add(R, FLUX, RC);
         // 32 x 16 compiled for three resident CTAs per SM (register cap)
         Cand<E, FLUX, RC, 2, 32, 16, 1, 256, true, 3>::add(R, FLUX, RC);
+        // the same with per-thread loads: the first stage of an in-place
+        // host step reads mapped host memory, which TMA does not stage
+        Cand<E, FLUX, RC, 2, 32, 16, 1, 256, false, 3>::add(R, FLUX, RC);
     } else {
         Cand<E, FLUX, RC, 3, 8, 8, 4, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 3, 16, 8, 4, 256, true>::add(R, FLUX, RC);

@@ -957,9 +957,20 @@ static int advance_host_mapped(gbfv_solver* s, void* hdev, double end_time, int 
     const StageCandidate* c = candidates(s->var, s->eq, s->fl, s->rc, s->G.dim, &ncand);
     const StageCandidate& stage = c[s->cand < 0 ? 0 : s->cand];
     cudaStream_t q = s->stream;
+    // the first stage reads host memory with per-thread loads: the chosen
+    // candidate if it loads that way, else the fastest such candidate the
+    // autotuner timed (candidate 0 untuned)
+    int first = 0;
+    if (s->cand >= 0 && !c[s->cand].tma) {
+        first = s->cand;
+    } else {
+        for (int i = 1; i < ncand && i < (int)s->tune_ms.size(); ++i)
+            if (!c[i].tma && s->tune_ms[i] >= 0 && (s->tune_ms[first] < 0 || s->tune_ms[i] < s->tune_ms[first]))
+                first = i;
+    }
     StageArgs a = stage_args(s, s->st, hdev, hdev, nullptr, s->L, MODE_L, 0);
     a.copy_in = s->U;
-    STAGE_TRY(launch_stage(s, c[0], a));
+    STAGE_TRY(launch_stage(s, c[first], a));
     dt_kernel<<<1, 1, 0, q>>>(s->st, P);
     CUDA_TRY(cudaGetLastError());
     s->launches += 2;  // dt + finish

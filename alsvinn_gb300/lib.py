@@ -848,7 +848,7 @@ class Batch:
         _check(load().gbfv_batch_current_candidate(self.h, ctypes.byref(i), ctypes.byref(m)))
         return i.value, m.value
 
-    def autotune_result(self, n=6):
+    def autotune_result(self, n=8):
         ms = (ctypes.c_double * n)()
         _check(load().gbfv_batch_autotune_result(self.h, ms, n))
         return list(ms)
