@@ -139,6 +139,28 @@ def test_product_fp64_matches_the_reference_cuda_path(refcuda_ready, name):
     assert (err <= 1e-10).all(), err
 
 
+def test_product_fp64_matches_the_reference_cuda_path_at_full_size(refcuda_ready):
+    """Kelvin-Helmholtz 1024 x 1024, the benchmark workload: three SSP-RK3
+    steps of the reference's CUDA path and of the product's FP64 solver from
+    the same initial data agree within 1e-10 relative L1 per variable, with
+    the same end time."""
+    n = (1024, 1024, 1)
+    prim = workloads.kh_prim(1024, fvoracle.uniform(40, 0))
+    with refcuda.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", n, (0, 0, 0), (1, 1, 0)) as r:
+        r.set_state(padded_conserved("euler2", n, prim))
+        rt, rsteps = r.run(1e9, 0, 3)
+        R = r.get_state()
+    with lib.Solver("euler2", "hll3", "weno2", "rungekutta3", "periodic", n, (0, 0, 0), (1, 1, 0), cfl=0.4,
+                    precision=lib.FP64) as s:
+        s.set_primitive(prim)
+        s.advance(1e9, 0, 3)
+        t, steps, _ = s.time()
+        U = s.get_state()
+    assert steps == rsteps == 3 and abs(t - rt) <= 1e-12 * rt
+    err = rel_l1(interior(U, n, G), interior(R, n, G))
+    assert (err <= 1e-10).all(), err
+
+
 def test_reference_cuda_launches_per_step(refcuda_ready):
     """2D RK3: per stage five computeFlux calls (the interior and four side
     strips), each a makeZero plus, per direction, a reconstruction, a face
