@@ -249,6 +249,7 @@ def run_reference(args):
                                                                                  threads, done1)},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     line["reference_gpu_path"] = time_reference_cuda(prim, args)
+    line["reference_gpu_path_other"] = time_reference_cuda_other(args)
     print(json.dumps(line), flush=True)
 
 
@@ -288,6 +289,58 @@ def time_reference_cuda(prim, args):
                         "and computeFlux call, thrust constraint reduce per step)",
             "timing": "CUDA events on the legacy default stream around %d steps after %d warm-up steps; working "
                       "set (seven FP64 volumes, 237 MB) larger than L2" % (done, max(args.warmup, 3))}
+
+
+def time_reference_cuda_other(args):
+    """The reference's CUDA path on the other two finite-volume
+    configurations, for comparison with the headline line's `sod` and `tg`
+    sub-objects: Sod 2048 from t = 0 to 1.3 (one save's dt clamp) and
+    Taylor-Green 256^3 (2 steps after 1), FP64, CUDA events around the runs."""
+    import math
+    import numpy as np
+    import workloads
+    from oracle import fvoracle, refcuda
+    why = refcuda.missing()
+    if why:
+        return {"unavailable": why}
+    out = {}
+    g = 2
+    try:
+        prim = workloads.sod_prim(2048)
+        P = np.zeros((3, 2048 + 2 * g))
+        P[:, g:g + 2048] = prim
+        U0 = fvoracle.prim_to_cons("euler1", (2048, 1, 1), g, 1.4, P)
+        with refcuda.Solver("euler1", "hll3", "weno2", "rungekutta3", "neumann", (2048, 1, 1), (-5, 0, 0),
+                            (5, 1, 1), 1.4, 0.475) as s:
+            s.set_state(U0)
+            s.run(1.3, 1, 0)  # warm-up run
+            s.set_state(U0)
+            t, done = s.run(1.3, 1, 0)
+            out["sod2048_to_t1.3"] = {"ms_to_end_time": s.last_ms(), "steps": done, "end_time": t,
+                                      "value": 2048 * done / (s.last_ms() * 1e-3), "unit": METRIC}
+        n = 256
+        x = (np.arange(n) + 0.5) * (2 * math.pi / n)
+        Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+        P = np.zeros((5, n + 2 * g, n + 2 * g, n + 2 * g))
+        inner = (slice(None), slice(g, g + n), slice(g, g + n), slice(g, g + n))
+        P[0][inner[1:]] = 1.0
+        P[1][inner[1:]] = np.sin(X) * np.cos(Y) * np.cos(Z)
+        P[2][inner[1:]] = -np.cos(X) * np.sin(Y) * np.cos(Z)
+        P[4][inner[1:]] = 100 + ((np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2) - 2) / 16
+        del X, Y, Z
+        U0 = fvoracle.prim_to_cons("euler3", (n, n, n), g, 1.4, P.reshape(5, -1))
+        del P
+        with refcuda.Solver("euler3", "hll3", "weno2", "rungekutta3", "periodic", (n, n, n), (0, 0, 0),
+                            (2 * math.pi,) * 3, 1.4, 0.4) as s:
+            s.set_state(U0)
+            s.run(1e9, 0, 1)
+            _, done = s.run(1e9, 0, 2)
+            ms = s.last_ms()
+            out["tg256"] = {"value": n ** 3 * done / (ms * 1e-3), "unit": METRIC, "steps": done,
+                            "ms_per_step": ms / done}
+    except refcuda.RefCudaError as e:
+        out["unavailable"] = str(e)
+    return out
 
 
 def run_gpu(args):
