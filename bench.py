@@ -1043,7 +1043,9 @@ def main():
     ap.add_argument("--headline-fv", type=int, default=1,
                     help="add the Sod 2048 and Taylor-Green 256^3 measurements to the headline line (0: skip)")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=500,
+                    help="timed steps (the default keeps the headline's timed region near one second, "
+                         "so the clock samples fall inside it)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=200)
