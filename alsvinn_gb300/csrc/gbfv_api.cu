@@ -248,6 +248,9 @@ struct gbfv_solver {
     std::vector<double> tune_ms;  // the autotuner's MODE_L time per candidate (-1: not eligible)
     void* op_block = nullptr;     // scratch of the per-variable operator calls (allocated at first use)
     unsigned tma_extra_tx = 0;    // gbfv_test_tma_wait_limit: extra bytes announced on the halo barrier
+    // st_host mirrors st: set after each copy back, cleared while step kernels
+    // may be in flight (an advance skips its opening copy when it is set)
+    bool st_host_valid = false;
     // kGraphSteps time steps captured as one CUDA graph, replayed for the
     // long stretches of an advance (valid for graph_params and graph_cand)
     cudaGraphExec_t step_graph = nullptr;
@@ -364,6 +367,7 @@ int gbfv_create(const gbfv_desc* d, gbfv_solver** out) {
         *s->st_host = z;
         e = cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e == cudaSuccess) s->st_host_valid = true;
     }
     if (e != cudaSuccess) {
         const int code = (e == cudaErrorMemoryAllocation) ? GBFV_ERR_MEMORY : GBFV_ERR_CUDA;
@@ -396,8 +400,10 @@ static int reset_time(gbfv_solver* s) {
     z.number_saved2 = 1;
     z.done = 1;
     *s->st_host = z;
+    s->st_host_valid = false;
     CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof z, cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->st_host_valid = true;
     return GBFV_OK;
 }
 
@@ -664,6 +670,7 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
         const int r = tune(s, false);
         if (r) return r;
     }
+    s->st_host_valid = false;
     begin_kernel<<<1, 1, 0, s->stream>>>(s->st, P.end_time, limit);
     CUDA_TRY(cudaGetLastError());
     s->launches += 1;
@@ -673,7 +680,9 @@ static int drive(gbfv_solver* s, const StepParams& P, long long limit) {
         if (r) return r;
         CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
         CUDA_TRY(cudaStreamSynchronize(s->stream));
+        s->st_host_valid = true;
         if (s->st_host->done) break;
+        s->st_host_valid = false;
         // steps queued after the one that ended the advance return at once
         // (done), leaving the state and the saved mask as that step left them
         if (chunk < 64) chunk *= 2;
@@ -802,10 +811,21 @@ static StepParams step_params(const gbfv_solver* s, double end_time) {
     return P;
 }
 
-int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps) {
-    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+// The host copy of the step state, fetched unless it is current.
+static int sync_step_state(gbfv_solver* s) {
+    if (s->st_host_valid) return GBFV_OK;
     CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->st_host_valid = true;
+    return GBFV_OK;
+}
+
+int gbfv_advance(gbfv_solver* s, double end_time, int number_of_saves, int max_steps) {
+    if (!s) return fail(GBFV_ERR_ARGUMENT, "null solver");
+    {
+        const int r = sync_step_state(s);
+        if (r) return r;
+    }
     const long long limit = max_steps > 0 ? s->st_host->steps + max_steps : -1;
     if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
     StepParams P = step_params(s, end_time);
@@ -818,8 +838,10 @@ int gbfv_advance_schedule(gbfv_solver* s, const gbfv_schedule* sch, int* saved_m
     if (!(sch->save_interval[0] >= 0) || !(sch->save_interval[1] >= 0))
         return fail(GBFV_ERR_ARGUMENT, "save intervals must be non-negative");
     if (saved_mask) *saved_mask = 0;
-    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    {
+        const int r = sync_step_state(s);
+        if (r) return r;
+    }
     const long long steps0 = s->st_host->steps;
     const long long limit = sch->max_steps > 0 ? steps0 + sch->max_steps : -1;
     StepParams P = step_params(s, sch->end_time);
@@ -944,12 +966,15 @@ static int advance_host_mapped(gbfv_solver* s, void* hdev, double end_time, int 
         const int r = tune(s, false);
         if (r) return r;
     }
-    CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    {
+        const int r = sync_step_state(s);
+        if (r) return r;
+    }
     if (!(s->st_host->t < end_time) || s->st_host->status != 0) return 1;
     if (number_of_saves > 0) s->time_interval = end_time / number_of_saves;
     StepParams P = step_params(s, end_time);
     P.time_interval = number_of_saves > 0 ? s->time_interval : 0.0;
+    s->st_host_valid = false;
     begin_kernel<<<1, 1, 0, s->stream>>>(s->st, P.end_time, s->st_host->steps + 1);
     CUDA_TRY(cudaGetLastError());
     s->launches += 1;
@@ -992,6 +1017,7 @@ static int advance_host_mapped(gbfv_solver* s, void* hdev, double end_time, int 
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(StepState), cudaMemcpyDeviceToHost, q));
     CUDA_TRY(cudaStreamSynchronize(q));
+    s->st_host_valid = true;
     if (s->st_host->status == kStatusTmaTimeout) {
         char msg[256];
         snprintf(msg, sizeof msg, "a TMA halo copy did not complete within the time limit (step %d)",
