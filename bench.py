@@ -587,7 +587,7 @@ def measure_tg(n, precision_name, steps, warmup, candidate=-1):
             "roofline": {"bound": "hbm", "achieved": alg / (launch_ms * 1e-3) / 1e9, "peak": peak[0], "unit": "GB/s",
                          "frac": alg / (launch_ms * 1e-3) / 1e9 / peak[0], "alg_bytes_per_launch": alg,
                          "peak_source": peak[1],
-                         "note": "FP64 builds are FP64-pipe bound (77 %% of the pipe, "
+                         "note": "FP64 builds are FP64-pipe bound (75 % of the pipe, "
                                  "profiles/stage_kernel_tg128_fp64.md)" if elem == 8 else
                                  "FP32: arithmetic-bound stencil"},
             "clocks": clocks.summary()}
