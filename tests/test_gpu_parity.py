@@ -366,6 +366,60 @@ def test_advance_host_in_place_equals_device_path(cuda_device, precision, integr
         assert np.array_equal(Um, before) and mapped.time() == dev.time()
 
 
+def test_interleaved_calls_keep_the_step_state(cuda_device):
+    """The solver keeps its host copy of the step state and skips the opening
+    copy of an advance when no step ran since. Advances mixed with state
+    reads and writes (a write restarts the clock), time queries, in-place
+    host steps and a restart from initial data give the same states, times
+    and step counts as the same steps taken by plain advances; an advance to
+    a time already passed changes nothing."""
+    import torch
+    case = LARGE["kh128_50"]
+    prim = case["prim"]()
+
+    def make():
+        s = lib.Solver(case["equation"], case["flux"], case["recon"], "rungekutta3", "periodic", case["n"],
+                       (0, 0, 0), case["upper"], cfl=case["cfl"], precision=lib.FP64)
+        s.set_primitive(prim)
+        return s
+
+    with make() as ref, make() as s:
+        ref.advance(1.0, 0, 2)
+        ref.set_state(ref.get_state())
+        ref.advance(1.0, 0, 3)
+        ref.set_state(ref.get_state())
+        ref.advance(1.0, 0, 7)
+        s.advance(1.0, 0, 2)
+        s.time()
+        s.set_state(s.get_state())
+        s.advance(1.0, 0, 1)
+        pinned = torch.empty((s.nvar, s.total), dtype=torch.float64).pin_memory()
+        Um = pinned.numpy()
+        Um[...] = s.get_state()
+        s.advance_host(Um, 1.0, 0, 1)  # in place over mapped memory
+        s.time()
+        s.advance_host(Um, 1.0, 0, 1)
+        assert np.array_equal(s.get_state(), Um)
+        s.set_state(Um)
+        s.advance(1.0, 0, 4)
+        s.time()
+        s.time()
+        s.advance(1.0, 0, 3)
+        assert s.time() == ref.time()
+        assert np.array_equal(s.get_state(), ref.get_state())
+    with make() as ref, make() as s:
+        ref.advance(1.0, 0, 9)
+        s.advance(1.0, 0, 5)
+        s.set_primitive(prim)  # restart: time and step count back to zero
+        assert s.time()[:2] == (0.0, 0)
+        for _ in range(9):
+            s.advance(1.0, 0, 1)
+        assert s.time() == ref.time() and np.array_equal(s.get_state(), ref.get_state())
+        t_now = s.time()
+        s.advance(t_now[0] * 0.5, 0, 5)
+        assert s.time() == t_now and np.array_equal(s.get_state(), ref.get_state())
+
+
 def test_constraint_violation_is_reported(cuda_device):
     prim = workloads.sod_prim(64)
     prim[2, 30] = -1.0
