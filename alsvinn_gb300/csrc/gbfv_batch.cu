@@ -98,16 +98,24 @@ __global__ void batch_begin_kernel(StepState* st, const MemberParam* mp, int M, 
 // statistics save a member is folded when it reaches end_time; with nsaves
 // saves (FixedIntervalStatistics at (k + 1) end_time / nsaves) it is folded
 // into accumulator (group, k) at each save k its clamp stopped it at.
-// list[i] = (member, accumulator, count after the fold). One warp: the lanes
-// read 32 members' flags at a time, lane 0 numbers the (few) folds in order.
-__global__ void batch_assign_kernel(StepState* st, const MemberParam* mp, int M, GroupAcc* accs, int nacc,
-                                    int nsaves, int4* list, int* nlist) {
-    const int lane = threadIdx.x;
-    int m = 0;
-    for (int base = 0; base < M; base += 32) {
-        const int s = base + lane;
-        int a = -1;
-        if (s < M) {
+// list[i] = (member, accumulator, count after the fold). All threads read the
+// members' flags in parallel; one warp then numbers the (few) folds in order.
+constexpr int kAssignThreads = 1024;
+constexpr int kAssignChunk = 4096;
+__global__ void __launch_bounds__(kAssignThreads) batch_assign_kernel(StepState* st, const MemberParam* mp, int M,
+                                                                      GroupAcc* accs, int nacc, int nsaves,
+                                                                      int4* list, int* nlist) {
+    // every thread: the accumulator index of members of the chunk (and their
+    // flags cleared); then warp 0 compacts the list in member order, so the
+    // counts each group's members receive follow the member order
+    __shared__ int acc_of[kAssignChunk];
+    __shared__ int m_shared;
+    if (threadIdx.x == 0) m_shared = 0;
+    for (int base0 = 0; base0 < M; base0 += kAssignChunk) {
+        const int len = min(kAssignChunk, M - base0);
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+            const int s = base0 + i;
+            int a = -1;
             const int done = st[s].just_done;
             const int saved = st[s].just_saved;
             if (done || saved >= 0) {
@@ -122,19 +130,30 @@ __global__ void batch_assign_kernel(StepState* st, const MemberParam* mp, int M,
                 const int g = st[s].group;
                 if (k >= 0 && k < nsaves && g >= 0 && g * nsaves + k < nacc) a = g * nsaves + k;
             }
+            acc_of[i] = a;
         }
-        unsigned mask = __ballot_sync(0xffffffffu, a >= 0);
-        while (mask) {
-            const int l = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int al = __shfl_sync(0xffffffffu, a, l);
-            if (lane == 0 && accs[al].mean) {
-                accs[al].count += 1;
-                list[m++] = make_int4(base + l, al, (int)accs[al].count, 0);
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            int m = m_shared;
+            for (int b = 0; b < len; b += 32) {
+                const int a = b + lane < len ? acc_of[b + lane] : -1;
+                unsigned mask = __ballot_sync(0xffffffffu, a >= 0);
+                while (mask) {
+                    const int l = __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    const int al = __shfl_sync(0xffffffffu, a, l);
+                    if (lane == 0 && accs[al].mean) {
+                        accs[al].count += 1;
+                        list[m++] = make_int4(base0 + b + l, al, (int)accs[al].count, 0);
+                    }
+                }
             }
+            if (lane == 0) m_shared = m;
         }
+        __syncthreads();
     }
-    if (lane == 0) *nlist = m;
+    if (threadIdx.x == 0) *nlist = m_shared;
 }
 
 template <class R>
@@ -361,8 +380,9 @@ int enqueue_batch_step(gbfv_batch* b) {
     if (r) return bfail(GBFV_ERR_CUDA, std::string("batch stage: ") + cudaGetErrorString((cudaError_t)r));
     batch_finish_kernel<<<mb, 128, 0, q>>>(b->d_states, b->d_params, M, p.in == 1 ? 1 : 0);
     if (!b->groups.empty()) {
-        batch_assign_kernel<<<1, 32, 0, q>>>(b->d_states, b->d_params, M, b->d_groups, (int)b->groups.size(),
-                                             b->stats_saves, b->d_list, b->d_nlist);
+        batch_assign_kernel<<<1, kAssignThreads, 0, q>>>(b->d_states, b->d_params, M, b->d_groups,
+                                                          (int)b->groups.size(), b->stats_saves, b->d_list,
+                                                          b->d_nlist);
         const long long cells = b->stats_cells;
         unsigned nb = (unsigned)std::min<long long>((cells + 255) / 256, 152 * 8);
         if (b->scheme.elem == 8)
