@@ -1029,7 +1029,8 @@ def main():
     ap.add_argument("--uq-error-members", type=int, default=8, help="members per grid size of --workload uq-error")
     ap.add_argument("--serve-requests", type=int, default=128)
     ap.add_argument("--serve-rate", type=float, default=2.0)
-    ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--serve-chunk", type=int, default=256,
+                    help="time steps per ensemble advance between admissions (larger chunks: fewer host round trips)")
     ap.add_argument("--serve-plain", type=int, default=12,
                     help="requests of the stream also run by plain FP64 one at a time")
     ap.add_argument("--uq-samples", type=int, default=4096)
