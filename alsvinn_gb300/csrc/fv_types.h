@@ -86,7 +86,10 @@ struct StepParams {
 // warps waiting at the next barrier). Threads past the tile's cells join the
 // reconstruction and flux phases only.
 template <int DIM, int VAR> struct TileShape;
-template <int VAR> struct TileShape<1, VAR> { static constexpr int X = 128, Y = 1, Z = 1, THREADS = 128; };
+// (1D: 160 threads for 128 cells, so the 130 reconstructions and 129 faces of
+// a tile take one pass of the threads; on small grids the stage time is the
+// per-thread chain of FP64 instructions, which a second pass would double)
+template <int VAR> struct TileShape<1, VAR> { static constexpr int X = 128, Y = 1, Z = 1, THREADS = 160; };
 template <int VAR> struct TileShape<2, VAR> { static constexpr int X = 32, Y = 8, Z = 1, THREADS = 256; };
 template <> struct TileShape<2, 3> { static constexpr int X = 16, Y = 12, Z = 1, THREADS = 256; };
 template <int VAR> struct TileShape<3, VAR> { static constexpr int X = 8, Y = 8, Z = 4, THREADS = 256; };

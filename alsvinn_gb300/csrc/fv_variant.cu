@@ -301,9 +301,10 @@ template <int FLUX, int DIM>
 static void reg_tuned(Registry& R) {
     constexpr int E = FV_EQ, RC = RC_WENO2;
     if constexpr (DIM == 1) {
-        Cand<E, FLUX, RC, 1, 128, 1, 1, 128, true>::add(R, FLUX, RC);
-        Cand<E, FLUX, RC, 1, 64, 1, 1, 64, true>::add(R, FLUX, RC);
-        Cand<E, FLUX, RC, 1, 32, 1, 1, 32, true>::add(R, FLUX, RC);
+        // threads >= tile + 2: reconstructions and faces in one pass
+        Cand<E, FLUX, RC, 1, 128, 1, 1, 160, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 1, 64, 1, 1, 96, true>::add(R, FLUX, RC);
+        Cand<E, FLUX, RC, 1, 32, 1, 1, 64, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 1, 240, 1, 1, 256, true>::add(R, FLUX, RC);
     } else if constexpr (DIM == 2) {
         Cand<E, FLUX, RC, 2, 32, 8, 1, 256, true, 3>::add(R, FLUX, RC);
