@@ -321,6 +321,9 @@ static void reg_tuned(Registry& R) {
         Cand<E, FLUX, RC, 3, 16, 8, 4, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 3, 8, 8, 8, 256, true>::add(R, FLUX, RC);
         Cand<E, FLUX, RC, 3, 16, 16, 2, 256, true>::add(R, FLUX, RC);
+        // the default tile on 384 threads (its 320 / 320 / 384 reconstructions
+        // and 288 / 288 / 320 faces per direction in one pass), two CTAs per SM
+        Cand<E, FLUX, RC, 3, 8, 8, 4, 384, false, 2>::add(R, FLUX, RC);
     }
 }
 #endif
